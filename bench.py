@@ -1,0 +1,414 @@
+#!/usr/bin/env python
+"""Benchmark of the HydroThermal3D pseudo-transient hot path on GB300.
+
+Workload: the dimensionless Horton-Rogers-Lapwood convection problem
+(Ra = 1000, unit cube, T linear 1 -> 0 plus a seeded 1e-3 perturbation,
+DYREL tolerance 1e-8, WENO5 advection, adaptive dt) at 255^3 cells.
+A step is one full time step: thermal DYREL solve, Darcy DYREL solve,
+Darcy velocity, WENO5 advection, dt update.
+
+Metric: T_eff (GB/s) = algorithmic bytes / wall time, where a DYREL
+pseudo-iteration counts 9*N*s bytes and a WENO5 advection 21*N*s bytes
+(s = storage width: 4 B for the mixed form, 8 B for FP64).  `value` is the
+mixed-precision form; the FP64 form, time-steps/s and the mixed-vs-FP64 error
+are reported beside it.
+
+  python bench.py [--steps K] [--warmup W] [--n 255] [--impl reference]
+Under torchrun with N > 1 every rank runs an independent replica on its own
+GPU (the path has no exchange step); value = all ranks' bytes / max time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "T_eff GB/s & time-steps/s at 255^3: FP32-mixed vs FP64 GPU at 1e-6 rel err in T"
+UNIT = "GB/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=255)
+    ap.add_argument("--nitout", type=int, default=1000)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--skip-fp64", action="store_true")
+    return ap.parse_args()
+
+
+def workload_config(a, extra=None):
+    c = {"workload": f"HRL porous convection {a.n}^3 (Ra=1000, DYREL tol 1e-8, nitout {a.nitout}, WENO5 v1, adaptive dt)",
+         "cells": a.n ** 3, "Ra": 1000.0, "dyrel_tol": 1e-8, "nitout": a.nitout,
+         "l2_policy": "inputs larger than L2 (each 255^3 FP64 field is 133 MB > 129 MB L2)",
+         "parallelism": f"replicas x{a.gpus}"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """Samples nvidia-smi SM clocks and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 6:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = max(mx, float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[2:6]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ distributed
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def reduce_max_sum(ws, t, units):
+    from hydrothermal3d_gb300.replicas import max_time_sum_units
+    return max_time_sum_units(t, units) if ws > 1 else (t, units)
+
+
+# ------------------------------------------------------------------ CPU baseline
+def cpu_sample(n, seconds, threads=None):
+    """Time the oracle (unfused FP64, OpenMP over z) on a bounded sample of the
+    workload: DYREL pseudo-iterations of both solves plus WENO5 advections at
+    the same grid.  Returns (T_eff GB/s, cores, description)."""
+    import oracle
+    from hydrothermal3d_gb300 import hrl, abi
+    if threads:
+        oracle.set_threads(threads)
+    cores = oracle.num_threads()
+    T, P, ktv, kfv = hrl.initial_fields(n, n, n, seed=1)
+    nx = ny = nz = n
+    d = 1.0 / n
+    R = np.asfortranarray(-T[1:-1, 1:-1, 1:-1] / (d * d / 6.1))
+    k = [np.ones(s, order="F") for s in ((nx + 1, ny, nz), (nx, ny + 1, nz), (nx, ny, nz + 1))]
+    F, F0 = oracle.zeros(nx, ny, nz), oracle.zeros(nx, ny, nz)
+    V = [np.asfortranarray(np.random.default_rng(2).uniform(-1, 1, s)) for s in ((nx + 1, ny, nz), (nx, ny + 1, nz), (nx, ny, nz + 1))]
+    prm = abi.DyrelParams.reference(nitout=1000)
+    tb = oracle.int6(0, 0, 1, 1, 0, 0)
+    tv = oracle.dbl6(0, 0, 1, 0, 0, 0)
+    iters, adv, t_tot = 0, 0, 0.0
+    chunk = 10
+    while t_tot < seconds or iters == 0:
+        t0 = time.perf_counter()
+        oracle.dyrel_solve_dimless(T, R, *k, 6.1 / (d * d), d, d, d, [0, 0, 1, 1, 0, 0], [0, 0, 1, 0, 0, 0], prm, F, F0,
+                                   n_iter_fixed=chunk)
+        oracle.dyrel_solve_dimless(P, R, *k, 0.0, d, d, d, [0] * 6, [0.0] * 6, prm, F, F0, n_iter_fixed=chunk)
+        oracle.call("AdvectWithWeno5_v1", T, *V, 1e-4, float(n), float(n), float(n), tb, tv, nx, ny, nz)
+        t_tot += time.perf_counter() - t0
+        iters += 2 * chunk
+        adv += 1
+    nbytes = iters * hrl.bytes_per_iteration(n, n, n, 8) + adv * hrl.bytes_per_advection(n, n, n, 8)
+    desc = (f"oracle FP64 at {n}^3: {iters} DYREL pseudo-iterations (thermal+Darcy, incl. per-solve Gershgorin set-up)"
+            f" + {adv} WENO5 advections in {t_tot:.1f} s")
+    return nbytes / t_tot / 1e9, cores, desc, t_tot
+
+
+def run_reference(a):
+    ws, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    cores = os.cpu_count()
+    vals = []
+    for s in range(a.warmup + a.steps):
+        v, cores, desc, _ = cpu_sample(a.n, max(2.0, a.cpu_seconds / 4), threads=os.cpu_count())
+        if s >= a.warmup:
+            vals.append(v)
+    value = float(np.mean(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
+            "warmup": a.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded HRL initial condition)",
+            "config": workload_config(a, {"reference_impl": "CPU oracle port (reference is Julia; not runnable here)"}),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ------------------------------------------------------------------ GPU arm
+def run_ours(a):
+    import torch
+    import hydrothermal3d_gb300 as ht
+    from hydrothermal3d_gb300 import api, abi, hrl
+
+    ws, rank, local = dist_setup()
+    dev = local if torch.cuda.is_available() else 0
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream()
+    ctx = ht.Context(device=dev, stream=stream.cuda_stream)
+    n = a.n
+    N = n ** 3
+    T0, P0, ktv, kfv = hrl.initial_fields(n, n, n, seed=1)
+    ktd, kfd = ht.from_numpy(ktv), ht.from_numpy(kfv)
+    Vd = [ht.zeros(n + 1, n, n), ht.zeros(n, n + 1, n), ht.zeros(n, n, n + 1)]
+    torch.cuda.synchronize()
+
+    def run_form(prec, steps, warmup, sampler=None):
+        Td, Pd = ht.from_numpy(T0), ht.from_numpy(P0)
+        p = hrl.params(n, n, n, nitout=a.nitout)
+        s = 8 if prec == abi.FP64 else 4
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                api.step_hrl(ctx, Td, Pd, ktd, kfd, *Vd, p, prec)
+            torch.cuda.synchronize()
+            barrier(ws)
+            l0 = ctx.launches
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            iters, nbytes = [], 0
+            cm = sampler if sampler is not None else _Null()
+            with cm:
+                e0.record(stream)
+                for _ in range(steps):
+                    gt, gd = api.step_hrl(ctx, Td, Pd, ktd, kfd, *Vd, p, prec)
+                    iters.append((gt.iters, gd.iters))
+                    nbytes += (gt.iters + gd.iters) * hrl.bytes_per_iteration(n, n, n, s) + hrl.bytes_per_advection(n, n, n, s)
+                e1.record(stream)
+                torch.cuda.synchronize()
+            barrier(ws)
+            ms = e0.elapsed_time(e1)
+        return dict(ms=ms, bytes=nbytes, iters=iters, launches=ctx.launches - l0, T=Td, P=Pd)
+
+    sampler = ClockSampler(dev)
+    mixed = run_form(abi.MIXED, a.steps, a.warmup, sampler)
+    fp64 = None if a.skip_fp64 else run_form(abi.FP64, a.steps, a.warmup)
+    t_mixed, b_mixed = reduce_max_sum(ws, mixed["ms"] / 1e3, mixed["bytes"])
+    value = b_mixed / t_mixed / 1e9
+    steps_per_s = a.steps * ws / t_mixed
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
+           "ms_per_step": mixed["ms"] / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32+f64 (mixed)", "data": "synthetic (seeded HRL initial condition)",
+           "config": workload_config(a), "time_steps_per_s": steps_per_s,
+           "pseudo_iterations_per_step": [list(x) for x in mixed["iters"]], "gpu_launches": mixed["launches"]}
+    if fp64 is not None:
+        t64, b64 = reduce_max_sum(ws, fp64["ms"] / 1e3, fp64["bytes"])
+        out["fp64"] = {"T_eff_GBs": b64 / t64 / 1e9, "time_steps_per_s": a.steps * ws / t64,
+                       "ms_per_step": fp64["ms"] / a.steps,
+                       "pseudo_iterations_per_step": [list(x) for x in fp64["iters"]]}
+        out["mixed_vs_fp64_time_steps_speedup"] = steps_per_s / out["fp64"]["time_steps_per_s"]
+        inner = (slice(1, -1),) * 3
+        Tm, T6 = mixed["T"][inner], fp64["T"][inner]
+        Pm, P6 = mixed["P"][inner], fp64["P"][inner]
+        Pm, P6 = Pm - Pm.mean(), P6 - P6.mean()
+        out["mixed_error_vs_fp64_gpu"] = {
+            "T_rel_maxnorm": float((Tm - T6).abs().max() / T6.abs().max()),
+            "P_rel_maxnorm_mean_removed": float((Pm - P6).abs().max() / P6.abs().max()),
+            "after_steps": a.warmup + a.steps}
+    out["clocks"] = sampler.summary()
+
+    # --- roofline of the dominant kernel: the FP32 fused DYREL iteration
+    out["roofline"] = roofline(ctx, stream, n)
+
+    # --- end to end through the public API with host buffers (mixed form)
+    out["e2e"] = e2e(ctx, stream, a, ktd, kfd, Vd)
+
+    if rank == 0:
+        v, cores, desc, _ = cpu_sample(n, a.cpu_seconds, threads=os.cpu_count())
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc}
+    if rank == 0:
+        print(json.dumps(out))
+    ctx.close()
+
+
+class _Null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *e):
+        return False
+
+
+def roofline(ctx, stream, n, iters=40):
+    import torch
+    import hydrothermal3d_gb300 as ht
+    from hydrothermal3d_gb300 import abi, hrl
+    N = n ** 3
+    f32 = torch.float32
+    X = ht.zeros(n + 2, n + 2, n + 2, dtype=f32)
+    X.uniform_(0, 1)
+    R = ht.zeros(n, n, n, dtype=f32)
+    R.uniform_(-1, 1)
+    k = [ht.ones(n + 1, n, n, dtype=f32), ht.ones(n, n + 1, n, dtype=f32), ht.ones(n, n, n + 1, dtype=f32)]
+    iPC = ht.ones(n, n, n, dtype=f32) * (1.0 / (6 * n * n))
+    F0 = ht.zeros(n, n, n, dtype=f32)
+    bt, bv = abi.int6(0, 0, 1, 1, 0, 0), abi.dbl6(0, 0, 1, 0, 0, 0)
+    d = 1.0 / n
+    args = lambda m: (X.data_ptr(), R.data_ptr(), k[0].data_ptr(), k[1].data_ptr(), k[2].data_ptr(), iPC.data_ptr(),
+                      F0.data_ptr(), 0.0, d, d, d, bt, bv, 0.99, 0.05, 0.01, m, n, n, n)
+    torch.cuda.synchronize()
+    ctx.call("ht3d_dyrel_iterate_f32", *args(4))
+    ctx.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ctx.call("ht3d_dyrel_iterate_f32", *args(iters))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3 / iters
+    alg = hrl.bytes_per_iteration(n, n, n, 4)
+    peak = measured_peak()
+    achieved = alg / t / 1e9
+    res = {"kernel": "k_dyrel_iter<float,PLAIN> (mixed-form pseudo-iteration)", "bound": "hbm",
+           "achieved": achieved, "peak": peak[0], "unit": "GB/s", "frac": achieved / peak[0], "peak_source": peak[1],
+           "traffic": profile_traffic("dyrel_iter_f32"), "us_per_launch": t * 1e6,
+           "alg_bytes_per_launch": alg}
+    # FP64 form's kernel for comparison (FP64-ALU bound on GB300)
+    X64 = X.double()
+    R64, k64, iPC64, F064 = R.double(), [a.double() for a in k], iPC.double(), F0.double()
+    X64c = ht.zeros(n + 2, n + 2, n + 2)
+    X64c.copy_(X64)
+    R64c = ht.zeros(n, n, n); R64c.copy_(R64)
+    k64c = [ht.zeros(*a.shape) for a in k64]
+    for a, b in zip(k64c, k64):
+        a.copy_(b)
+    iPCc = ht.zeros(n, n, n); iPCc.copy_(iPC64)
+    F0c = ht.zeros(n, n, n)
+    a64 = lambda m: (X64c.data_ptr(), R64c.data_ptr(), k64c[0].data_ptr(), k64c[1].data_ptr(), k64c[2].data_ptr(),
+                     iPCc.data_ptr(), F0c.data_ptr(), 0.0, d, d, d, bt, bv, 0.99, 0.05, 0.01, m, n, n, n)
+    torch.cuda.synchronize()
+    ctx.call("ht3d_dyrel_iterate", *a64(2))
+    ctx.synchronize()
+    e0.record(stream)
+    ctx.call("ht3d_dyrel_iterate", *a64(iters // 2))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t64 = e0.elapsed_time(e1) / 1e3 / (iters // 2)
+    alg64 = hrl.bytes_per_iteration(n, n, n, 8)
+    res["fp64_kernel"] = {"kernel": "k_dyrel_iter<double,PLAIN>", "us_per_launch": t64 * 1e6,
+                          "achieved_GBs": alg64 / t64 / 1e9, "frac_hbm": alg64 / t64 / 1e9 / peak[0],
+                          "fp64_alu_nominal_tflops": 1.25}
+    return res
+
+
+def e2e(ctx, stream, a, ktd, kfd, Vd):
+    import torch
+    import hydrothermal3d_gb300 as ht
+    from hydrothermal3d_gb300 import api, abi, hrl
+    n = a.n
+    T0, P0, _, _ = hrl.initial_fields(n, n, n, seed=1)
+    hT = torch.from_numpy(np.ascontiguousarray(T0.transpose(2, 1, 0))).pin_memory()
+    hP = torch.from_numpy(np.ascontiguousarray(P0.transpose(2, 1, 0))).pin_memory()
+    Td, Pd = ht.zeros(n + 2, n + 2, n + 2), ht.zeros(n + 2, n + 2, n + 2)
+    p = hrl.params(n, n, n, nitout=a.nitout)
+    nbytes = 0
+    with torch.cuda.stream(stream):
+        for w in range(2):  # warm-up of the copy path
+            Td.permute(2, 1, 0).copy_(hT, non_blocking=True)
+            hT.copy_(Td.permute(2, 1, 0), non_blocking=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(a.steps):
+            Td.permute(2, 1, 0).copy_(hT, non_blocking=True)
+            Pd.permute(2, 1, 0).copy_(hP, non_blocking=True)
+            gt, gd = api.step_hrl(ctx, Td, Pd, ktd, kfd, *Vd, p, abi.MIXED)
+            hT.copy_(Td.permute(2, 1, 0), non_blocking=True)
+            hP.copy_(Pd.permute(2, 1, 0), non_blocking=True)
+            stream.synchronize()
+            nbytes += (gt.iters + gd.iters) * hrl.bytes_per_iteration(n, n, n, 4) + hrl.bytes_per_advection(n, n, n, 4)
+        t = time.perf_counter() - t0
+    per = 2 * (n + 2) ** 3 * 8
+    return {"value": nbytes / t / 1e9, "unit": UNIT, "h2d_bytes_per_step": per, "d2h_bytes_per_step": per,
+            "time_steps_per_s": a.steps / t, "note": "host-timed; pinned host T,P copied in and out every step"}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    except Exception:
+        return 6800.0, "fallback 6.8 TB/s"
+
+
+def profile_traffic(name):
+    """DRAM bytes per launch from the committed ncu summary, if one exists."""
+    p = os.path.join(ROOT, "profiles", f"{name}.md")
+    try:
+        with open(p) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch_at_255:"):
+                    return float(line.split(":", 1)[1].split()[0])
+    except Exception:
+        pass
+    return None
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,87 @@
+"""ctypes mirrors of the parameter structs and constants of include/ht3d.h."""
+import ctypes
+
+OK = 0
+ERR_ARG, ERR_CUDA, ERR_NAN, ERR_DIVERGED, ERR_MAXITER, ERR_TIMEOUT, ERR_NOMEM = 1, 2, 3, 4, 5, 6, 7
+FP64, MIXED = 0, 1
+BC_NEUMANN, BC_DIRICHLET, BC_PERIODIC = 0, 1, 2
+WENO_V1, WENO_V2_REF, WENO_V2_FIXED = 0, 1, 2
+RED_SUM, RED_SUM_ABS, RED_MAX, RED_MIN, RED_MAX_ABS = 0, 1, 2, 3, 4
+
+
+class DyrelParams(ctypes.Structure):
+    """ht3d_dyrel_params: DYREL controls of Dimensional/HydroThermal3D_v18.jl:292-303,433-439."""
+    _fields_ = [
+        ("tol_abs", ctypes.c_double),
+        ("tol_rel", ctypes.c_double),
+        ("nitmax", ctypes.c_int),
+        ("nitout", ctypes.c_int),
+        ("cfl", ctypes.c_double),
+        ("cfact", ctypes.c_double),
+        ("lmin_ratio", ctypes.c_double),
+        ("norm_scale", ctypes.c_double),
+    ]
+
+    @classmethod
+    def reference(cls, tol=1e-8, nitmax=10000, nitout=1000, norm_scale=1.0):
+        """The reference's values: CFL 0.99, cfact 0.5, lambda_min = lambda_max/500."""
+        return cls(tol_abs=tol, tol_rel=tol, nitmax=nitmax, nitout=nitout, cfl=0.99, cfact=0.5, lmin_ratio=500.0,
+                   norm_scale=norm_scale)
+
+
+class DyrelStats(ctypes.Structure):
+    _fields_ = [
+        ("iters", ctypes.c_int),
+        ("converged", ctypes.c_int),
+        ("status", ctypes.c_int),
+        ("checks", ctypes.c_int),
+        ("nF_abs", ctypes.c_double),
+        ("nF_rel", ctypes.c_double),
+        ("nF_ini", ctypes.c_double),
+        ("lambda_min", ctypes.c_double),
+        ("lambda_max", ctypes.c_double),
+        ("h1", ctypes.c_double),
+        ("h2", ctypes.c_double),
+        ("dtau", ctypes.c_double),
+    ]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+Int6 = ctypes.c_int * 6
+Dbl6 = ctypes.c_double * 6
+
+
+class HrlParams(ctypes.Structure):
+    """ht3d_hrl_params: one time step of the dimensionless HRL model."""
+    _fields_ = [
+        ("Ra", ctypes.c_double),
+        ("dx", ctypes.c_double),
+        ("dy", ctypes.c_double),
+        ("dz", ctypes.c_double),
+        ("dt", ctypes.c_double),
+        ("Tbot", ctypes.c_double),
+        ("Ttop", ctypes.c_double),
+        ("thermal_bc", Int6),
+        ("thermal_val", Dbl6),
+        ("darcy_bc", Int6),
+        ("darcy_val", Dbl6),
+        ("weno_bc", Int6),
+        ("weno_val", Dbl6),
+        ("weno_variant", ctypes.c_int),
+        ("kill_ns", ctypes.c_int),
+        ("dt_adapt", ctypes.c_int),
+        ("advection", ctypes.c_int),
+        ("dt_fact", ctypes.c_double),
+        ("thermal", DyrelParams),
+        ("darcy", DyrelParams),
+    ]
+
+
+def int6(*v):
+    return Int6(*v)
+
+
+def dbl6(*v):
+    return Dbl6(*[float(x) for x in v])

@@ -1,0 +1,387 @@
+"""Host-side mirror of the reference's ParallelStencil kernel interface.
+
+Every function here has the name of the reference kernel it replaces (without
+the trailing ``!``; ``ρ``/``ϕ`` spelled ``Rho``/``Phi``), takes the same
+arguments in the same order, mutates its output arrays in place and returns
+``None`` -- so a driver line ``@parallel ComputeFlux!(qx, qy, qz, kx, ky, kz,
+A, _dx, _dy, _dz)`` becomes ``ComputeFlux(ctx, qx, qy, qz, kx, ky, kz, A, _dx,
+_dy, _dz)``.  Arrays are CUDA float64 torch tensors in the reference's
+column-major layout (see :func:`zeros`); grid sizes are inferred from the
+array shapes exactly like ParallelStencil infers its launch range.
+
+Errors: a bad shape/dtype raises ``ValueError`` before anything is launched; a
+non-zero status from libht3d raises :class:`Ht3dError`.
+"""
+import ctypes
+
+import torch
+
+from . import _lib
+from . import abi
+
+
+class Ht3dError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"libht3d status {status} ({msg})")
+        self.status = status
+
+
+class Context:
+    """Owns one ht3d_ctx (one CUDA stream; scratch memory)."""
+
+    def __init__(self, device=0, stream=None, sync=True):
+        self.lib = _lib.load()
+        self.ptr = ctypes.c_void_p()
+        s = 0 if stream is None else int(stream)
+        st = self.lib.ht3d_ctx_create(ctypes.byref(self.ptr), int(device), s)
+        if st != abi.OK:
+            raise Ht3dError(st, self.lib.ht3d_status_string(st).decode())
+        self.device = device
+        if not sync:
+            self.lib.ht3d_ctx_set_sync(self.ptr, 0)
+
+    def check(self, st):
+        if st != abi.OK:
+            msg = self.lib.ht3d_status_string(st).decode()
+            detail = self.lib.ht3d_ctx_last_error(self.ptr).decode()
+            raise Ht3dError(st, f"{msg}: {detail}" if detail else msg)
+
+    def call(self, name, *args):
+        self.check(getattr(self.lib, name)(self.ptr, *args))
+
+    def synchronize(self):
+        self.check(self.lib.ht3d_ctx_synchronize(self.ptr))
+
+    @property
+    def launches(self):
+        return int(self.lib.ht3d_ctx_launch_count(self.ptr))
+
+    def close(self):
+        if self.ptr:
+            self.lib.ht3d_ctx_destroy(self.ptr)
+            self.ptr = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# --------------------------------------------------------------- arrays
+def zeros(n1, n2, n3=1, dtype=torch.float64, device="cuda"):
+    """@zeros(n1,n2,n3): column-major (x fastest) tensor of shape (n1,n2,n3)."""
+    return torch.zeros((n3, n2, n1), dtype=dtype, device=device).permute(2, 1, 0)
+
+
+def ones(n1, n2, n3=1, dtype=torch.float64, device="cuda"):
+    return torch.ones((n3, n2, n1), dtype=dtype, device=device).permute(2, 1, 0)
+
+
+def from_numpy(a, device="cuda"):
+    """Copy a numpy array (any order) into a column-major device tensor."""
+    import numpy as np
+    a = np.asarray(a, dtype=np.float64)
+    if a.ndim == 2:
+        a = a[:, :, None]
+    t = zeros(*a.shape, device=device)
+    t.copy_(torch.from_numpy(np.ascontiguousarray(a.transpose(2, 1, 0))).permute(2, 1, 0))
+    return t
+
+
+def to_numpy(t):
+    """Device tensor -> Fortran-ordered numpy array of the same shape."""
+    import numpy as np
+    return np.asfortranarray(t.detach().permute(2, 1, 0).contiguous().cpu().numpy().transpose(2, 1, 0))
+
+
+def _ptr(t, shape=None, name="array"):
+    if not isinstance(t, torch.Tensor):
+        raise ValueError(f"{name}: expected a torch tensor")
+    if t.dtype != torch.float64 or not t.is_cuda:
+        raise ValueError(f"{name}: expected a CUDA float64 tensor, got {t.dtype} on {t.device}")
+    if t.dim() == 2:
+        n1, n2 = t.shape
+        ok = t.stride() == (1, n1)
+        s = (n1, n2)
+    else:
+        n1, n2, n3 = t.shape
+        ok = t.stride() == (1, n1, n1 * n2)
+        s = (n1, n2, n3)
+    if not ok:
+        raise ValueError(f"{name}: expected a column-major (x fastest) contiguous tensor (use hydrothermal3d_gb300.zeros)")
+    if shape is not None and tuple(shape) != s:
+        raise ValueError(f"{name}: shape {s} does not match the staggering {tuple(shape)}")
+    return t.data_ptr()
+
+
+def _cells_ex(A, name="A"):
+    if A.dim() != 3:
+        raise ValueError(f"{name}: expected a 3-D ghosted array")
+    nx, ny, nz = (int(s) - 2 for s in A.shape)
+    return nx, ny, nz
+
+
+def _cells(A):
+    return tuple(int(s) for s in A.shape)
+
+
+def _shapes(nx, ny, nz):
+    return dict(c=(nx, ny, nz), ex=(nx + 2, ny + 2, nz + 2), fx=(nx + 1, ny, nz), fy=(nx, ny + 1, nz),
+                fz=(nx, ny, nz + 1), v=(nx + 1, ny + 1, nz + 1), xxx=(nx + 6, ny + 6, nz + 6))
+
+
+def _numel(t):
+    return int(t.numel())
+
+
+# ------------------------------------------------- dimensionless kernels
+def Init_vel(ctx, Vx, Vy, Vz, kx, ky, kz, Pc_ex, Ty, Ra, _dx, _dy, _dz):
+    nx, ny, nz = _cells_ex(Pc_ex, "Pc_ex"); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_Init_vel", _ptr(Vx, S["fx"], "Vx"), _ptr(Vy, S["fy"], "Vy"), _ptr(Vz, S["fz"], "Vz"),
+             _ptr(kx, S["fx"], "kx"), _ptr(ky, S["fy"], "ky"), _ptr(kz, S["fz"], "kz"), _ptr(Pc_ex, S["ex"]),
+             _ptr(Ty, S["fy"], "Ty"), Ra, _dx, _dy, _dz, nx, ny, nz)
+
+
+def InitDarcy(ctx, Ty, kx, ky, kz, Tc_ex, kfv, _dt):
+    nx, ny, nz = _cells_ex(Tc_ex, "Tc_ex"); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_InitDarcy", _ptr(Ty, S["fy"], "Ty"), _ptr(kx, S["fx"], "kx"), _ptr(ky, S["fy"], "ky"),
+             _ptr(kz, S["fz"], "kz"), _ptr(Tc_ex, S["ex"]), _ptr(kfv, S["v"], "kfv"), _dt, nx, ny, nz)
+
+
+def Compute_Rp(ctx, Rp, ky, Ty, Ra, _dy):
+    nx, ny, nz = _cells(Rp); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_Compute_Rp", _ptr(Rp, S["c"], "Rp"), _ptr(ky, S["fy"], "ky"), _ptr(Ty, S["fy"], "Ty"), Ra, _dy,
+             nx, ny, nz)
+
+
+def InitThermal(ctx, Rt, kx, ky, kz, Tc_ex, ktv, _dt):
+    nx, ny, nz = _cells_ex(Tc_ex, "Tc_ex"); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_InitThermal", _ptr(Rt, S["c"], "Rt"), _ptr(kx, S["fx"], "kx"), _ptr(ky, S["fy"], "ky"),
+             _ptr(kz, S["fz"], "kz"), _ptr(Tc_ex, S["ex"]), _ptr(ktv, S["v"], "ktv"), _dt, nx, ny, nz)
+
+
+def ComputeFlux(ctx, qx, qy, qz, kx, ky, kz, A, _dx, _dy, _dz):
+    nx, ny, nz = _cells_ex(A); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_ComputeFlux", _ptr(qx, S["fx"], "qx"), _ptr(qy, S["fy"], "qy"), _ptr(qz, S["fz"], "qz"),
+             _ptr(kx, S["fx"], "kx"), _ptr(ky, S["fy"], "ky"), _ptr(kz, S["fz"], "kz"), _ptr(A, S["ex"]), _dx, _dy,
+             _dz, nx, ny, nz)
+
+
+def UpdateT(ctx, F, T, R, qx, qy, qz, _dt, dtau, _dx, _dy, _dz):
+    nx, ny, nz = _cells(F); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_UpdateT", _ptr(F, S["c"], "F"), _ptr(T, S["ex"], "T"), _ptr(R, S["c"], "R"),
+             _ptr(qx, S["fx"], "qx"), _ptr(qy, S["fy"], "qy"), _ptr(qz, S["fz"], "qz"), _dt, dtau, _dx, _dy, _dz,
+             nx, ny, nz)
+
+
+def ResidualDiffusion(ctx, F, R, qx, qy, qz, _dx, _dy, _dz):
+    nx, ny, nz = _cells(F); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_ResidualDiffusion", _ptr(F, S["c"], "F"), _ptr(R, S["c"], "R"), _ptr(qx, S["fx"], "qx"),
+             _ptr(qy, S["fy"], "qy"), _ptr(qz, S["fz"], "qz"), _dx, _dy, _dz, nx, ny, nz)
+
+
+def ResidualDiffusionTransient(ctx, F, T, R, qx, qy, qz, _dt, _dx, _dy, _dz):
+    nx, ny, nz = _cells(F); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_ResidualDiffusionTransient", _ptr(F, S["c"], "F"), _ptr(T, S["ex"], "T"), _ptr(R, S["c"], "R"),
+             _ptr(qx, S["fx"], "qx"), _ptr(qy, S["fy"], "qy"), _ptr(qz, S["fz"], "qz"), _dt, _dx, _dy, _dz,
+             nx, ny, nz)
+
+
+def UpdateP(ctx, F0, P, F, dampx, dtau):
+    nx, ny, nz = _cells(F); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_UpdateP", _ptr(F0, S["c"], "F0"), _ptr(P, S["ex"], "P"), _ptr(F, S["c"], "F"), dampx, dtau,
+             nx, ny, nz)
+
+
+DampedUpdate = UpdateP
+
+
+def DYRELUpdate(ctx, F0, X, F, h1, h2, dtau):
+    nx, ny, nz = _cells(F); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_DYRELUpdate", _ptr(F0, S["c"], "F0"), _ptr(X, S["ex"], "X"), _ptr(F, S["c"], "F"), h1, h2, dtau,
+             nx, ny, nz)
+
+
+def SetPressureBCs(ctx, Pc_ex, Pbot, Ptop):
+    nx, ny, nz = _cells_ex(Pc_ex, "Pc_ex")
+    ctx.call("ht3d_SetPressureBCs", _ptr(Pc_ex), Pbot, Ptop, nx, ny, nz)
+
+
+def SetFaceBCs(ctx, X_ex, bc_type6, bc_val6):
+    nx, ny, nz = _cells_ex(X_ex, "X_ex")
+    ctx.call("ht3d_SetFaceBCs", _ptr(X_ex), abi.int6(*bc_type6), abi.dbl6(*bc_val6), nx, ny, nz)
+
+
+def KillNorthSouthFluxes(ctx, Ty):
+    nx, ny1, nz = _cells(Ty)
+    ctx.call("ht3d_KillNorthSouthFluxes", _ptr(Ty), nx, ny1 - 1, nz)
+
+
+def ResetA(ctx, A, B):
+    if A.numel() != B.numel():
+        raise ValueError("ResetA: arrays differ in size")
+    ctx.call("ht3d_ResetA", _ptr(A, None, "A"), _ptr(B, None, "B"), _numel(A))
+
+
+def Cpy_inn_to_all(ctx, A, B):
+    nx, ny, nz = _cells(A); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_Cpy_inn_to_all", _ptr(A, S["c"], "A"), _ptr(B, S["ex"], "B"), nx, ny, nz)
+
+
+def Cpy_all_to_inn(ctx, A, B):
+    nx, ny, nz = _cells(B); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_Cpy_all_to_inn", _ptr(A, S["ex"], "A"), _ptr(B, S["c"], "B"), nx, ny, nz)
+
+
+def ArrayEqualArray(ctx, A, B):
+    if A.shape != B.shape:
+        raise ValueError("ArrayEqualArray: shapes differ")
+    ctx.call("ht3d_ArrayEqualArray", _ptr(A, None, "A"), _ptr(B, None, "B"), _numel(A))
+
+
+def Multiply(ctx, a, b, c):
+    if not (a.shape == b.shape == c.shape):
+        raise ValueError("Multiply: shapes differ")
+    ctx.call("ht3d_Multiply", _ptr(a), _ptr(b), _ptr(c), _numel(a))
+
+
+# ------------------------------------------------------ DYREL support
+def GershgorinPoisson(ctx, G, D, rhoC_eff, kx, ky, kz, transient, dt, dx, dy, dz):
+    nx, ny, nz = _cells(G); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_GershgorinPoisson", _ptr(G, S["c"], "G"), _ptr(D, S["c"], "D"), _ptr(rhoC_eff, S["c"], "rhoC"),
+             _ptr(kx, S["fx"], "kx"), _ptr(ky, S["fy"], "ky"), _ptr(kz, S["fz"], "kz"), transient, dt, dx, dy, dz,
+             nx, ny, nz)
+
+
+def GershgorinHydro(ctx, G, phidrhodP, kx, ky, kz, transient, dt, dx, dy, dz):
+    nx, ny, nz = _cells(G); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_GershgorinHydro", _ptr(G, S["c"], "G"), _ptr(phidrhodP, S["c"]), _ptr(kx, S["fx"], "kx"),
+             _ptr(ky, S["fy"], "ky"), _ptr(kz, S["fz"], "kz"), transient, dt, dx, dy, dz, nx, ny, nz)
+
+
+def SwapDYREL(ctx, Xc, Yc, X0c_ex, Y0c):
+    nx, ny, nz = _cells(Xc); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_SwapDYREL", _ptr(Xc, S["c"]), _ptr(Yc, S["c"]), _ptr(X0c_ex, S["ex"]), _ptr(Y0c, S["c"]),
+             nx, ny, nz)
+
+
+def RayleighQuotientNumerator(ctx, G, Fc0, Fcit, Fc, dtau):
+    ctx.call("ht3d_RayleighQuotientNumerator", _ptr(G), _ptr(Fc0), _ptr(Fcit), _ptr(Fc), dtau, _numel(G))
+
+
+def RayleighQuotientDenominator(ctx, G, Fc0, dtau):
+    ctx.call("ht3d_RayleighQuotientDenominator", _ptr(G), _ptr(Fc0), dtau, _numel(G))
+
+
+# ------------------------------------------------------ reductions
+def _reduce(ctx, a, op):
+    out = ctypes.c_double()
+    ctx.call("ht3d_reduce", _ptr(a), _numel(a), op, ctypes.byref(out))
+    return out.value
+
+
+def sum_g(ctx, a):
+    return _reduce(ctx, a, abi.RED_SUM)
+
+
+def maximum_g(ctx, a):
+    return _reduce(ctx, a, abi.RED_MAX)
+
+
+def minimum_g(ctx, a):
+    return _reduce(ctx, a, abi.RED_MIN)
+
+
+def mean_g(ctx, a):
+    return _reduce(ctx, a, abi.RED_SUM) / a.numel()
+
+
+def mean_abs_g(ctx, a):
+    """mean_g(abs.(a)) -- Dimensional/HydroThermal3D_v18.jl:460."""
+    return _reduce(ctx, a, abi.RED_SUM_ABS) / a.numel()
+
+
+def maximum_abs_g(ctx, a):
+    return _reduce(ctx, a, abi.RED_MAX_ABS)
+
+
+# ------------------------------------------------------ WENO5
+def VPlusMinus(ctx, Vm, Vp, V, axis):
+    nx, ny, nz = _cells(Vm)
+    ctx.call("ht3d_VPlusMinus", _ptr(Vm), _ptr(Vp), _ptr(V), axis, nx, ny, nz)
+
+
+def VxPlusMinus(ctx, Vxm, Vxp, Vx):
+    VPlusMinus(ctx, Vxm, Vxp, Vx, 0)
+
+
+def VyPlusMinus(ctx, Vym, Vyp, Vy):
+    VPlusMinus(ctx, Vym, Vyp, Vy, 1)
+
+
+def VzPlusMinus(ctx, Vzm, Vzp, Vz):
+    VPlusMinus(ctx, Vzm, Vzp, Vz, 2)
+
+
+def dFdx_Weno5(ctx, dFdxi, V1, V2, V3, V4, V5):
+    ctx.call("ht3d_dFdx_Weno5", _ptr(dFdxi), _ptr(V1), _ptr(V2), _ptr(V3), _ptr(V4), _ptr(V5), _numel(dFdxi))
+
+
+def Gradients_Weno5(ctx, v1, v2, v3, v4, v5, Fc_exxx, axis, sign, _dx, _dy, _dz):
+    nx, ny, nz = _cells(v1); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_Gradients_Weno5", _ptr(v1), _ptr(v2), _ptr(v3), _ptr(v4), _ptr(v5), _ptr(Fc_exxx, S["xxx"]),
+             axis, sign, _dx, _dy, _dz, nx, ny, nz)
+
+
+def Boundaries_Weno5(ctx, Fc_exxx, Fc, axis, type_L, val_L, type_R, val_R):
+    nx, ny, nz = (int(s) - 6 for s in Fc_exxx.shape)
+    ghosted = 1 if tuple(Fc.shape) == (nx + 2, ny + 2, nz + 2) else 0
+    ctx.call("ht3d_Boundaries_Weno5", _ptr(Fc_exxx), _ptr(Fc), axis, type_L, val_L, type_R, val_R, ghosted,
+             nx, ny, nz)
+
+
+def Advect_v1(ctx, Fc, Vxp, dTdxm, Vxm, dTdxp, dt):
+    ctx.call("ht3d_Advect_v1", _ptr(Fc), _ptr(Vxp), _ptr(dTdxm), _ptr(Vxm), _ptr(dTdxp), dt, _numel(Fc))
+
+
+def TimeAveraging_v1(ctx, Fc, Fold, order):
+    ctx.call("ht3d_TimeAveraging_v1", _ptr(Fc), _ptr(Fold), order, _numel(Fc))
+
+
+def Advect_v2(ctx, Fc_ex, X, V, axis, dt, _dx, _dy, _dz, quirk=1):
+    nx, ny, nz = _cells_ex(Fc_ex, "Fc")
+    ctx.call("ht3d_Advect_v2", _ptr(Fc_ex), _ptr(X), _ptr(V), axis, dt, _dx, _dy, _dz, quirk, nx, ny, nz)
+
+
+def TimeAveraging_v2(ctx, Fc_ex, Fold, order):
+    nx, ny, nz = _cells(Fold)
+    ctx.call("ht3d_TimeAveraging_v2", _ptr(Fc_ex), _ptr(Fold), order, nx, ny, nz)
+
+
+def weno5_advect(ctx, Tc_ex, Vx, Vy, Vz, dt, _dx, _dy, _dz, bc_type6, bc_val6, variant=abi.WENO_V1,
+                 precision=abi.FP64):
+    nx, ny, nz = _cells_ex(Tc_ex, "Tc_ex"); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_weno5_advect", _ptr(Tc_ex, S["ex"]), _ptr(Vx, S["fx"]), _ptr(Vy, S["fy"]), _ptr(Vz, S["fz"]), dt,
+             _dx, _dy, _dz, abi.int6(*bc_type6), abi.dbl6(*bc_val6), variant, precision, nx, ny, nz)
+
+
+# ------------------------------------------------------ fused solver / step
+def dyrel_solve_dimless(ctx, X_ex, R, kx, ky, kz, cX, dx, dy, dz, bc_type6, bc_val6, params, F, F0,
+                        precision=abi.FP64, n_iter_fixed=0):
+    nx, ny, nz = _cells_ex(X_ex, "X_ex"); S = _shapes(nx, ny, nz)
+    st = abi.DyrelStats()
+    ctx.call("ht3d_dyrel_solve_dimless", _ptr(X_ex, S["ex"]), _ptr(R, S["c"], "R"), _ptr(kx, S["fx"], "kx"),
+             _ptr(ky, S["fy"], "ky"), _ptr(kz, S["fz"], "kz"), cX, dx, dy, dz, abi.int6(*bc_type6),
+             abi.dbl6(*bc_val6), ctypes.byref(params), n_iter_fixed, _ptr(F, S["c"], "F"), _ptr(F0, S["c"], "F0"),
+             precision, ctypes.byref(st), nx, ny, nz)
+    return st
+
+
+def step_hrl(ctx, Tc_ex, Pc_ex, ktv, kfv, Vx, Vy, Vz, params, precision=abi.FP64):
+    nx, ny, nz = _cells_ex(Tc_ex, "Tc_ex"); S = _shapes(nx, ny, nz)
+    st_t, st_d = abi.DyrelStats(), abi.DyrelStats()
+    ctx.call("ht3d_step_hrl", _ptr(Tc_ex, S["ex"]), _ptr(Pc_ex, S["ex"]), _ptr(ktv, S["v"]), _ptr(kfv, S["v"]),
+             _ptr(Vx, S["fx"]), _ptr(Vy, S["fy"]), _ptr(Vz, S["fz"]), ctypes.byref(params), ctypes.byref(st_t),
+             ctypes.byref(st_d), precision, nx, ny, nz)
+    return st_t, st_d

@@ -1,0 +1,424 @@
+// WENO5 temperature advection (tools/Weno5_Routines.jl, tools/Weno5_Routines_v2.jl).
+//
+// Two layers:
+//  * granular drop-ins that mirror the reference kernels one for one
+//    (VxPlusMinus!, Gradients_*_Weno5!, dFdx_Weno5!, Boundaries_*_Weno5!,
+//    Advect!, TimeAveraging!), and
+//  * the fused sweep used by the solver: per axis two launches (the two
+//    SSP-RK2 stages), ghost values evaluated on the fly from the boundary
+//    rules (no (n+6)^3 buffer, no v1..v5 temporaries), the RK averaging fused
+//    into the second stage.
+#include "ht3d_internal.cuh"
+
+namespace {
+
+// ----------------------------------------------------------------- WENO core
+// dFdx_Weno5! body, tools/Weno5_Routines.jl:51-66 (FP64, reference order)
+__device__ __forceinline__ double weno5_ref(double v1, double v2, double v3, double v4, double v5) {
+    const double p1 = v1 / 3.0 - 7.0 / 6.0 * v2 + 11.0 / 6.0 * v3;
+    const double p2 = -v2 / 6.0 + 5.0 / 6.0 * v3 + v4 / 3.0;
+    const double p3 = v3 / 3.0 + 5.0 / 6.0 * v4 - v5 / 6.0;
+    const double maxV = fmax(fmax(fmax(fmax(v1 * v1, v2 * v2), v3 * v3), v4 * v4), v5 * v5);
+    const double e = 1e-99 + 1e-6 * maxV;
+    const double a1 = v1 - 2.0 * v2 + v3, b1 = v1 - 4.0 * v2 + 3.0 * v3;
+    const double a2 = v2 - 2.0 * v3 + v4, b2 = v2 - v4;
+    const double a3 = v3 - 2.0 * v4 + v5, b3 = 3.0 * v3 - 4.0 * v4 + v5;
+    double w1 = 13.0 / 12.0 * (a1 * a1) + 1.0 / 4.0 * (b1 * b1);
+    double w2 = 13.0 / 12.0 * (a2 * a2) + 1.0 / 4.0 * (b2 * b2);
+    double w3 = 13.0 / 12.0 * (a3 * a3) + 1.0 / 4.0 * (b3 * b3);
+    w1 = 0.1 / ((w1 + e) * (w1 + e));
+    w2 = 0.6 / ((w2 + e) * (w2 + e));
+    w3 = 0.3 / ((w3 + e) * (w3 + e));
+    const double w = (w1 + w2 + w3);
+    w1 = w1 / w;
+    w2 = w2 / w;
+    w3 = w3 / w;
+    return w1 * p1 + w2 * p2 + w3 * p3;
+}
+
+// Fast-path FP64 form: the same weights with one reciprocal of the weight sum
+// instead of three divisions (differs from the reference by rounding only).
+__device__ __forceinline__ double weno5_fast(double v1, double v2, double v3, double v4, double v5) {
+    const double p1 = v1 * (1.0 / 3.0) - (7.0 / 6.0) * v2 + (11.0 / 6.0) * v3;
+    const double p2 = -v2 * (1.0 / 6.0) + (5.0 / 6.0) * v3 + v4 * (1.0 / 3.0);
+    const double p3 = v3 * (1.0 / 3.0) + (5.0 / 6.0) * v4 - v5 * (1.0 / 6.0);
+    const double maxV = fmax(fmax(fmax(fmax(v1 * v1, v2 * v2), v3 * v3), v4 * v4), v5 * v5);
+    const double e = 1e-99 + 1e-6 * maxV;
+    const double a1 = v1 - 2.0 * v2 + v3, b1 = v1 - 4.0 * v2 + 3.0 * v3;
+    const double a2 = v2 - 2.0 * v3 + v4, b2 = v2 - v4;
+    const double a3 = v3 - 2.0 * v4 + v5, b3 = 3.0 * v3 - 4.0 * v4 + v5;
+    const double s1 = (13.0 / 12.0) * (a1 * a1) + 0.25 * (b1 * b1) + e;
+    const double s2 = (13.0 / 12.0) * (a2 * a2) + 0.25 * (b2 * b2) + e;
+    const double s3 = (13.0 / 12.0) * (a3 * a3) + 0.25 * (b3 * b3) + e;
+    const double w1 = 0.1 / (s1 * s1), w2 = 0.6 / (s2 * s2), w3 = 0.3 / (s3 * s3);
+    const double iw = 1.0 / (w1 + w2 + w3);
+    return (w1 * p1 + w2 * p2 + w3 * p3) * iw;
+}
+
+// FP32 form for the mixed-precision path.  The reference's epsilon floor
+// 1e-99 underflows in FP32; 1e-18 is the smallest floor whose square stays a
+// normal FP32 number, so a flat field still yields the linear weights.
+__device__ __forceinline__ float weno5_f32(float v1, float v2, float v3, float v4, float v5) {
+    const float p1 = v1 * (1.0f / 3.0f) - (7.0f / 6.0f) * v2 + (11.0f / 6.0f) * v3;
+    const float p2 = -v2 * (1.0f / 6.0f) + (5.0f / 6.0f) * v3 + v4 * (1.0f / 3.0f);
+    const float p3 = v3 * (1.0f / 3.0f) + (5.0f / 6.0f) * v4 - v5 * (1.0f / 6.0f);
+    const float maxV = fmaxf(fmaxf(fmaxf(fmaxf(v1 * v1, v2 * v2), v3 * v3), v4 * v4), v5 * v5);
+    const float e = 1e-18f + 1e-6f * maxV;
+    const float a1 = v1 - 2.0f * v2 + v3, b1 = v1 - 4.0f * v2 + 3.0f * v3;
+    const float a2 = v2 - 2.0f * v3 + v4, b2 = v2 - v4;
+    const float a3 = v3 - 2.0f * v4 + v5, b3 = 3.0f * v3 - 4.0f * v4 + v5;
+    const float s1 = (13.0f / 12.0f) * (a1 * a1) + 0.25f * (b1 * b1) + e;
+    const float s2 = (13.0f / 12.0f) * (a2 * a2) + 0.25f * (b2 * b2) + e;
+    const float s3 = (13.0f / 12.0f) * (a3 * a3) + 0.25f * (b3 * b3) + e;
+    const float w1 = 0.1f / (s1 * s1), w2 = 0.6f / (s2 * s2), w3 = 0.3f / (s3 * s3);
+    const float iw = 1.0f / (w1 + w2 + w3);
+    return (w1 * p1 + w2 * p2 + w3 * p3) * iw;
+}
+
+struct WenoBC {
+    int typeL, typeR;
+    double valL, valR;
+};
+
+// value at position p (-3 <= p <= n+2) along the sweep axis of a line whose
+// inner value at index m is line[m*stride]; ghost rules of
+// Boundaries_*_Weno5! (Neumann mirror, Dirichlet 2v-mirror, periodic wrap).
+__device__ __forceinline__ double line_at(const double* __restrict__ line, long long stride, int p, int n,
+                                          const WenoBC& bc) {
+    if (p < 0) {
+        if (bc.typeL == HT3D_BC_PERIODIC) return line[(long long)(n + p) * stride];
+        const double v = line[(long long)(-1 - p) * stride];
+        return bc.typeL == HT3D_BC_DIRICHLET ? 2 * bc.valL - v : v;
+    }
+    if (p >= n) {
+        if (bc.typeR == HT3D_BC_PERIODIC) return line[(long long)(p - n) * stride];
+        const double v = line[(long long)(2 * n - 1 - p) * stride];
+        return bc.typeR == HT3D_BC_DIRICHLET ? 2 * bc.valR - v : v;
+    }
+    return line[(long long)p * stride];
+}
+
+// One SSP-RK2 stage along AXIS on ghosted (ex) fields.
+//   PREC 0: FP64 reference-order arithmetic (parity form)
+//   PREC 1: FP32 stencil arithmetic, FP64 state (mixed form)
+//   STAGE 1: dst = src - dt*(Vp*dFm + Vm*dFp)
+//   STAGE 2: dst = 0.5*(src - dt*(...)) + 0.5*T0   (TimeAveraging!, order 2)
+template <int AXIS, int QUIRK, int STAGE, int PREC>
+__global__ void __launch_bounds__(256) k_weno_stage(const double* __restrict__ src, double* dst, const double* T0,
+                                                    const double* __restrict__ V, double dt, double h, WenoBC bc,
+                                                    int nx, int ny, int nz) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= nx || j >= ny || k >= nz) return;
+    const int n1 = nx + 2, n2 = ny + 2;
+    const long long e = (i + 1) + (long long)n1 * ((j + 1) + (long long)n2 * (k + 1));
+    const int idx = AXIS == 0 ? i : (AXIS == 1 ? j : k);
+    const int n = AXIS == 0 ? nx : (AXIS == 1 ? ny : nz);
+    const long long stride = AXIS == 0 ? 1 : (AXIS == 1 ? (long long)n1 : (long long)n1 * n2);
+    const double* line = src + e - (long long)idx * stride;
+    double x[7];
+#pragma unroll
+    for (int o = 0; o < 7; ++o) x[o] = line_at(line, stride, idx + o - 3, n, bc);
+    // face velocities: V[idx] (left) and V[idx+1] (right) along AXIS
+    long long vl;
+    long long vs;
+    if (AXIS == 0) { vl = ix3(i, j, k, nx + 1, ny); vs = 1; }
+    else if (AXIS == 1) { vl = ix3(i, j, k, nx, ny + 1); vs = nx; }
+    else { vl = ix3(i, j, k, nx, ny); vs = (long long)nx * ny; }
+    const double a = V[vl], b = V[vl + vs];
+    const double Vm = a < 0.0 ? a : 0.0;
+    const double Vp = b >= 0.0 ? b : 0.0;
+    double rhs;
+    if (PREC == 0) {
+        // x[o] holds X[I+o-3]
+        const double m1 = h * (x[1] - x[0]), m2 = h * (x[2] - x[1]), m3 = h * (x[3] - x[2]), m4 = h * (x[4] - x[3]);
+        const double m5 = QUIRK ? h * (x[5] - x[2]) : h * (x[5] - x[4]);
+        const double dFm = weno5_fast(m1, m2, m3, m4, m5);
+        const double p1 = h * (x[6] - x[5]), p2 = h * (x[5] - x[4]), p3 = h * (x[4] - x[3]), p4 = h * (x[3] - x[2]);
+        const double p5 = h * (x[2] - x[1]);
+        const double dFp = weno5_fast(p1, p2, p3, p4, p5);
+        rhs = Vp * dFm + Vm * dFp;
+    } else {
+        const float hf = (float)h;
+        float d[6];
+#pragma unroll
+        for (int o = 0; o < 6; ++o) d[o] = hf * (float)(x[o + 1] - x[o]);  // d[o] = h*(X[I+o-2]-X[I+o-3])
+        const float m5 = QUIRK ? hf * (float)(x[5] - x[2]) : d[4];
+        const float dFm = weno5_f32(d[0], d[1], d[2], d[3], m5);
+        const float dFp = weno5_f32(d[5], d[4], d[3], d[2], d[1]);
+        rhs = (double)((float)Vp * dFm + (float)Vm * dFp);
+    }
+    const double t = x[3] - dt * rhs;
+    if (STAGE == 1) dst[e] = t;
+    else dst[e] = 0.5 * t + 0.5 * T0[e];
+}
+
+// ------------------------------------------------------- granular drop-ins
+#define GIDX                                             \
+    const int i = blockIdx.x * blockDim.x + threadIdx.x; \
+    const int j = blockIdx.y * blockDim.y + threadIdx.y; \
+    const int k = blockIdx.z * blockDim.z + threadIdx.z
+
+__global__ void k_vplusminus(double* Vm, double* Vp, const double* __restrict__ V, int axis, int nx, int ny, int nz) {
+    GIDX;
+    if (i >= nx || j >= ny || k >= nz) return;
+    const int c = ix3(i, j, k, nx, ny);
+    const int v1 = axis == 0 ? ix3(i, j, k, nx + 1, ny) : (axis == 1 ? ix3(i, j, k, nx, ny + 1) : ix3(i, j, k, nx, ny));
+    const int v2 = axis == 0 ? v1 + 1 : (axis == 1 ? v1 + nx : v1 + nx * ny);
+    const double a = V[v1], b = V[v2];
+    if (a < 0.0) Vm[c] = a;
+    if (a > 0.0) Vm[c] = 0.0;
+    if (b < 0.0) Vp[c] = 0.0;
+    if (b > 0.0) Vp[c] = b;
+}
+
+__global__ void k_dfdx(double* dF, const double* __restrict__ v1, const double* __restrict__ v2,
+                       const double* __restrict__ v3, const double* __restrict__ v4, const double* __restrict__ v5,
+                       long long n) {
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        dF[t] = weno5_ref(v1[t], v2[t], v3[t], v4[t], v5[t]);
+}
+
+__global__ void k_gradients(double* v1, double* v2, double* v3, double* v4, double* v5, const double* __restrict__ X,
+                            int axis, int sign, double h, int nx, int ny, int nz) {
+    GIDX;
+    if (i >= nx || j >= ny || k >= nz) return;
+    const int n1 = nx + 6, n2 = ny + 6;
+    const long long base = ix3(i + 3, j + 3, k + 3, n1, n2);
+    const long long st = axis == 0 ? 1 : (axis == 1 ? n1 : (long long)n1 * n2);
+    auto x = [&](int o) { return X[base + o * st]; };
+    const int c = ix3(i, j, k, nx, ny);
+    if (sign < 0) {
+        v1[c] = h * (x(-2) - x(-3));
+        v2[c] = h * (x(-1) - x(-2));
+        v3[c] = h * (x(0) - x(-1));
+        v4[c] = h * (x(1) - x(0));
+        v5[c] = h * (x(2) - x(1));
+    } else {
+        v1[c] = h * (x(3) - x(2));
+        v2[c] = h * (x(2) - x(1));
+        v3[c] = h * (x(1) - x(0));
+        v4[c] = h * (x(0) - x(-1));
+        v5[c] = h * (x(-1) - x(-2));
+    }
+}
+
+__global__ void k_boundaries(double* X, const double* __restrict__ Fc, int axis, WenoBC bc, int o, int nx, int ny,
+                             int nz) {
+    GIDX;
+    const int n1 = nx + 6, n2 = ny + 6, n3 = nz + 6;
+    if (i >= n1 || j >= n2 || k >= n3) return;
+    const int f1 = nx + 2 * o, f2 = ny + 2 * o;
+    if (i < nx && j < ny && k < nz) X[ix3(i + 3, j + 3, k + 3, n1, n2)] = Fc[ix3(i + o, j + o, k + o, f1, f2)];
+    const int idx[3] = {i, j, k};
+    const int N[3] = {nx, ny, nz};
+    for (int a = 0; a < 3; ++a)
+        if (a != axis && !(idx[a] >= 3 && idx[a] < N[a] + 3)) return;
+    const int p = idx[axis], n = N[axis];
+    int s[3] = {i - 3, j - 3, k - 3};
+    if (p < 3) {
+        if (bc.typeL == HT3D_BC_PERIODIC) s[axis] = n - 3 + p;
+        else s[axis] = 2 - p;
+        const double v = Fc[ix3(s[0] + o, s[1] + o, s[2] + o, f1, f2)];
+        X[ix3(i, j, k, n1, n2)] = bc.typeL == HT3D_BC_DIRICHLET ? 2 * bc.valL - v : v;
+    } else if (p >= n + 3) {
+        const int q = p - (n + 3);
+        if (bc.typeR == HT3D_BC_PERIODIC) s[axis] = q;
+        else s[axis] = n - 1 - q;
+        const double v = Fc[ix3(s[0] + o, s[1] + o, s[2] + o, f1, f2)];
+        X[ix3(i, j, k, n1, n2)] = bc.typeR == HT3D_BC_DIRICHLET ? 2 * bc.valR - v : v;
+    }
+}
+
+__global__ void k_advect_v1(double* Fc, const double* __restrict__ Vxp, const double* __restrict__ dm,
+                            const double* __restrict__ Vxm, const double* __restrict__ dp, double dt, long long n) {
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        Fc[t] = Fc[t] - dt * (Vxp[t] * dm[t] + Vxm[t] * dp[t]);
+}
+__global__ void k_timeavg_v1(double* Fc, const double* __restrict__ Fold, double order, long long n) {
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        Fc[t] = (1.0 / order) * Fc[t] + (1.0 - 1.0 / order) * Fold[t];
+}
+__global__ void k_timeavg_v2(double* Fc, const double* __restrict__ Fold, double order, int nx, int ny, int nz) {
+    GIDX;
+    if (i >= nx || j >= ny || k >= nz) return;
+    const long long e = ix3(i + 1, j + 1, k + 1, nx + 2, ny + 2);
+    Fc[e] = (1.0 / order) * Fc[e] + (1.0 - 1.0 / order) * Fold[ix3(i, j, k, nx, ny)];
+}
+
+// Advect! v2 (tools/Weno5_Routines_v2.jl:55-212), reference arithmetic
+__global__ void k_advect_v2(double* Fc, const double* __restrict__ X, const double* __restrict__ V, int axis, double dt,
+                            double h, int quirk, int nx, int ny, int nz) {
+    GIDX;
+    if (i >= nx || j >= ny || k >= nz) return;
+    const int n1 = nx + 6, n2 = ny + 6;
+    const long long base = ix3(i + 3, j + 3, k + 3, n1, n2);
+    const long long st = axis == 0 ? 1 : (axis == 1 ? n1 : (long long)n1 * n2);
+    auto x = [&](int o) { return X[base + o * st]; };
+    const int v1 = axis == 0 ? ix3(i, j, k, nx + 1, ny) : (axis == 1 ? ix3(i, j, k, nx, ny + 1) : ix3(i, j, k, nx, ny));
+    const int v2 = axis == 0 ? v1 + 1 : (axis == 1 ? v1 + nx : v1 + nx * ny);
+    const double a = V[v1], b = V[v2];
+    double Vm = 0.0, Vp = 0.0;
+    if (a < 0.0) Vm = a;
+    if (a >= 0.0) Vm = 0.0;
+    if (b < 0.0) Vp = 0.0;
+    if (b >= 0.0) Vp = b;
+    const double dFm = weno5_ref(h * (x(-2) - x(-3)), h * (x(-1) - x(-2)), h * (x(0) - x(-1)), h * (x(1) - x(0)),
+                                 quirk ? h * (x(2) - x(-1)) : h * (x(2) - x(1)));
+    const double dFp = weno5_ref(h * (x(3) - x(2)), h * (x(2) - x(1)), h * (x(1) - x(0)), h * (x(0) - x(-1)),
+                                 h * (x(-1) - x(-2)));
+    const long long e = ix3(i + 1, j + 1, k + 1, nx + 2, ny + 2);
+    Fc[e] = Fc[e] - dt * (Vp * dFm + Vm * dFp);
+}
+
+inline dim3 g1(ht3d_ctx* ctx, long long n) {
+    long long b = (n + 255) / 256;
+    return dim3((unsigned)std::max<long long>(1, std::min<long long>(b, (long long)ctx->num_sms * 16)));
+}
+
+template <int AXIS, int QUIRK, int PREC>
+void weno_axis(ht3d_ctx* ctx, double* T, double* T1, const double* V, double dt, double h, WenoBC bc, int nx, int ny,
+               int nz) {
+    dim3 b(32, 8, 1), g((nx + 31) / 32, (ny + 7) / 8, nz);
+    HT3D_LAUNCH(ctx, (k_weno_stage<AXIS, QUIRK, 1, PREC>), g, b, 0, T, T1, (const double*)nullptr, V, dt, h, bc, nx,
+                ny, nz);
+    HT3D_LAUNCH(ctx, (k_weno_stage<AXIS, QUIRK, 2, PREC>), g, b, 0, T1, T, T, V, dt, h, bc, nx, ny, nz);
+}
+
+template <int QUIRK, int PREC>
+void weno_all(ht3d_ctx* ctx, double* T, double* T1, const double* const* V, double dt, const double* h,
+              const WenoBC* bc, int nx, int ny, int nz) {
+    weno_axis<0, QUIRK, PREC>(ctx, T, T1, V[0], dt, h[0], bc[0], nx, ny, nz);
+    weno_axis<1, QUIRK, PREC>(ctx, T, T1, V[1], dt, h[1], bc[1], nx, ny, nz);
+    weno_axis<2, QUIRK, PREC>(ctx, T, T1, V[2], dt, h[2], bc[2], nx, ny, nz);
+}
+
+}  // namespace
+
+// used by the step driver
+void ht3d_weno5_advect_impl(ht3d_ctx* ctx, double* Tc_ex, const double* Vx, const double* Vy, const double* Vz,
+                            double dt, double _dx, double _dy, double _dz, const int* bc_type6, const double* bc_val6,
+                            int variant, int precision, int nx, int ny, int nz) {
+    ht3d_check_dims(nx, ny, nz, 3);
+    HT3D_REQUIRE(variant >= HT3D_WENO_V1 && variant <= HT3D_WENO_V2_FIXED, "unknown WENO variant");
+    HT3D_REQUIRE(precision == HT3D_FP64 || precision == HT3D_MIXED, "unknown precision");
+    WenoBC bc[3];
+    for (int a = 0; a < 3; ++a) {
+        HT3D_REQUIRE(bc_type6[2 * a] >= 0 && bc_type6[2 * a] <= 2 && bc_type6[2 * a + 1] >= 0 && bc_type6[2 * a + 1] <= 2,
+                     "WENO BC type must be 0, 1 or 2");
+        bc[a].typeL = bc_type6[2 * a];
+        bc[a].typeR = bc_type6[2 * a + 1];
+        bc[a].valL = bc_val6[2 * a];
+        bc[a].valR = bc_val6[2 * a + 1];
+    }
+    const long long nex = (long long)(nx + 2) * (ny + 2) * (nz + 2);
+    double* T1 = (double*)ht3d_scratch(ctx, SLOT_WENO_T1, sizeof(double) * nex);
+    const double* V[3] = {Vx, Vy, Vz};
+    const double h[3] = {_dx, _dy, _dz};
+    const bool quirk = variant == HT3D_WENO_V2_REF;
+    if (precision == HT3D_FP64) {
+        if (quirk) weno_all<1, 0>(ctx, Tc_ex, T1, V, dt, h, bc, nx, ny, nz);
+        else weno_all<0, 0>(ctx, Tc_ex, T1, V, dt, h, bc, nx, ny, nz);
+    } else {
+        if (quirk) weno_all<1, 1>(ctx, Tc_ex, T1, V, dt, h, bc, nx, ny, nz);
+        else weno_all<0, 1>(ctx, Tc_ex, T1, V, dt, h, bc, nx, ny, nz);
+    }
+}
+
+extern "C" {
+
+#define G3(a, b, c) grid3((a), (b), (c), kBlock3)
+
+int ht3d_VPlusMinus(ht3d_ctx* ctx, double* Vm, double* Vp, const double* V, int axis, int nx, int ny, int nz) {
+    return ht3d_guard(ctx, [&]() {
+        ht3d_check_dims(nx, ny, nz, 1);
+        HT3D_REQUIRE(axis >= 0 && axis <= 2, "axis must be 0, 1 or 2");
+        HT3D_LAUNCH(ctx, k_vplusminus, G3(nx, ny, nz), kBlock3, 0, Vm, Vp, V, axis, nx, ny, nz);
+        return HT3D_OK;
+    });
+}
+
+int ht3d_dFdx_Weno5(ht3d_ctx* ctx, double* dFdxi, const double* V1, const double* V2, const double* V3,
+                    const double* V4, const double* V5, long long n) {
+    return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(n >= 0, "negative size");
+        if (n) HT3D_LAUNCH(ctx, k_dfdx, g1(ctx, n), 256, 0, dFdxi, V1, V2, V3, V4, V5, n);
+        return HT3D_OK;
+    });
+}
+
+int ht3d_Gradients_Weno5(ht3d_ctx* ctx, double* v1, double* v2, double* v3, double* v4, double* v5,
+                         const double* Fc_exxx, int axis, int sign, double _dx, double _dy, double _dz, int nx, int ny,
+                         int nz) {
+    return ht3d_guard(ctx, [&]() {
+        ht3d_check_dims(nx, ny, nz, 1);
+        HT3D_REQUIRE(axis >= 0 && axis <= 2 && (sign == 1 || sign == -1), "bad axis/sign");
+        const double h = axis == 0 ? _dx : (axis == 1 ? _dy : _dz);
+        HT3D_LAUNCH(ctx, k_gradients, G3(nx, ny, nz), kBlock3, 0, v1, v2, v3, v4, v5, Fc_exxx, axis, sign, h, nx, ny, nz);
+        return HT3D_OK;
+    });
+}
+
+int ht3d_Boundaries_Weno5(ht3d_ctx* ctx, double* Fc_exxx, const double* Fc, int axis, int type_L, double val_L,
+                          int type_R, double val_R, int fc_ghosted, int nx, int ny, int nz) {
+    return ht3d_guard(ctx, [&]() {
+        ht3d_check_dims(nx, ny, nz, 3);
+        HT3D_REQUIRE(axis >= 0 && axis <= 2, "axis must be 0, 1 or 2");
+        HT3D_REQUIRE(type_L >= 0 && type_L <= 2 && type_R >= 0 && type_R <= 2, "BC type must be 0, 1 or 2");
+        WenoBC bc{type_L, type_R, val_L, val_R};
+        HT3D_LAUNCH(ctx, k_boundaries, G3(nx + 6, ny + 6, nz + 6), kBlock3, 0, Fc_exxx, Fc, axis, bc, fc_ghosted ? 1 : 0,
+                    nx, ny, nz);
+        return HT3D_OK;
+    });
+}
+
+int ht3d_Advect_v1(ht3d_ctx* ctx, double* Fc, const double* Vxp, const double* dTdxm, const double* Vxm,
+                   const double* dTdxp, double dt, long long n) {
+    return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(n >= 0, "negative size");
+        if (n) HT3D_LAUNCH(ctx, k_advect_v1, g1(ctx, n), 256, 0, Fc, Vxp, dTdxm, Vxm, dTdxp, dt, n);
+        return HT3D_OK;
+    });
+}
+
+int ht3d_TimeAveraging_v1(ht3d_ctx* ctx, double* Fc, const double* Fold, double order, long long n) {
+    return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(n >= 0, "negative size");
+        if (n) HT3D_LAUNCH(ctx, k_timeavg_v1, g1(ctx, n), 256, 0, Fc, Fold, order, n);
+        return HT3D_OK;
+    });
+}
+
+int ht3d_Advect_v2(ht3d_ctx* ctx, double* Fc_ex, const double* X_exxx, const double* V, int axis, double dt,
+                   double _dx, double _dy, double _dz, int quirk, int nx, int ny, int nz) {
+    return ht3d_guard(ctx, [&]() {
+        ht3d_check_dims(nx, ny, nz, 1);
+        HT3D_REQUIRE(axis >= 0 && axis <= 2, "axis must be 0, 1 or 2");
+        const double h = axis == 0 ? _dx : (axis == 1 ? _dy : _dz);
+        HT3D_LAUNCH(ctx, k_advect_v2, G3(nx, ny, nz), kBlock3, 0, Fc_ex, X_exxx, V, axis, dt, h, quirk ? 1 : 0, nx, ny,
+                    nz);
+        return HT3D_OK;
+    });
+}
+
+int ht3d_TimeAveraging_v2(ht3d_ctx* ctx, double* Fc_ex, const double* Fold, double order, int nx, int ny, int nz) {
+    return ht3d_guard(ctx, [&]() {
+        ht3d_check_dims(nx, ny, nz, 1);
+        HT3D_LAUNCH(ctx, k_timeavg_v2, G3(nx, ny, nz), kBlock3, 0, Fc_ex, Fold, order, nx, ny, nz);
+        return HT3D_OK;
+    });
+}
+
+int ht3d_weno5_advect(ht3d_ctx* ctx, double* Tc_ex, const double* Vx, const double* Vy, const double* Vz, double dt,
+                      double _dx, double _dy, double _dz, const int* bc_type6, const double* bc_val6, int variant,
+                      int precision, int nx, int ny, int nz) {
+    return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(Tc_ex && Vx && Vy && Vz && bc_type6 && bc_val6, "null argument");
+        ht3d_weno5_advect_impl(ctx, Tc_ex, Vx, Vy, Vz, dt, _dx, _dy, _dz, bc_type6, bc_val6, variant, precision, nx, ny,
+                               nz);
+        return HT3D_OK;
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,74 @@
+"""Problem set-up for the dimensionless Horton-Rogers-Lapwood (porous
+convection) workload: the physics of Dimensionless/HydroThermal3D_Alban_v6.jl
+in a unit cube, solved with DYREL.
+
+Initial condition: T linear from Tbot = 1 (bottom, y = 0) to Ttop = 0 (top,
+y = 1) at the cell centres (ghosts included), plus a seeded uniform
+perturbation of amplitude ``amp`` on the inner cells; P = 0; uniform
+conductivity and permeability (ktv = kfv = 1).
+
+Boundary conditions (Alban_v6.jl:108-130, 153-159):
+  thermal : x, z Neumann; y Dirichlet Tbot / Ttop
+  Darcy   : all Neumann, buoyancy flux through top/bottom removed
+            (KillNorthSouthFluxes!)
+  WENO5   : W/E/B/F Neumann, S/N Dirichlet Tbot/Ttop
+            (Dimensionless/kernels_HT3D.jl:164-177)
+Time step: dt0 = min(dx,dy,dz)^2/6.1 (Dimensionless/HydroThermal3D_v7.jl:68),
+then dt = dt_fact/6.1*min(dx,dy,dz)/max|V| after each step (v7.jl:220).
+"""
+import numpy as np
+
+from . import abi
+
+N, D = abi.BC_NEUMANN, abi.BC_DIRICHLET
+
+
+def initial_fields(nx, ny, nz, seed=1, amp=1e-3, Tbot=1.0, Ttop=0.0, L=(1.0, 1.0, 1.0)):
+    """Return numpy (Fortran-order) Tc_ex, Pc_ex, ktv, kfv for the HRL set-up."""
+    Lx, Ly, Lz = L
+    dy = Ly / ny
+    yce = np.linspace(-dy / 2, Ly + dy / 2, ny + 2)
+    T = np.empty((nx + 2, ny + 2, nz + 2), order="F")
+    T[...] = (Tbot + (Ttop - Tbot) * yce / Ly)[None, :, None]
+    rng = np.random.default_rng(seed)
+    pert = rng.uniform(-amp, amp, size=(nz, ny, nx)).transpose(2, 1, 0)
+    T[1:-1, 1:-1, 1:-1] += pert
+    P = np.zeros((nx + 2, ny + 2, nz + 2), order="F")
+    ktv = np.ones((nx + 1, ny + 1, nz + 1), order="F")
+    kfv = np.ones((nx + 1, ny + 1, nz + 1), order="F")
+    return T, P, ktv, kfv
+
+
+def params(nx, ny, nz, Ra=1000.0, tol=1e-8, nitmax=10000, nitout=1000, dt_fact=10.0, weno_variant=abi.WENO_V1,
+           L=(1.0, 1.0, 1.0), Tbot=1.0, Ttop=0.0, advection=True, dt_adapt=True):
+    Lx, Ly, Lz = L
+    dx, dy, dz = Lx / nx, Ly / ny, Lz / nz
+    p = abi.HrlParams()
+    p.Ra, p.dx, p.dy, p.dz = Ra, dx, dy, dz
+    p.dt = min(dx, dy, dz) ** 2 / 6.1
+    p.Tbot, p.Ttop = Tbot, Ttop
+    p.thermal_bc = abi.int6(N, N, D, D, N, N)
+    p.thermal_val = abi.dbl6(0, 0, Tbot, Ttop, 0, 0)
+    p.darcy_bc = abi.int6(N, N, N, N, N, N)
+    p.darcy_val = abi.dbl6(0, 0, 0, 0, 0, 0)
+    p.weno_bc = abi.int6(N, N, D, D, N, N)
+    p.weno_val = abi.dbl6(0, 0, Tbot, Ttop, 0, 0)
+    p.weno_variant = weno_variant
+    p.kill_ns = 1
+    p.dt_adapt = 1 if dt_adapt else 0
+    p.advection = 1 if advection else 0
+    p.dt_fact = dt_fact
+    p.thermal = abi.DyrelParams.reference(tol=tol, nitmax=nitmax, nitout=nitout)
+    p.darcy = abi.DyrelParams.reference(tol=tol, nitmax=nitmax, nitout=nitout)
+    return p
+
+
+def bytes_per_iteration(nx, ny, nz, s):
+    """Algorithmic bytes of one dimensionless DYREL pseudo-iteration:
+    update {X, F0} (read+write) and read {kx, ky, kz, R, PC}: 9*N*s."""
+    return 9 * nx * ny * nz * s
+
+
+def bytes_per_advection(nx, ny, nz, s):
+    """WENO5 SSP-RK2 over three axes: 7*N*s per axis."""
+    return 21 * nx * ny * nz * s

@@ -1,0 +1,277 @@
+/*
+ * ht3d.h -- C ABI of libht3d.so, a GB300 (sm_103a) CUDA implementation of the
+ * pseudo-transient hot path of HydroThermal3D (tduretz/HydroThermal3D).
+ *
+ * Each `ht3d_<Kernel>` entry point replaces one ParallelStencil call
+ * `@parallel Kernel!(args...)` of the reference, with the same argument order;
+ * the reference file:line of every replaced kernel is cited beside it.
+ *
+ * Conventions
+ *   - Arrays are caller-owned DEVICE pointers to FP64 data laid out exactly
+ *     like the reference's Data.Array: 3-D, column-major (x fastest), with the
+ *     reference's staggering. nx, ny, nz are numbers of cells:
+ *       cell   : nx   x ny   x nz        ghosted "ex" : (nx+2)x(ny+2)x(nz+2)
+ *       x-face : (nx+1) x ny x nz        y-face : nx x (ny+1) x nz
+ *       z-face : nx x ny x (nz+1)        vertex : (nx+1)x(ny+1)x(nz+1)
+ *       WENO "exxx" : (nx+6)x(ny+6)x(nz+6)   wN : (nx+2)x(nz+2)
+ *     Phase fields are FP64 codes {-1,0,1,2,3} as in the reference.
+ *   - Scalars are passed by value, in the reference's order.
+ *   - Every call returns an int status (HT3D_OK = 0). Nothing aborts or traps.
+ *   - One ctx = one CUDA stream = one host thread. By default every call is
+ *     synchronous (like @parallel); ht3d_ctx_set_sync(ctx, 0) makes the
+ *     per-kernel calls asynchronous on the ctx stream.
+ *   - The ctx owns only scratch memory (reduction partials, ping-pong and
+ *     FP32 shadow buffers); it never frees or reallocates caller buffers.
+ */
+#ifndef HT3D_H
+#define HT3D_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HT3D_ABI_VERSION 1
+
+/* status codes */
+#define HT3D_OK 0
+#define HT3D_ERR_ARG 1         /* bad dimensions / null pointer / bad option */
+#define HT3D_ERR_CUDA 2        /* CUDA runtime error (see ht3d_ctx_last_error) */
+#define HT3D_ERR_NAN 3         /* residual became NaN (reference: error("Nan T...")) */
+#define HT3D_ERR_DIVERGED 4    /* nF_rel > 100 (reference: error("Diverged T...")) */
+#define HT3D_ERR_MAXITER 5     /* reserved: the reference does not error at nitmax */
+#define HT3D_ERR_TIMEOUT 6     /* a bounded device wait gave up */
+#define HT3D_ERR_NOMEM 7
+
+/* precision forms */
+#define HT3D_FP64 0            /* plain FP64, reproduces the reference */
+#define HT3D_MIXED 1           /* FP32 storage/stencils + FP64 norms, defect correction, T accumulation */
+
+/* face boundary-condition types (tools/Weno5_Routines.jl:134-168) */
+#define HT3D_BC_NEUMANN 0
+#define HT3D_BC_DIRICHLET 1
+#define HT3D_BC_PERIODIC 2
+
+/* WENO5 variants */
+#define HT3D_WENO_V1 0         /* tools/Weno5_Routines.jl (unfused reference, textbook stencil) */
+#define HT3D_WENO_V2_REF 1     /* tools/Weno5_Routines_v2.jl incl. its minus-branch v5 stencil */
+#define HT3D_WENO_V2_FIXED 2   /* v2 loop structure with the textbook v5 stencil */
+
+typedef struct ht3d_ctx ht3d_ctx;
+
+/* DYREL controls (Dimensional/HydroThermal3D_v18.jl:433-439, 292-303) */
+typedef struct ht3d_dyrel_params {
+    double tol_abs;     /* stop when nF_abs < tol_abs ...            (tolT / tolP)  */
+    double tol_rel;     /* ... or nF_rel < tol_rel                                  */
+    int nitmax;         /* maximum pseudo-iterations                 (nitmax = 1e4) */
+    int nitout;         /* check cadence: iter % nitout == 0 || iter <= 2 (1000)   */
+    double cfl;         /* CFL_T / CFL_P                              (0.99)        */
+    double cfact;       /* damping factor                             (0.5)         */
+    double lmin_ratio;  /* initial lambda_min = lambda_max / lmin_ratio (500)       */
+    double norm_scale;  /* nF_abs multiplier (sc.rho*sc.C*sc.T/sc.t, 1 if dimensionless) */
+} ht3d_dyrel_params;
+
+typedef struct ht3d_dyrel_stats {
+    int iters;          /* pseudo-iterations performed */
+    int converged;      /* 1 if the stop test fired */
+    int status;         /* HT3D_OK / HT3D_ERR_NAN / HT3D_ERR_DIVERGED */
+    int checks;         /* number of check iterations */
+    double nF_abs, nF_rel, nF_ini;
+    double lambda_min, lambda_max, h1, h2, dtau;
+} ht3d_dyrel_stats;
+
+/* Dimensionless Horton-Rogers-Lapwood time step (see ht3d_step_hrl). */
+typedef struct ht3d_hrl_params {
+    double Ra, dx, dy, dz;
+    double dt;                 /* in: this step's dt; out: next dt when dt_adapt */
+    double Tbot, Ttop;
+    int thermal_bc[6]; double thermal_val[6];   /* faces W,E,S,N,B,F */
+    int darcy_bc[6];   double darcy_val[6];
+    int weno_bc[6];    double weno_val[6];
+    int weno_variant;          /* HT3D_WENO_* */
+    int kill_ns;               /* KillNorthSouthFluxes! (Alban_v6.jl:153-159) */
+    int dt_adapt;              /* dt = dt_fact/6.1*min(dx,dy,dz)/max|V| (v7.jl:220) */
+    int advection;
+    double dt_fact;
+    ht3d_dyrel_params thermal, darcy;
+} ht3d_hrl_params;
+
+/* ------------------------------------------------------------------ */
+/* library / context                                                   */
+/* ------------------------------------------------------------------ */
+int ht3d_abi_version(void);
+const char* ht3d_status_string(int status);
+/* stream: a cudaStream_t (NULL creates a private non-blocking stream) */
+int ht3d_ctx_create(ht3d_ctx** out, int device, void* stream);
+int ht3d_ctx_destroy(ht3d_ctx* ctx);
+int ht3d_ctx_set_stream(ht3d_ctx* ctx, void* stream);
+int ht3d_ctx_set_sync(ht3d_ctx* ctx, int sync_each_call);
+int ht3d_ctx_synchronize(ht3d_ctx* ctx);
+/* number of CUDA kernels this ctx has launched (monotonic) */
+unsigned long long ht3d_ctx_launch_count(const ht3d_ctx* ctx);
+const char* ht3d_ctx_last_error(const ht3d_ctx* ctx);
+/* sizes of the parameter structs, for binding checks */
+int ht3d_sizeof_dyrel_params(void);
+int ht3d_sizeof_dyrel_stats(void);
+int ht3d_sizeof_hrl_params(void);
+
+/* ------------------------------------------------------------------ */
+/* Reductions (tools/Macros.jl:20-25: maximum_g, minimum_g, mean_g,    */
+/* sum_g; and mean_g(abs.(F)) at Dimensional/HydroThermal3D_v18.jl:460)*/
+/* op: 0 sum, 1 sum|.|, 2 max, 3 min, 4 max|.| ; result to *out (host) */
+/* ------------------------------------------------------------------ */
+int ht3d_reduce(ht3d_ctx* ctx, const double* a, long long n, int op, double* out);
+
+/* ------------------------------------------------------------------ */
+/* Dimensionless kernels (Dimensionless/kernels_HT3D.jl,               */
+/* Dimensionless/HydroThermal3D_Alban_v6.jl, tools/Macros.jl)          */
+/* ------------------------------------------------------------------ */
+/* Init_vel!            Dimensionless/kernels_HT3D.jl:73-80 */
+int ht3d_Init_vel(ht3d_ctx* ctx, double* Vx, double* Vy, double* Vz, const double* kx, const double* ky,
+                  const double* kz, const double* Pc_ex, const double* Ty, double Ra, double _dx, double _dy,
+                  double _dz, int nx, int ny, int nz);
+/* InitDarcy!           Dimensionless/kernels_HT3D.jl:82-90 */
+int ht3d_InitDarcy(ht3d_ctx* ctx, double* Ty, double* kx, double* ky, double* kz, const double* Tc_ex,
+                   const double* kfv, double _dt, int nx, int ny, int nz);
+/* Compute_Rp!          Dimensionless/kernels_HT3D.jl:92-97 */
+int ht3d_Compute_Rp(ht3d_ctx* ctx, double* Rp, const double* ky, const double* Ty, double Ra, double _dy,
+                    int nx, int ny, int nz);
+/* InitThermal!         Dimensionless/kernels_HT3D.jl:99-107 */
+int ht3d_InitThermal(ht3d_ctx* ctx, double* Rt, double* kx, double* ky, double* kz, const double* Tc_ex,
+                     const double* ktv, double _dt, int nx, int ny, int nz);
+/* ComputeFlux!         Dimensionless/kernels_HT3D.jl:109-117, Dimensional/kernels_HT3D_dimensional.jl:140-146 */
+int ht3d_ComputeFlux(ht3d_ctx* ctx, double* qx, double* qy, double* qz, const double* kx, const double* ky,
+                     const double* kz, const double* A, double _dx, double _dy, double _dz, int nx, int ny, int nz);
+/* UpdateT!             Dimensionless/kernels_HT3D.jl:119-126 */
+int ht3d_UpdateT(ht3d_ctx* ctx, double* F, double* T, const double* R, const double* qx, const double* qy,
+                 const double* qz, double _dt, double dtau, double _dx, double _dy, double _dz, int nx, int ny, int nz);
+/* ResidualDiffusion!   Dimensionless/kernels_HT3D.jl:128-134 */
+int ht3d_ResidualDiffusion(ht3d_ctx* ctx, double* F, const double* R, const double* qx, const double* qy,
+                           const double* qz, double _dx, double _dy, double _dz, int nx, int ny, int nz);
+/* ResidualDiffusionTransient!  Dimensionless/HydroThermal3D_Alban_v6.jl:84-90 */
+int ht3d_ResidualDiffusionTransient(ht3d_ctx* ctx, double* F, const double* T, const double* R, const double* qx,
+                                    const double* qy, const double* qz, double _dt, double _dx, double _dy,
+                                    double _dz, int nx, int ny, int nz);
+/* UpdateP!             Dimensionless/kernels_HT3D.jl:136-142
+   (== DampedUpdate!    Dimensional/kernels_HT3D_dimensional.jl:316-320) */
+int ht3d_UpdateP(ht3d_ctx* ctx, double* F0, double* P, const double* F, double dampx, double dtau,
+                 int nx, int ny, int nz);
+/* DYRELUpdate!         Dimensional/kernels_HT3D_dimensional.jl:322-326 */
+int ht3d_DYRELUpdate(ht3d_ctx* ctx, double* F0, double* X, const double* F, double h1, double h2, double dtau,
+                     int nx, int ny, int nz);
+/* SetPressureBCs!      Dimensionless/kernels_HT3D.jl:144-154 (x,z Neumann; y Dirichlet Pbot/Ptop) */
+int ht3d_SetPressureBCs(ht3d_ctx* ctx, double* Pc_ex, double Pbot, double Ptop, int nx, int ny, int nz);
+/* Generic six-face ghost BCs covering SetPressureBCs!/SetTemperatureBCs! of
+   Dimensionless/HydroThermal3D_Alban_v6.jl:108-130. type/val: W,E,S,N,B,F.
+   Face ghosts are exact; edge and corner ghosts are not written. */
+int ht3d_SetFaceBCs(ht3d_ctx* ctx, double* X_ex, const int* bc_type6, const double* bc_val6, int nx, int ny, int nz);
+/* KillNorthSouthFluxes!  Dimensionless/HydroThermal3D_Alban_v6.jl:153-159 */
+int ht3d_KillNorthSouthFluxes(ht3d_ctx* ctx, double* Ty, int nx, int ny, int nz);
+/* ResetA!              tools/Macros.jl:171-177 (two arrays of n elements) */
+int ht3d_ResetA(ht3d_ctx* ctx, double* A, double* B, long long n);
+/* Cpy_inn_to_all!      tools/Macros.jl:187-192  A(n^3) = inn(B) */
+int ht3d_Cpy_inn_to_all(ht3d_ctx* ctx, double* A, const double* B_ex, int nx, int ny, int nz);
+/* Cpy_all_to_inn!      tools/Macros.jl:194-199  inn(A) = B(n^3) */
+int ht3d_Cpy_all_to_inn(ht3d_ctx* ctx, double* A_ex, const double* B, int nx, int ny, int nz);
+/* ArrayEqualArray!     tools/Weno5_Routines.jl:271-276 */
+int ht3d_ArrayEqualArray(ht3d_ctx* ctx, double* A, const double* B, long long n);
+/* Multiply             Dimensional/kernels_HT3D_dimensional.jl:106-109 */
+int ht3d_Multiply(ht3d_ctx* ctx, double* a, const double* b, const double* c, long long n);
+
+/* ------------------------------------------------------------------ */
+/* DYREL support kernels (Dimensional/kernels_HT3D_dimensional.jl)     */
+/* ------------------------------------------------------------------ */
+/* GershgorinPoisson!   :207-221 (G <- Gershgorin bound / diagonal, D <- diagonal) */
+int ht3d_GershgorinPoisson(ht3d_ctx* ctx, double* G, double* D, const double* rhoC_eff, const double* kx,
+                           const double* ky, const double* kz, double transient, double dt, double dx, double dy,
+                           double dz, int nx, int ny, int nz);
+/* GershgorinHydro!     :335-347 */
+int ht3d_GershgorinHydro(ht3d_ctx* ctx, double* G, const double* phidrhodP, const double* kx, const double* ky,
+                         const double* kz, double transient, double dt, double dx, double dy, double dz,
+                         int nx, int ny, int nz);
+/* SwapDYREL!           :122-126 */
+int ht3d_SwapDYREL(ht3d_ctx* ctx, double* Xc, double* Yc, const double* X0c_ex, const double* Y0c,
+                   int nx, int ny, int nz);
+/* RayleighQuotientNumerator!   :349-355 */
+int ht3d_RayleighQuotientNumerator(ht3d_ctx* ctx, double* G, const double* Fc0, const double* Fcit,
+                                   const double* Fc, double dtau, long long n);
+/* RayleighQuotientDenominator! :357-363 */
+int ht3d_RayleighQuotientDenominator(ht3d_ctx* ctx, double* G, const double* Fc0, double dtau, long long n);
+
+/* ------------------------------------------------------------------ */
+/* WENO5 advection                                                     */
+/* ------------------------------------------------------------------ */
+/* V{x,y,z}PlusMinus!   tools/Weno5_Routines.jl:5-42 (axis 0,1,2) */
+int ht3d_VPlusMinus(ht3d_ctx* ctx, double* Vm, double* Vp, const double* V, int axis, int nx, int ny, int nz);
+/* dFdx_Weno5!          tools/Weno5_Routines.jl:44-68 */
+int ht3d_dFdx_Weno5(ht3d_ctx* ctx, double* dFdxi, const double* V1, const double* V2, const double* V3,
+                    const double* V4, const double* V5, long long n);
+/* Gradients_{minus,plus}_{x,y,z}_Weno5!  tools/Weno5_Routines.jl:70-128 (sign -1 minus, +1 plus) */
+int ht3d_Gradients_Weno5(ht3d_ctx* ctx, double* v1, double* v2, double* v3, double* v4, double* v5,
+                         const double* Fc_exxx, int axis, int sign, double _dx, double _dy, double _dz,
+                         int nx, int ny, int nz);
+/* Boundaries_{x,y,z}_Weno5!  v1 tools/Weno5_Routines.jl:130-255 (Fc is n^3, fc_ghosted = 0),
+                              v2 tools/Weno5_Routines_v2.jl:221-347 (Fc is ex, fc_ghosted = 1) */
+int ht3d_Boundaries_Weno5(ht3d_ctx* ctx, double* Fc_exxx, const double* Fc, int axis, int type_L, double val_L,
+                          int type_R, double val_R, int fc_ghosted, int nx, int ny, int nz);
+/* Advect! v1           tools/Weno5_Routines.jl:257-262 */
+int ht3d_Advect_v1(ht3d_ctx* ctx, double* Fc, const double* Vxp, const double* dTdxm, const double* Vxm,
+                   const double* dTdxp, double dt, long long n);
+/* TimeAveraging! v1    tools/Weno5_Routines.jl:264-269 */
+int ht3d_TimeAveraging_v1(ht3d_ctx* ctx, double* Fc, const double* Fold, double order, long long n);
+/* Advect! v2           tools/Weno5_Routines_v2.jl:55-212 (quirk 1 = reference v5 stencil) */
+int ht3d_Advect_v2(ht3d_ctx* ctx, double* Fc_ex, const double* X_exxx, const double* V, int axis, double dt,
+                   double _dx, double _dy, double _dz, int quirk, int nx, int ny, int nz);
+/* TimeAveraging! v2    tools/Weno5_Routines_v2.jl:214-219 */
+int ht3d_TimeAveraging_v2(ht3d_ctx* ctx, double* Fc_ex, const double* Fold, double order, int nx, int ny, int nz);
+
+/* Fused advection: one SSP-RK2 (Heun) sweep per axis x, y, z, ghost cells
+   computed on the fly (no exxx buffer).  Replaces AdvectWithWeno5
+   (Dimensionless/kernels_HT3D.jl:156-233, minus its Init_vel! call) for
+   HT3D_WENO_V1 and AdvectWithWeno5_v2 (tools/Weno5_Routines_v2.jl:1-50) for
+   HT3D_WENO_V2_*.  bc_type6/bc_val6: W,E,S,N,B,F.  Needs n >= 3 per axis. */
+int ht3d_weno5_advect(ht3d_ctx* ctx, double* Tc_ex, const double* Vx, const double* Vy, const double* Vz, double dt,
+                      double _dx, double _dy, double _dz, const int* bc_type6, const double* bc_val6, int variant,
+                      int precision, int nx, int ny, int nz);
+
+/* ------------------------------------------------------------------ */
+/* Fused DYREL solver (replaces the loop Dimensional/HydroThermal3D_v18.jl:448-477
+   composed with the dimensionless residuals):
+     F = (R + cX*inn(X) + div q(X)) / PC,  q = -k grad X,
+   cX = _dt gives ResidualDiffusionTransient! (Alban_v6.jl:84-90), cX = 0
+   gives ResidualDiffusion! (kernels_HT3D.jl:128-134); PC is the diagonal of
+   GershgorinPoisson! with rhoC = 1.  Face BCs as ht3d_SetFaceBCs.
+   On return X holds the solution (inner cells + face ghosts as the reference
+   leaves them), F the last residual and F0 the DYREL momentum (both n^3).
+   n_iter_fixed > 0 runs exactly that many iterations with no stop test. */
+int ht3d_dyrel_solve_dimless(ht3d_ctx* ctx, double* X_ex, const double* R, const double* kx, const double* ky,
+                             const double* kz, double cX, double dx, double dy, double dz, const int* bc_type6,
+                             const double* bc_val6, const ht3d_dyrel_params* prm, int n_iter_fixed, double* F,
+                             double* F0, int precision, ht3d_dyrel_stats* stats, int nx, int ny, int nz);
+
+/* n_iter plain pseudo-iterations of the fused DYREL kernel with fixed
+   (h1, h2, dtau) and no checks -- the inner loop of ht3d_dyrel_solve_dimless
+   (Dimensional/HydroThermal3D_v18.jl:451-455 without the check block), for
+   callers that run their own schedule.  invPC is 1/PC (n^3).  The _f32
+   variant takes FP32 fields (the mixed form's inner iteration). */
+int ht3d_dyrel_iterate(ht3d_ctx* ctx, double* X_ex, const double* R, const double* kx, const double* ky,
+                       const double* kz, const double* invPC, double* F0, double cX, double dx, double dy, double dz,
+                       const int* bc_type6, const double* bc_val6, double h1, double h2, double dtau, int n_iter,
+                       int nx, int ny, int nz);
+int ht3d_dyrel_iterate_f32(ht3d_ctx* ctx, float* X_ex, const float* R, const float* kx, const float* ky,
+                           const float* kz, const float* invPC, float* F0, double cX, double dx, double dy, double dz,
+                           const int* bc_type6, const double* bc_val6, double h1, double h2, double dtau, int n_iter,
+                           int nx, int ny, int nz);
+
+/* One time step of the dimensionless Horton-Rogers-Lapwood model:
+   thermal DYREL solve, Darcy DYREL solve, Init_vel!, WENO5 advection and the
+   adaptive dt (Dimensionless/HydroThermal3D_Alban_v6.jl:322-464,
+   Dimensionless/HydroThermal3D_v7.jl:167-222).  Tc_ex, Pc_ex are updated in
+   place; Vx,Vy,Vz receive the Darcy velocity; p->dt is updated when dt_adapt. */
+int ht3d_step_hrl(ht3d_ctx* ctx, double* Tc_ex, double* Pc_ex, const double* ktv, const double* kfv, double* Vx,
+                  double* Vy, double* Vz, ht3d_hrl_params* p, ht3d_dyrel_stats* st_thermal,
+                  ht3d_dyrel_stats* st_darcy, int precision, int nx, int ny, int nz);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HT3D_H */

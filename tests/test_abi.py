@@ -1,0 +1,51 @@
+"""CPU checks of the C ABI: the library loads and exports every symbol the
+header declares, and the ctypes structs match the C structs.  No kernel is
+launched (there may be no GPU here)."""
+import ctypes
+import os
+
+import pytest
+
+from hydrothermal3d_gb300 import _lib, abi
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(_lib.LIBPATH):
+        from hydrothermal3d_gb300 import build
+        build.build()
+    return _lib.load()
+
+
+def test_header_parses_and_lists_entry_points():
+    protos = _lib.parse_header()
+    assert len(protos) >= 40
+    for name in ("ht3d_ctx_create", "ht3d_ComputeFlux", "ht3d_dyrel_solve_dimless", "ht3d_step_hrl",
+                 "ht3d_weno5_advect", "ht3d_reduce"):
+        assert name in protos
+
+
+def test_every_declared_symbol_is_exported(lib):
+    handle = ctypes.CDLL(_lib.LIBPATH)
+    missing = [n for n in _lib.parse_header() if not hasattr(handle, n)]
+    assert not missing, missing
+
+
+def test_struct_layouts_match(lib):
+    assert lib.ht3d_abi_version() == 1
+    assert lib.ht3d_sizeof_dyrel_params() == ctypes.sizeof(abi.DyrelParams)
+    assert lib.ht3d_sizeof_dyrel_stats() == ctypes.sizeof(abi.DyrelStats)
+    assert lib.ht3d_sizeof_hrl_params() == ctypes.sizeof(abi.HrlParams)
+
+
+def test_status_strings(lib):
+    assert lib.ht3d_status_string(0) == b"ok"
+    assert b"NaN" in lib.ht3d_status_string(abi.ERR_NAN)
+    assert b"diverged" in lib.ht3d_status_string(abi.ERR_DIVERGED)
+    assert lib.ht3d_status_string(999) == b"unknown status"
+
+
+def test_null_ctx_is_rejected_without_gpu(lib):
+    assert lib.ht3d_ctx_destroy(None) == abi.ERR_ARG
+    assert lib.ht3d_ctx_launch_count(None) == 0
+    assert lib.ht3d_ComputeFlux(None, *([None] * 7), 1.0, 1.0, 1.0, 4, 4, 4) == abi.ERR_ARG

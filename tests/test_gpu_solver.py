@@ -1,0 +1,160 @@
+"""GPU parity of the fused fast paths (DYREL solver, WENO5 sweep, full HRL
+time step) against the oracle, FP64 and mixed precision.
+
+Tolerances (relative, max-norm over the compared cells):
+  FP64 form  : <= 1e-12 (the plain form's contract; FMA contraction and one
+               reciprocal differ from the oracle by rounding only)
+  mixed form : <= 1e-6 in T after a full step (BASELINE target), solver
+               outputs within the DYREL tolerance.
+Edge and corner ghost cells are excluded (the reference writes them with a
+race; no consumer on the dimensionless path reads them)."""
+import numpy as np
+import pytest
+
+import hydrothermal3d_gb300 as ht
+from hydrothermal3d_gb300 import api, abi, hrl
+from conftest import rel_err, no_edges_mask
+
+pytestmark = pytest.mark.gpu
+
+
+def rnd(rng, *s, lo=-1.0, hi=1.0):
+    return np.asfortranarray(rng.uniform(lo, hi, s))
+
+
+def problem(n, seed=21):
+    nx, ny, nz = n
+    rng = np.random.default_rng(seed)
+    X = rnd(rng, nx + 2, ny + 2, nz + 2)
+    R = rnd(rng, nx, ny, nz)
+    k = [rnd(rng, *s, lo=0.5, hi=2.0) for s in ((nx + 1, ny, nz), (nx, ny + 1, nz), (nx, ny, nz + 1))]
+    return X, R, k
+
+
+BCS = {
+    "thermal": ([0, 0, 1, 1, 0, 0], [0, 0, 1.0, 0.0, 0, 0]),
+    "neumann": ([0] * 6, [0.0] * 6),
+    "mixedbc": ([1, 0, 1, 1, 0, 1], [0.5, 0, 1.0, -1.0, 0, 2.0]),
+}
+
+
+@pytest.mark.parametrize("n", [(1, 1, 1), (5, 4, 3), (33, 17, 9), (40, 24, 70)])
+@pytest.mark.parametrize("bc", ["thermal", "neumann", "mixedbc"])
+@pytest.mark.parametrize("cX", [0.0, 25.0])
+def test_fused_dyrel_fixed_iterations_fp64(ctx, orc, n, bc, cX):
+    nx, ny, nz = n
+    X, R, k = problem(n)
+    types, vals = BCS[bc]
+    prm = abi.DyrelParams.reference(nitout=10)
+    dx, dy, dz = 1.0 / nx, 0.7 / ny, 1.3 / nz
+    Xo, Fo, F0o = X.copy(order="F"), orc.zeros(nx, ny, nz), orc.zeros(nx, ny, nz)
+    so, sto = orc.dyrel_solve_dimless(Xo, R, *k, cX, dx, dy, dz, types, vals, prm, Fo, F0o, n_iter_fixed=23)
+    Xd, Fd, F0d = ht.from_numpy(X), ht.zeros(nx, ny, nz), ht.zeros(nx, ny, nz)
+    std = api.dyrel_solve_dimless(ctx, Xd, ht.from_numpy(R), *[ht.from_numpy(a) for a in k], cX, dx, dy, dz, types,
+                                  vals, prm, Fd, F0d, abi.FP64, n_iter_fixed=23)
+    assert so == 0 and std.status == 0 and std.iters == sto.iters == 23 and std.checks == sto.checks
+    m = no_edges_mask(X.shape)
+    assert rel_err(ht.to_numpy(Xd), Xo, m) <= 1e-12
+    assert rel_err(ht.to_numpy(Fd), Fo) <= 1e-11
+    assert rel_err(ht.to_numpy(F0d), F0o) <= 1e-11
+    assert abs(std.lambda_max - sto.lambda_max) <= 1e-14 * sto.lambda_max
+    assert abs(std.h1 - sto.h1) <= 1e-10 and abs(std.nF_abs - sto.nF_abs) <= 1e-10 * sto.nF_abs
+
+
+@pytest.mark.parametrize("n,bc,cX", [((31, 31, 31), "thermal", 200.0), ((24, 20, 28), "neumann", 0.0)])
+def test_fused_dyrel_converged_solve(ctx, orc, n, bc, cX):
+    """Full solve with the reference stop test: same iteration count, same solution."""
+    nx, ny, nz = n
+    X, R, k = problem(n, seed=22)
+    if bc == "neumann":
+        R -= R.mean()  # compatible right-hand side for the singular problem
+    types, vals = BCS[bc]
+    prm = abi.DyrelParams.reference(tol=1e-9, nitout=100, nitmax=20000)
+    d = (1.0 / nx, 1.0 / ny, 1.0 / nz)
+    Xo, Fo, F0o = X.copy(order="F"), orc.zeros(nx, ny, nz), orc.zeros(nx, ny, nz)
+    so, sto = orc.dyrel_solve_dimless(Xo, R, *k, cX, *d, types, vals, prm, Fo, F0o)
+    for prec in (abi.FP64, abi.MIXED):
+        Xd, Fd, F0d = ht.from_numpy(X), ht.zeros(nx, ny, nz), ht.zeros(nx, ny, nz)
+        std = api.dyrel_solve_dimless(ctx, Xd, ht.from_numpy(R), *[ht.from_numpy(a) for a in k], cX, *d, types, vals,
+                                      prm, Fd, F0d, prec)
+        assert std.status == 0 and std.converged == 1
+        inner = (slice(1, -1),) * 3
+        got, ref = ht.to_numpy(Xd)[inner], Xo[inner]
+        if bc == "neumann":  # defined up to a constant
+            got, ref = got - got.mean(), ref - ref.mean()
+        if prec == abi.FP64:
+            assert std.iters == sto.iters
+            assert rel_err(got, ref) <= 1e-10
+        else:
+            assert abs(std.iters - sto.iters) <= prm.nitout
+            assert rel_err(got, ref) <= 1e-6
+            assert std.nF_rel < prm.tol_rel or std.nF_abs < prm.tol_abs
+
+
+@pytest.mark.parametrize("n", [(3, 3, 3), (17, 9, 12), (64, 48, 40)])
+@pytest.mark.parametrize("variant", [abi.WENO_V1, abi.WENO_V2_REF, abi.WENO_V2_FIXED])
+def test_fused_weno_fp64_and_mixed(ctx, orc, n, variant):
+    nx, ny, nz = n
+    rng = np.random.default_rng(31)
+    T = np.asfortranarray(rng.uniform(0, 1, (nx + 2, ny + 2, nz + 2)))
+    V = [rnd(rng, *s) for s in ((nx + 1, ny, nz), (nx, ny + 1, nz), (nx, ny, nz + 1))]
+    types, vals = [0, 0, 1, 1, 2, 2], [0, 0, 1.0, 0.0, 0, 0]
+    h = (float(nx), float(ny), float(nz))
+    dt = 0.2 / max(h)
+    To = T.copy(order="F")
+    if variant == abi.WENO_V1:
+        orc.call("AdvectWithWeno5_v1", To, *V, dt, *h, orc.int6(*types), orc.dbl6(*vals), nx, ny, nz)
+    else:
+        import ctypes
+        orc.call("AdvectWithWeno5_v2", To, *V, dt, *h, orc.int6(*types), orc.dbl6(*vals),
+                 ctypes.c_int(1 if variant == abi.WENO_V2_REF else 0), nx, ny, nz)
+    inner = (slice(1, -1),) * 3
+    for prec, tol in ((abi.FP64, 1e-12), (abi.MIXED, 2e-6)):
+        Td = ht.from_numpy(T)
+        api.weno5_advect(ctx, Td, *[ht.from_numpy(v) for v in V], dt, *h, types, vals, variant, prec)
+        got = ht.to_numpy(Td)
+        assert rel_err(got[inner], To[inner]) <= tol
+        np.testing.assert_array_equal(got[0], T[0])  # ghosts untouched
+
+
+@pytest.mark.parametrize("n", [(16, 16, 16), (33, 31, 29)])
+def test_step_hrl_fp64_matches_oracle(ctx, orc, n):
+    nx, ny, nz = n
+    T, P, ktv, kfv = hrl.initial_fields(nx, ny, nz, seed=1)
+    p_o = hrl.params(nx, ny, nz, nitout=100)
+    p_d = hrl.params(nx, ny, nz, nitout=100)
+    V = [np.zeros(s, order="F") for s in ((nx + 1, ny, nz), (nx, ny + 1, nz), (nx, ny, nz + 1))]
+    Td, Pd = ht.from_numpy(T), ht.from_numpy(P)
+    Vd = [ht.zeros(*v.shape) for v in V]
+    ktd, kfd = ht.from_numpy(ktv), ht.from_numpy(kfv)
+    m = no_edges_mask(T.shape)
+    for step in range(3):
+        s, st_t, st_d = orc.step_hrl(T, P, ktv, kfv, *V, p_o)
+        assert s == 0
+        gt, gd = api.step_hrl(ctx, Td, Pd, ktd, kfd, *Vd, p_d, abi.FP64)
+        assert gt.iters == st_t.iters and gd.iters == st_d.iters
+        assert rel_err(ht.to_numpy(Td), T, m) <= 1e-12
+        Pn, Pg = P[1:-1, 1:-1, 1:-1], ht.to_numpy(Pd)[1:-1, 1:-1, 1:-1]
+        assert rel_err(Pg - Pg.mean(), Pn - Pn.mean()) <= 1e-10
+        for a, b in zip(Vd, V):
+            assert rel_err(ht.to_numpy(a), b) <= 1e-9
+        assert abs(p_d.dt - p_o.dt) <= 1e-9 * p_o.dt
+
+
+def test_step_hrl_mixed_error_vs_oracle(ctx, orc):
+    nx = ny = nz = 32
+    T, P, ktv, kfv = hrl.initial_fields(nx, ny, nz, seed=1)
+    p_o = hrl.params(nx, ny, nz, nitout=100)
+    p_d = hrl.params(nx, ny, nz, nitout=100)
+    V = [np.zeros(s, order="F") for s in ((nx + 1, ny, nz), (nx, ny + 1, nz), (nx, ny, nz + 1))]
+    Td, Pd = ht.from_numpy(T), ht.from_numpy(P)
+    Vd = [ht.zeros(*v.shape) for v in V]
+    ktd, kfd = ht.from_numpy(ktv), ht.from_numpy(kfv)
+    inner = (slice(1, -1),) * 3
+    for step in range(3):
+        orc.step_hrl(T, P, ktv, kfv, *V, p_o)
+        gt, gd = api.step_hrl(ctx, Td, Pd, ktd, kfd, *Vd, p_d, abi.MIXED)
+        assert gt.status == 0 and gd.status == 0
+        # the same dt sequence keeps the comparison meaningful
+        p_d.dt = p_o.dt
+    assert rel_err(ht.to_numpy(Td)[inner], T[inner]) <= 1e-6
