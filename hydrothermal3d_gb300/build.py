@@ -3,9 +3,9 @@
 Every translation unit under ``csrc/`` is compiled in parallel for one
 architecture (``-gencode arch=compute_103a,code=sm_103a``) and linked into
 ``hydrothermal3d_gb300/libht3d.so``.  The granular, reference-shaped kernels
-are compiled with ``-fmad=false`` so their FP64 rounding follows the
-reference's statement order exactly; the fused fast paths keep FMA
-contraction.
+and the plain FP64 fused paths are compiled with ``-fmad=false`` so their
+FP64 rounding follows the reference's statement order exactly (Julia does not
+contract a*b+c); the mixed-precision paths keep FMA contraction.
 """
 import concurrent.futures as cf
 import os
@@ -22,7 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3", "--expt-relaxed-constexpr",
           "-I", INCLUDE]
 # translation units that restate reference kernels statement by statement
-NO_FMA = {"kernels_dimless.cu", "kernels_dim.cu"}
+NO_FMA = {"kernels_dimless.cu", "kernels_dim.cu", "dyrel_fp64.cu", "step.cu", "weno.cu"}
 
 
 def _nvcc() -> str:

@@ -1,0 +1,238 @@
+// Fused DYREL solver for the dimensionless diffusion problems of the
+// HydroThermal3D hot path.
+//
+// One launch of k_dyrel_iter performs one pseudo-iteration of the reference
+// loop Dimensional/HydroThermal3D_v18.jl:448-455 composed with the
+// dimensionless residual:
+//     SetFaceBCs(X) ; ComputeFlux!(q, k, X) ;
+//     F = (R + cX*inn(X) + div q) / PC ;  DYRELUpdate!(F0, X, F, h1, h2, dtau)
+// reading every field once.  Ghost cells are evaluated on the fly from the
+// adjacent inner cell; the updated field goes to a second buffer (ping-pong),
+// so every thread sees the pre-iteration state exactly like the reference's
+// separate launches do.  The output buffer's face ghosts receive BC(X_in),
+// which is the state the reference leaves after the same iteration.
+//
+// Thread layout: a 32x8 tile of (x,y) columns per block, marching in z over a
+// chunk of planes.  The z-face flux is carried in a register (each z face is
+// evaluated once); x/y neighbours come through L1.
+#pragma once
+#include <type_traits>
+#include "ht3d_internal.cuh"
+
+namespace {
+
+struct DyrelScal {
+    double h1, h2, dtau, cX, _dx, _dy, _dz;
+};
+
+template <typename T>
+struct BC6 {
+    int dir[6];  // 1 = Dirichlet, 0 = Neumann
+    T val2[6];   // 2*value
+};
+
+template <typename T>
+__device__ __forceinline__ T ghost(const BC6<T>& bc, int f, T inner) {
+    return bc.dir[f] ? bc.val2[f] - inner : inner;
+}
+
+enum { MODE_PLAIN = 0, MODE_STOREF = 1, MODE_CHECK = 2 };
+
+constexpr int TX = 32, TY = 8;
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(TX* TY) k_dyrel_iter(const T* __restrict__ Xin, T* __restrict__ Xout,
+                                                       const T* __restrict__ R, const T* __restrict__ kx,
+                                                       const T* __restrict__ ky, const T* __restrict__ kz,
+                                                       const T* __restrict__ PCx, T* __restrict__ F0,
+                                                       T* __restrict__ F, DyrelScal s, BC6<T> bc, int nx, int ny,
+                                                       int nz, int zchunk, double* __restrict__ partials) {
+    const int i = blockIdx.x * TX + threadIdx.x;
+    const int j = blockIdx.y * TY + threadIdx.y;
+    const int k0 = blockIdx.z * zchunk;
+    const int k1 = min(nz, k0 + zchunk);
+    double acc[3] = {0.0, 0.0, 0.0};
+    const T h1 = (T)s.h1, h2 = (T)s.h2, dtau = (T)s.dtau, cX = (T)s.cX, _dx = (T)s._dx, _dy = (T)s._dy, _dz = (T)s._dz;
+    if (i < nx && j < ny && k0 < k1) {
+        const int n1 = nx + 2, n2 = ny + 2;
+        const long long pl = (long long)n1 * n2;  // ex plane
+        const long long cpl = (long long)nx * ny;  // cell plane
+        // pointers to this column
+        const T* xcol = Xin + (i + 1) + (long long)n1 * (j + 1);
+        T* ocol = Xout + (i + 1) + (long long)n1 * (j + 1);
+        const long long ccol = i + (long long)nx * j;
+        const T* kxcol = kx + i + (long long)(nx + 1) * j;
+        const T* kycol = ky + i + (long long)nx * j;
+        const T* kzcol = kz + ccol;
+        T xc = xcol[pl * (k0 + 1)];
+        T xb = (k0 == 0) ? ghost(bc, 4, xc) : xcol[pl * k0];
+        T qB = -kzcol[cpl * k0] * (_dz * (xc - xb));
+        for (int k = k0; k < k1; ++k) {
+            const long long e = pl * (k + 1);
+            const T xf = (k == nz - 1) ? ghost(bc, 5, xc) : xcol[e + pl];
+            const T xw = (i == 0) ? ghost(bc, 0, xc) : xcol[e - 1];
+            const T xe = (i == nx - 1) ? ghost(bc, 1, xc) : xcol[e + 1];
+            const T xs = (j == 0) ? ghost(bc, 2, xc) : xcol[e - n1];
+            const T xn = (j == ny - 1) ? ghost(bc, 3, xc) : xcol[e + n1];
+            const long long c = ccol + cpl * k;
+            const T qF = -kzcol[cpl * (k + 1)] * (_dz * (xf - xc));
+            const long long fxo = (long long)(nx + 1) * ny * k;
+            const long long fyo = (long long)nx * (ny + 1) * k;
+            const T qW = -kxcol[fxo] * (_dx * (xc - xw));
+            const T qE = -kxcol[fxo + 1] * (_dx * (xe - xc));
+            const T qS = -kycol[fyo] * (_dy * (xc - xs));
+            const T qN = -kycol[fyo + nx] * (_dy * (xn - xc));
+            const T fu = R[c] + cX * xc + _dx * (qE - qW) + _dy * (qN - qS) + _dz * (qF - qB);
+            // FP64: the reference's F /= PC (exact rounding); FP32: PCx holds 1/PC
+            T f;
+            if constexpr (std::is_same<T, double>::value) f = fu / PCx[c];
+            else f = fu * PCx[c];
+            const T f0 = h1 * F0[c] + h2 * f;
+            F0[c] = f0;
+            ocol[e] = xc - dtau * f0;
+            if (MODE == MODE_CHECK) {
+                const T fit = F[c];
+                const double d = (double)dtau * (double)f0;
+                acc[0] += fabs((double)fu);
+                acc[1] += -d * ((double)f - (double)fit);
+                acc[2] += d * d;
+            }
+            if (MODE >= MODE_STOREF) F[c] = f;
+            // face ghosts of the output = BC of the input (reference state)
+            if (i == 0) ocol[e - 1] = xw;
+            if (i == nx - 1) ocol[e + 1] = xe;
+            if (j == 0) ocol[e - n1] = xs;
+            if (j == ny - 1) ocol[e + n1] = xn;
+            if (k == 0) ocol[e - pl] = xb;
+            if (k == nz - 1) ocol[e + pl] = xf;
+            xb = xc;
+            xc = xf;
+            qB = qF;
+        }
+    }
+    if (MODE == MODE_CHECK) {
+        block_reduce<RED_SUM, 3>(acc);
+        if (threadIdx.x == 0 && threadIdx.y == 0) {
+            const long long b = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
+            partials[3 * b + 0] = acc[0];
+            partials[3 * b + 1] = acc[1];
+            partials[3 * b + 2] = acc[2];
+        }
+    }
+}
+
+// Gershgorin bound of the preconditioned operator (GershgorinPoisson!,
+// Dimensional/kernels_HT3D_dimensional.jl:207-221 with a scalar rhoC) ->
+// invPC = 1/D and per-block max of G/D.
+template <int INV>
+__global__ void k_dyrel_setup(const double* __restrict__ kx, const double* __restrict__ ky,
+                              const double* __restrict__ kz, double rhoC, double transient, double dt, double dx,
+                              double dy, double dz, int nx, int ny, int nz, double* __restrict__ invPC,
+                              double* __restrict__ partials) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    double v[1] = {-INFINITY};
+    if (i < nx && j < ny && k < nz) {
+        const double kW = kx[ix3(i, j, k, nx + 1, ny)], kE = kx[ix3(i + 1, j, k, nx + 1, ny)];
+        const double kS = ky[ix3(i, j, k, nx, ny + 1)], kN = ky[ix3(i, j + 1, k, nx, ny + 1)];
+        const double kB = kz[ix3(i, j, k, nx, ny)], kF = kz[ix3(i, j, k + 1, nx, ny)];
+        const double diag = ((kB / dz + kF / dz) / dz + (kN / dy + kS / dy) / dy + (kE / dx + kW / dx) / dx + rhoC * transient / dt);
+        double g = fabs(kE / (dx * dx)) + fabs(kW / (dx * dx)) + fabs(kN / (dy * dy)) + fabs(kS / (dy * dy)) +
+                   fabs(kB / (dz * dz)) + fabs(kF / (dz * dz)) + fabs(diag);
+        g /= diag;
+        invPC[ix3(i, j, k, nx, ny)] = INV ? 1.0 / diag : diag;
+        v[0] = g;
+    }
+    block_reduce<RED_MAX, 1>(v);
+    if (threadIdx.x == 0 && threadIdx.y == 0)
+        partials[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = v[0];
+}
+
+// copy inner cells + face ghosts (not edges/corners) of a ghosted field
+template <typename T>
+__global__ void k_copy_ex_faces(T* __restrict__ dst, const T* __restrict__ src, int nx, int ny, int nz) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    const int n1 = nx + 2, n2 = ny + 2, n3 = nz + 2;
+    if (i >= n1 || j >= n2 || k >= n3) return;
+    const int nb = (i == 0 || i == n1 - 1) + (j == 0 || j == n2 - 1) + (k == 0 || k == n3 - 1);
+    if (nb <= 1) dst[ix3(i, j, k, n1, n2)] = src[ix3(i, j, k, n1, n2)];
+}
+
+struct IterLaunch {
+    dim3 grid, block;
+    int zchunk;
+    long long nblocks;
+};
+
+inline IterLaunch iter_launch(ht3d_ctx* ctx, int nx, int ny, int nz) {
+    IterLaunch L;
+    L.block = dim3(TX, TY, 1);
+    const int gx = (nx + TX - 1) / TX, gy = (ny + TY - 1) / TY;
+    const long long tiles = (long long)gx * gy;
+    const long long target = (long long)ctx->num_sms * 6;
+    int zc = (int)std::max<long long>(1, std::min<long long>(nz, (target + tiles - 1) / tiles));
+    L.zchunk = (nz + zc - 1) / zc;
+    zc = (nz + L.zchunk - 1) / L.zchunk;
+    L.grid = dim3(gx, gy, zc);
+    L.nblocks = tiles * zc;
+    return L;
+}
+
+}  // namespace
+
+
+struct DyrelState {
+    double lmax, lmin, dtau, c, h1, h2;
+};
+
+inline void dyrel_init_params(const ht3d_dyrel_params* prm, double lmax, DyrelState& S) {
+    S.lmax = lmax;
+    S.lmin = lmax / prm->lmin_ratio;
+    S.dtau = 2.0 / sqrt(lmax) * prm->cfl;
+    S.c = 2.0 * sqrt(S.lmin) * prm->cfact;
+    S.h1 = (2 - S.c * S.dtau) / (2 + S.c * S.dtau);
+    S.h2 = 2 * S.dtau / (2 + S.c * S.dtau);
+}
+
+inline bool is_check(int iter, int nitout) { return (iter % nitout == 0) || iter <= 2; }
+
+
+// ---------------------------------------------------------------------------
+// n_iter plain pseudo-iterations with fixed (h1, h2, dtau): the solver's inner
+// loop without checks.  PCx is PC (FP64) or 1/PC (FP32).
+// ---------------------------------------------------------------------------
+template <typename T>
+static int dyrel_iterate_impl(ht3d_ctx* ctx, T* X, const T* R, const T* kx, const T* ky, const T* kz, const T* PCx,
+                              T* F0, double cX, double dx, double dy, double dz, const int* bc_type6,
+                              const double* bc_val6, double h1, double h2, double dtau, int n_iter, int nx, int ny,
+                              int nz, int slot) {
+    ht3d_check_dims(nx, ny, nz, 1);
+    HT3D_REQUIRE(X && R && kx && ky && kz && PCx && F0 && bc_type6 && bc_val6, "null argument");
+    HT3D_REQUIRE(n_iter >= 0, "n_iter must be >= 0");
+    const long long nex = (long long)(nx + 2) * (ny + 2) * (nz + 2);
+    T* X2 = (T*)ht3d_scratch(ctx, slot, sizeof(T) * nex);
+    BC6<T> bc;
+    for (int f = 0; f < 6; ++f) {
+        HT3D_REQUIRE(bc_type6[f] == HT3D_BC_NEUMANN || bc_type6[f] == HT3D_BC_DIRICHLET, "face BC type must be 0 or 1");
+        bc.dir[f] = bc_type6[f];
+        bc.val2[f] = (T)(2.0 * bc_val6[f]);
+    }
+    IterLaunch L = iter_launch(ctx, nx, ny, nz);
+    DyrelScal sc{h1, h2, dtau, cX, 1.0 / dx, 1.0 / dy, 1.0 / dz};
+    T* cur = X;
+    T* nxt = X2;
+    for (int it = 0; it < n_iter; ++it) {
+        HT3D_LAUNCH(ctx, (k_dyrel_iter<T, MODE_PLAIN>), L.grid, L.block, 0, cur, nxt, R, kx, ky, kz, PCx, F0,
+                    (T*)nullptr, sc, bc, nx, ny, nz, L.zchunk, (double*)nullptr);
+        std::swap(cur, nxt);
+    }
+    if (cur != X) {
+        dim3 b(32, 8, 1), g((nx + 2 + 31) / 32, (ny + 2 + 7) / 8, nz + 2);
+        HT3D_LAUNCH(ctx, k_copy_ex_faces<T>, g, b, 0, X, cur, nx, ny, nz);
+    }
+    return HT3D_OK;
+}
+

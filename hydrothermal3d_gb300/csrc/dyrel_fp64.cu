@@ -1,0 +1,134 @@
+// Plain FP64 DYREL solver.  Compiled with -fmad=false: every pseudo-iteration
+// rounds exactly like the reference's separate kernels (no FMA contraction,
+// F divided by PC), so the solver differs from the reference only through the
+// summation order of its norm and Rayleigh-quotient reductions.
+#include "dyrel_common.cuh"
+
+int ht3d_dyrel_solve_fp64(ht3d_ctx* ctx, double* X, const double* R, const double* kx, const double* ky,
+                          const double* kz, double cX, double dx, double dy, double dz, const int* bc_type6,
+                          const double* bc_val6, const ht3d_dyrel_params* prm, int n_iter_fixed, double* F, double* F0,
+                          ht3d_dyrel_stats* st, int nx, int ny, int nz) {
+    const long long n = (long long)nx * ny * nz;
+    const long long nex = (long long)(nx + 2) * (ny + 2) * (nz + 2);
+    double* PC = (double*)ht3d_scratch(ctx, SLOT_PC, sizeof(double) * n);
+    double* X2 = (double*)ht3d_scratch(ctx, SLOT_X2, sizeof(double) * nex);
+    IterLaunch L = iter_launch(ctx, nx, ny, nz);
+    const long long nparts = std::max<long long>(L.nblocks, (long long)((nx + 31) / 32) * ((ny + 7) / 8) * nz);
+    double* parts = (double*)ht3d_scratch(ctx, SLOT_PARTIALS, sizeof(double) * 3 * nparts);
+    double* dres = (double*)ht3d_scratch(ctx, SLOT_RESULT, sizeof(double) * 64);
+
+    BC6<double> bc;
+    for (int f = 0; f < 6; ++f) {
+        HT3D_REQUIRE(bc_type6[f] == HT3D_BC_NEUMANN || bc_type6[f] == HT3D_BC_DIRICHLET, "face BC type must be 0 or 1");
+        bc.dir[f] = bc_type6[f];
+        bc.val2[f] = 2.0 * bc_val6[f];
+    }
+    // Gershgorin lambda_max and preconditioner
+    {
+        dim3 b(32, 8, 1), g((nx + 31) / 32, (ny + 7) / 8, nz);
+        const double transient = cX != 0.0 ? 1.0 : 0.0, dt = cX != 0.0 ? 1.0 / cX : 1.0;
+        HT3D_LAUNCH(ctx, k_dyrel_setup<0>, g, b, 0, kx, ky, kz, 1.0, transient, dt, dx, dy, dz, nx, ny, nz, PC, parts);
+        HT3D_LAUNCH(ctx, (k_reduce_partials<RED_MAX, 1>), 1, 1024, 0, parts, (int)(g.x * g.y * g.z), dres);
+        ht3d_fetch_results(ctx, dres, 1);
+    }
+    DyrelState S;
+    dyrel_init_params(prm, ctx->h_result[0], S);
+    HT3D_CUDA(cudaMemsetAsync(F, 0, sizeof(double) * n, ctx->stream));
+    HT3D_CUDA(cudaMemsetAsync(F0, 0, sizeof(double) * n, ctx->stream));
+
+    DyrelScal sc;
+    sc.cX = cX;
+    sc._dx = 1.0 / dx;
+    sc._dy = 1.0 / dy;
+    sc._dz = 1.0 / dz;
+    double* cur = X;
+    double* nxt = X2;
+    double nF_abs = 0., nF_rel = 0., nF_ini = 0.;
+    int it_done = 0, converged = 0, status = HT3D_OK, checks = 0;
+    const int nmax = n_iter_fixed > 0 ? n_iter_fixed : prm->nitmax;
+    HT3D_REQUIRE(prm->nitout >= 1, "nitout must be >= 1");
+    for (int iter = 1; iter <= nmax; ++iter) {
+        const bool chk = is_check(iter, prm->nitout);
+        const bool storef = !chk && (iter == nmax || is_check(iter + 1, prm->nitout));
+        sc.h1 = S.h1;
+        sc.h2 = S.h2;
+        sc.dtau = S.dtau;
+        if (chk)
+            HT3D_LAUNCH(ctx, (k_dyrel_iter<double, MODE_CHECK>), L.grid, L.block, 0, cur, nxt, R, kx, ky, kz, PC, F0,
+                        F, sc, bc, nx, ny, nz, L.zchunk, parts);
+        else if (storef)
+            HT3D_LAUNCH(ctx, (k_dyrel_iter<double, MODE_STOREF>), L.grid, L.block, 0, cur, nxt, R, kx, ky, kz, PC,
+                        F0, F, sc, bc, nx, ny, nz, L.zchunk, parts);
+        else
+            HT3D_LAUNCH(ctx, (k_dyrel_iter<double, MODE_PLAIN>), L.grid, L.block, 0, cur, nxt, R, kx, ky, kz, PC,
+                        F0, F, sc, bc, nx, ny, nz, L.zchunk, parts);
+        std::swap(cur, nxt);
+        it_done = iter;
+        if (chk) {
+            ++checks;
+            HT3D_LAUNCH(ctx, (k_reduce_partials<RED_SUM, 3>), 1, 1024, 0, parts, (int)L.nblocks, dres);
+            ht3d_fetch_results(ctx, dres, 3);
+            const double s_abs = ctx->h_result[0], s_num = ctx->h_result[1], s_den = ctx->h_result[2];
+            nF_abs = s_abs / (double)n / sqrt((double)n) * prm->norm_scale;
+            if (iter == 1) nF_ini = nF_abs;
+            nF_rel = nF_abs / nF_ini;
+            if (std::isnan(nF_abs)) { status = HT3D_ERR_NAN; break; }
+            if (nF_rel > 100) { status = HT3D_ERR_DIVERGED; break; }
+            if (iter > 1) {
+                S.lmin = fabs(s_num) / fabs(s_den);
+                S.c = 2.0 * sqrt(S.lmin) * prm->cfact;
+                S.h1 = (2 - S.c * S.dtau) / (2 + S.c * S.dtau);
+                S.h2 = 2 * S.dtau / (2 + S.c * S.dtau);
+            }
+            if (n_iter_fixed <= 0 && (nF_abs < prm->tol_abs || nF_rel < prm->tol_rel)) { converged = 1; break; }
+        }
+    }
+    if (cur != X) {
+        dim3 b(32, 8, 1), g((nx + 2 + 31) / 32, (ny + 2 + 7) / 8, nz + 2);
+        HT3D_LAUNCH(ctx, k_copy_ex_faces<double>, g, b, 0, X, cur, nx, ny, nz);
+    }
+    if (st) {
+        st->iters = it_done; st->converged = converged; st->status = status; st->checks = checks;
+        st->nF_abs = nF_abs; st->nF_rel = nF_rel; st->nF_ini = nF_ini; st->lambda_min = S.lmin;
+        st->lambda_max = S.lmax; st->h1 = S.h1; st->h2 = S.h2; st->dtau = S.dtau;
+    }
+    return status;
+}
+
+
+
+int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const double* kx, const double* ky,
+                           const double* kz, double cX, double dx, double dy, double dz, const int* bc_type6,
+                           const double* bc_val6, const ht3d_dyrel_params* prm, int n_iter_fixed, double* F,
+                           double* F0, ht3d_dyrel_stats* st, int nx, int ny, int nz);
+
+extern "C" int ht3d_dyrel_solve_dimless(ht3d_ctx* ctx, double* X_ex, const double* R, const double* kx,
+                                        const double* ky, const double* kz, double cX, double dx, double dy, double dz,
+                                        const int* bc_type6, const double* bc_val6, const ht3d_dyrel_params* prm,
+                                        int n_iter_fixed, double* F, double* F0, int precision, ht3d_dyrel_stats* stats,
+                                        int nx, int ny, int nz) {
+    return ht3d_guard(ctx, [&]() {
+        ht3d_check_dims(nx, ny, nz, 1);
+        HT3D_REQUIRE(X_ex && R && kx && ky && kz && bc_type6 && bc_val6 && prm && F && F0, "null argument");
+        HT3D_REQUIRE(prm->nitout >= 1 && prm->nitmax >= 1, "nitout and nitmax must be >= 1");
+        if (precision == HT3D_FP64)
+            return ht3d_dyrel_solve_fp64(ctx, X_ex, R, kx, ky, kz, cX, dx, dy, dz, bc_type6, bc_val6, prm, n_iter_fixed,
+                                         F, F0, stats, nx, ny, nz);
+        if (precision == HT3D_MIXED)
+            return ht3d_dyrel_solve_mixed(ctx, X_ex, R, kx, ky, kz, cX, dx, dy, dz, bc_type6, bc_val6, prm,
+                                          n_iter_fixed, F, F0, stats, nx, ny, nz);
+        throw ht3d_error(HT3D_ERR_ARG, "unknown precision");
+    });
+}
+
+
+extern "C" int ht3d_dyrel_iterate(ht3d_ctx* ctx, double* X_ex, const double* R, const double* kx, const double* ky,
+                                  const double* kz, const double* PC, double* F0, double cX, double dx, double dy,
+                                  double dz, const int* bc_type6, const double* bc_val6, double h1, double h2,
+                                  double dtau, int n_iter, int nx, int ny, int nz) {
+    return ht3d_guard(ctx, [&]() {
+        return dyrel_iterate_impl<double>(ctx, X_ex, R, kx, ky, kz, PC, F0, cX, dx, dy, dz, bc_type6, bc_val6, h1,
+                                          h2, dtau, n_iter, nx, ny, nz, SLOT_AUX0);
+    });
+}
+

@@ -36,25 +36,6 @@ __device__ __forceinline__ double weno5_ref(double v1, double v2, double v3, dou
     return w1 * p1 + w2 * p2 + w3 * p3;
 }
 
-// Fast-path FP64 form: the same weights with one reciprocal of the weight sum
-// instead of three divisions (differs from the reference by rounding only).
-__device__ __forceinline__ double weno5_fast(double v1, double v2, double v3, double v4, double v5) {
-    const double p1 = v1 * (1.0 / 3.0) - (7.0 / 6.0) * v2 + (11.0 / 6.0) * v3;
-    const double p2 = -v2 * (1.0 / 6.0) + (5.0 / 6.0) * v3 + v4 * (1.0 / 3.0);
-    const double p3 = v3 * (1.0 / 3.0) + (5.0 / 6.0) * v4 - v5 * (1.0 / 6.0);
-    const double maxV = fmax(fmax(fmax(fmax(v1 * v1, v2 * v2), v3 * v3), v4 * v4), v5 * v5);
-    const double e = 1e-99 + 1e-6 * maxV;
-    const double a1 = v1 - 2.0 * v2 + v3, b1 = v1 - 4.0 * v2 + 3.0 * v3;
-    const double a2 = v2 - 2.0 * v3 + v4, b2 = v2 - v4;
-    const double a3 = v3 - 2.0 * v4 + v5, b3 = 3.0 * v3 - 4.0 * v4 + v5;
-    const double s1 = (13.0 / 12.0) * (a1 * a1) + 0.25 * (b1 * b1) + e;
-    const double s2 = (13.0 / 12.0) * (a2 * a2) + 0.25 * (b2 * b2) + e;
-    const double s3 = (13.0 / 12.0) * (a3 * a3) + 0.25 * (b3 * b3) + e;
-    const double w1 = 0.1 / (s1 * s1), w2 = 0.6 / (s2 * s2), w3 = 0.3 / (s3 * s3);
-    const double iw = 1.0 / (w1 + w2 + w3);
-    return (w1 * p1 + w2 * p2 + w3 * p3) * iw;
-}
-
 // FP32 form for the mixed-precision path.  The reference's epsilon floor
 // 1e-99 underflows in FP32; 1e-18 is the smallest floor whose square stays a
 // normal FP32 number, so a flat field still yields the linear weights.
@@ -99,7 +80,8 @@ __device__ __forceinline__ double line_at(const double* __restrict__ line, long 
 }
 
 // One SSP-RK2 stage along AXIS on ghosted (ex) fields.
-//   PREC 0: FP64 reference-order arithmetic (parity form)
+//   PREC 0: FP64 reference-order arithmetic (parity form; this translation
+//           unit is compiled with -fmad=false)
 //   PREC 1: FP32 stencil arithmetic, FP64 state (mixed form)
 //   STAGE 1: dst = src - dt*(Vp*dFm + Vm*dFp)
 //   STAGE 2: dst = 0.5*(src - dt*(...)) + 0.5*T0   (TimeAveraging!, order 2)
@@ -134,10 +116,10 @@ __global__ void __launch_bounds__(256) k_weno_stage(const double* __restrict__ s
         // x[o] holds X[I+o-3]
         const double m1 = h * (x[1] - x[0]), m2 = h * (x[2] - x[1]), m3 = h * (x[3] - x[2]), m4 = h * (x[4] - x[3]);
         const double m5 = QUIRK ? h * (x[5] - x[2]) : h * (x[5] - x[4]);
-        const double dFm = weno5_fast(m1, m2, m3, m4, m5);
+        const double dFm = weno5_ref(m1, m2, m3, m4, m5);
         const double p1 = h * (x[6] - x[5]), p2 = h * (x[5] - x[4]), p3 = h * (x[4] - x[3]), p4 = h * (x[3] - x[2]);
         const double p5 = h * (x[2] - x[1]);
-        const double dFp = weno5_fast(p1, p2, p3, p4, p5);
+        const double dFp = weno5_ref(p1, p2, p3, p4, p5);
         rhs = Vp * dFm + Vm * dFp;
     } else {
         const float hf = (float)h;

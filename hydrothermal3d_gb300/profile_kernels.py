@@ -1,0 +1,75 @@
+"""Run one hot kernel of libht3d in isolation, for timing and ncu captures.
+
+  python -m hydrothermal3d_gb300.profile_kernels --kernel dyrel_f32 --n 255 --iters 5
+  ncu --set full --clock-control none -k regex:k_dyrel_iter -s 2 -c 1 -o out \\
+      python -m hydrothermal3d_gb300.profile_kernels --kernel dyrel_f32 --n 255 --iters 5
+
+Kernels: dyrel_f32 (mixed-form pseudo-iteration), dyrel_f64 (plain FP64
+pseudo-iteration), weno_f64 / weno_mixed (one fused WENO5 advection).
+Prints the average time per launch measured with CUDA events.
+"""
+import argparse
+import json
+
+import torch
+
+import hydrothermal3d_gb300 as ht
+from hydrothermal3d_gb300 import abi, hrl
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--kernel", default="dyrel_f32", choices=["dyrel_f32", "dyrel_f64", "weno_f64", "weno_mixed"])
+    ap.add_argument("--n", type=int, default=255)
+    ap.add_argument("--iters", type=int, default=5)
+    a = ap.parse_args()
+    n = a.n
+    stream = torch.cuda.Stream()
+    ctx = ht.Context(device=0, stream=stream.cuda_stream)
+    d = 1.0 / n
+    bt, bv = abi.int6(0, 0, 1, 1, 0, 0), abi.dbl6(0, 0, 1, 0, 0, 0)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if a.kernel.startswith("dyrel"):
+        dt = torch.float32 if a.kernel == "dyrel_f32" else torch.float64
+        X = ht.zeros(n + 2, n + 2, n + 2, dtype=dt).uniform_(0, 1)
+        R = ht.zeros(n, n, n, dtype=dt).uniform_(-1, 1)
+        k = [ht.ones(n + 1, n, n, dtype=dt), ht.ones(n, n + 1, n, dtype=dt), ht.ones(n, n, n + 1, dtype=dt)]
+        pc = 6.0 * n * n
+        PCx = ht.ones(n, n, n, dtype=dt) * (1.0 / pc if a.kernel == "dyrel_f32" else pc)
+        F0 = ht.zeros(n, n, n, dtype=dt)
+        name = "ht3d_dyrel_iterate_f32" if a.kernel == "dyrel_f32" else "ht3d_dyrel_iterate"
+        args = lambda m: (X.data_ptr(), R.data_ptr(), k[0].data_ptr(), k[1].data_ptr(), k[2].data_ptr(),
+                          PCx.data_ptr(), F0.data_ptr(), 0.0, d, d, d, bt, bv, 0.99, 0.05, 0.01, m, n, n, n)
+        torch.cuda.synchronize()
+        ctx.call(name, *args(2))
+        ctx.synchronize()
+        e0.record(stream)
+        ctx.call(name, *args(a.iters))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1e3 / a.iters
+        s = 4 if a.kernel == "dyrel_f32" else 8
+        alg = hrl.bytes_per_iteration(n, n, n, s)
+        print(json.dumps({"kernel": a.kernel, "n": n, "us_per_launch": t * 1e6, "alg_GBs": alg / t / 1e9}))
+    else:
+        prec = abi.FP64 if a.kernel == "weno_f64" else abi.MIXED
+        T = ht.zeros(n + 2, n + 2, n + 2).uniform_(0, 1)
+        V = [ht.zeros(n + 1, n, n).uniform_(-1, 1), ht.zeros(n, n + 1, n).uniform_(-1, 1), ht.zeros(n, n, n + 1).uniform_(-1, 1)]
+        args = (T.data_ptr(), V[0].data_ptr(), V[1].data_ptr(), V[2].data_ptr(), 0.1 * d, float(n), float(n), float(n),
+                abi.int6(0, 0, 1, 1, 0, 0), abi.dbl6(0, 0, 1, 0, 0, 0), abi.WENO_V1, prec, n, n, n)
+        ctx.call("ht3d_weno5_advect", *args)
+        ctx.synchronize()
+        e0.record(stream)
+        for _ in range(a.iters):
+            ctx.call("ht3d_weno5_advect", *args)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1e3 / a.iters
+        s = 8 if prec == abi.FP64 else 4
+        alg = hrl.bytes_per_advection(n, n, n, s)
+        print(json.dumps({"kernel": a.kernel, "n": n, "us_per_advection": t * 1e6, "alg_GBs": alg / t / 1e9}))
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()

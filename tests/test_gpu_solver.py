@@ -55,10 +55,14 @@ def test_fused_dyrel_fixed_iterations_fp64(ctx, orc, n, bc, cX):
     assert so == 0 and std.status == 0 and std.iters == sto.iters == 23 and std.checks == sto.checks
     m = no_edges_mask(X.shape)
     assert rel_err(ht.to_numpy(Xd), Xo, m) <= 1e-12
-    assert rel_err(ht.to_numpy(Fd), Fo) <= 1e-11
-    assert rel_err(ht.to_numpy(F0d), F0o) <= 1e-11
+    # F and F0 may converge to round-off on tiny grids: compare against the
+    # larger of their final size and 1e-6 of the initial residual scale
+    fscale = max(np.abs(Fo).max(), np.abs(F0o).max(), 1e-6 * np.abs(R).max() * min(dx, dy, dz) ** 2)
+    assert np.max(np.abs(ht.to_numpy(Fd) - Fo)) <= 1e-11 * fscale
+    assert np.max(np.abs(ht.to_numpy(F0d) - F0o)) <= 1e-11 * fscale
     assert abs(std.lambda_max - sto.lambda_max) <= 1e-14 * sto.lambda_max
-    assert abs(std.h1 - sto.h1) <= 1e-10 and abs(std.nF_abs - sto.nF_abs) <= 1e-10 * sto.nF_abs
+    assert abs(std.h1 - sto.h1) <= 1e-10
+    assert abs(std.nF_abs - sto.nF_abs) <= 1e-10 * max(sto.nF_abs, 1e-6 * sto.nF_ini)
 
 
 @pytest.mark.parametrize("n,bc,cX", [((31, 31, 31), "thermal", 200.0), ((24, 20, 28), "neumann", 0.0)])
@@ -136,8 +140,11 @@ def test_step_hrl_fp64_matches_oracle(ctx, orc, n):
         assert rel_err(ht.to_numpy(Td), T, m) <= 1e-12
         Pn, Pg = P[1:-1, 1:-1, 1:-1], ht.to_numpy(Pd)[1:-1, 1:-1, 1:-1]
         assert rel_err(Pg - Pg.mean(), Pn - Pn.mean()) <= 1e-10
+        # V = -k (grad P - Ra T e_y) is a small difference of O(Ra) terms while
+        # the flow is near hydrostatic: measure it against the term scale
+        vscale = p_o.Ra * np.abs(T).max()
         for a, b in zip(Vd, V):
-            assert rel_err(ht.to_numpy(a), b) <= 1e-9
+            assert np.max(np.abs(ht.to_numpy(a) - b)) <= 1e-12 * vscale
         assert abs(p_d.dt - p_o.dt) <= 1e-9 * p_o.dt
 
 
