@@ -7,6 +7,8 @@ FP64, MIXED = 0, 1
 BC_NEUMANN, BC_DIRICHLET, BC_PERIODIC = 0, 1, 2
 WENO_V1, WENO_V2_REF, WENO_V2_FIXED = 0, 1, 2
 RED_SUM, RED_SUM_ABS, RED_MAX, RED_MIN, RED_MAX_ABS = 0, 1, 2, 3, 4
+TUNE_DYREL_VARIANT = 1
+DYREL_ZMARCH, DYREL_CELL = 1, 2
 
 
 class DyrelParams(ctypes.Structure):

@@ -147,6 +147,16 @@ int ht3d_ctx_set_sync(ht3d_ctx* ctx, int sync_each_call) {
     return HT3D_OK;
 }
 
+int ht3d_ctx_set_tuning(ht3d_ctx* ctx, int key, int value) {
+    if (!ctx) return HT3D_ERR_ARG;
+    if (key == HT3D_TUNE_DYREL_VARIANT) {
+        if (value != HT3D_DYREL_ZMARCH && value != HT3D_DYREL_CELL) return HT3D_ERR_ARG;
+        ctx->dyrel_variant = value;
+        return HT3D_OK;
+    }
+    return HT3D_ERR_ARG;
+}
+
 int ht3d_ctx_synchronize(ht3d_ctx* ctx) {
     return ht3d_guard(ctx, [&]() {
         HT3D_CUDA(cudaStreamSynchronize(ctx->stream));

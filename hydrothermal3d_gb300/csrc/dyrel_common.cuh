@@ -12,9 +12,10 @@
 // separate launches do.  The output buffer's face ghosts receive BC(X_in),
 // which is the state the reference leaves after the same iteration.
 //
-// Thread layout: a 32x8 tile of (x,y) columns per block, marching in z over a
-// chunk of planes.  The z-face flux is carried in a register (each z face is
-// evaluated once); x/y neighbours come through L1.
+// Two thread layouts with identical arithmetic (selected per context):
+//  * k_dyrel_iter: a 32x8 tile of (x,y) columns per block marching in z over a
+//    chunk of planes, the z-face flux carried in a register;
+//  * k_dyrel_cell: one thread per cell, neighbours through L1/L2.
 #pragma once
 #include <type_traits>
 #include "ht3d_internal.cuh"
@@ -51,7 +52,6 @@ __global__ void __launch_bounds__(TX* TY) k_dyrel_iter(const T* __restrict__ Xin
     const int j = blockIdx.y * TY + threadIdx.y;
     const int k0 = blockIdx.z * zchunk;
     const int k1 = min(nz, k0 + zchunk);
-    double acc[3] = {0.0, 0.0, 0.0};
     const T h1 = (T)s.h1, h2 = (T)s.h2, dtau = (T)s.dtau, cX = (T)s.cX, _dx = (T)s._dx, _dy = (T)s._dy, _dz = (T)s._dz;
     if (i < nx && j < ny && k0 < k1) {
         const int n1 = nx + 2, n2 = ny + 2;
@@ -90,12 +90,12 @@ __global__ void __launch_bounds__(TX* TY) k_dyrel_iter(const T* __restrict__ Xin
             const T f0 = h1 * F0[c] + h2 * f;
             F0[c] = f0;
             ocol[e] = xc - dtau * f0;
-            if (MODE == MODE_CHECK) {
+            if (MODE == MODE_CHECK) {  // per-cell terms of the check sums (canonical tree order)
                 const T fit = F[c];
-                const double d = (double)dtau * (double)f0;
-                acc[0] += fabs((double)fu);
-                acc[1] += -d * ((double)f - (double)fit);
-                acc[2] += d * d;
+                const T d = dtau * f0;
+                partials[c] = fabs((double)(f * PCx[c]));
+                partials[c + cpl * nz] = (double)(-d * (f - fit));
+                partials[c + 2 * cpl * nz] = (double)(d * d);
             }
             if (MODE >= MODE_STOREF) F[c] = f;
             // face ghosts of the output = BC of the input (reference state)
@@ -110,14 +110,66 @@ __global__ void __launch_bounds__(TX* TY) k_dyrel_iter(const T* __restrict__ Xin
             qB = qF;
         }
     }
-    if (MODE == MODE_CHECK) {
-        block_reduce<RED_SUM, 3>(acc);
-        if (threadIdx.x == 0 && threadIdx.y == 0) {
-            const long long b = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
-            partials[3 * b + 0] = acc[0];
-            partials[3 * b + 1] = acc[1];
-            partials[3 * b + 2] = acc[2];
+}
+
+// One thread per cell: the same arithmetic as k_dyrel_iter, with every load
+// of a cell independent of the others (maximal memory-level parallelism, no
+// per-thread z loop).  Block 32x4x2.
+constexpr int CX_ = 32, CY_ = 4, CZ_ = 2;
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(CX_* CY_* CZ_) k_dyrel_cell(const T* __restrict__ Xin, T* __restrict__ Xout,
+                                                             const T* __restrict__ R, const T* __restrict__ kx,
+                                                             const T* __restrict__ ky, const T* __restrict__ kz,
+                                                             const T* __restrict__ PCx, T* __restrict__ F0,
+                                                             T* __restrict__ F, DyrelScal s, BC6<T> bc, int nx, int ny,
+                                                             int nz, double* __restrict__ partials) {
+    const int i = blockIdx.x * CX_ + threadIdx.x;
+    const int j = blockIdx.y * CY_ + threadIdx.y;
+    const int k = blockIdx.z * CZ_ + threadIdx.z;
+    const T h1 = (T)s.h1, h2 = (T)s.h2, dtau = (T)s.dtau, cX = (T)s.cX, _dx = (T)s._dx, _dy = (T)s._dy, _dz = (T)s._dz;
+    if (i < nx && j < ny && k < nz) {
+        const int n1 = nx + 2, n2 = ny + 2;
+        const int pl = n1 * n2;
+        const int e = (i + 1) + n1 * ((j + 1) + n2 * (k + 1));
+        const int c = i + nx * (j + ny * k);
+        const int fx = i + (nx + 1) * (j + ny * k);
+        const int fy = i + nx * (j + (ny + 1) * k);
+        const T xc = Xin[e];
+        const T xw = (i == 0) ? ghost(bc, 0, xc) : Xin[e - 1];
+        const T xe = (i == nx - 1) ? ghost(bc, 1, xc) : Xin[e + 1];
+        const T xs = (j == 0) ? ghost(bc, 2, xc) : Xin[e - n1];
+        const T xn = (j == ny - 1) ? ghost(bc, 3, xc) : Xin[e + n1];
+        const T xb = (k == 0) ? ghost(bc, 4, xc) : Xin[e - pl];
+        const T xf = (k == nz - 1) ? ghost(bc, 5, xc) : Xin[e + pl];
+        const T qW = -kx[fx] * (_dx * (xc - xw));
+        const T qE = -kx[fx + 1] * (_dx * (xe - xc));
+        const T qS = -ky[fy] * (_dy * (xc - xs));
+        const T qN = -ky[fy + nx] * (_dy * (xn - xc));
+        const T qB = -kz[c] * (_dz * (xc - xb));
+        const T qF = -kz[c + nx * ny] * (_dz * (xf - xc));
+        const T fu = R[c] + cX * xc + _dx * (qE - qW) + _dy * (qN - qS) + _dz * (qF - qB);
+        T f;
+        if constexpr (std::is_same<T, double>::value) f = fu / PCx[c];
+        else f = fu * PCx[c];
+        const T f0 = h1 * F0[c] + h2 * f;
+        F0[c] = f0;
+        Xout[e] = xc - dtau * f0;
+        if (MODE == MODE_CHECK) {  // per-cell terms of the check sums (canonical tree order)
+            const T fit = F[c];
+            const T d = dtau * f0;
+            const int n = nx * ny * nz;
+            partials[c] = fabs((double)(f * PCx[c]));
+            partials[c + n] = (double)(-d * (f - fit));
+            partials[c + 2 * n] = (double)(d * d);
         }
+        if (MODE >= MODE_STOREF) F[c] = f;
+        if (i == 0) Xout[e - 1] = xw;
+        if (i == nx - 1) Xout[e + 1] = xe;
+        if (j == 0) Xout[e - n1] = xs;
+        if (j == ny - 1) Xout[e + n1] = xn;
+        if (k == 0) Xout[e - pl] = xb;
+        if (k == nz - 1) Xout[e + pl] = xf;
     }
 }
 
@@ -161,14 +213,43 @@ __global__ void k_copy_ex_faces(T* __restrict__ dst, const T* __restrict__ src, 
     if (nb <= 1) dst[ix3(i, j, k, n1, n2)] = src[ix3(i, j, k, n1, n2)];
 }
 
+
+// One level of the canonical tree sum: block g (1024 threads) reduces
+// elements [1024 g, 1024 g + 1024) of NV arrays (SPLIT: NV separate arrays
+// `split` apart; otherwise NV-interleaved) with the warp-shuffle tree of
+// block_reduce, padding with zeros.  The oracle's tree_sum emulates this
+// order exactly.
+template <int NV, bool SPLIT>
+__global__ void __launch_bounds__(1024) k_tree_pass(const double* __restrict__ in, long long n, long long split,
+                                                    double* __restrict__ out) {
+    double v[NV];
+    const long long t = (long long)blockIdx.x * 1024 + threadIdx.x;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) v[q] = t < n ? (SPLIT ? in[q * split + t] : in[t * NV + q]) : 0.0;
+    block_reduce<RED_SUM, NV>(v);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) out[(long long)blockIdx.x * NV + q] = v[q];
+}
+
 struct IterLaunch {
+    int variant;  // HT3D_DYREL_ZMARCH or HT3D_DYREL_CELL
     dim3 grid, block;
     int zchunk;
     long long nblocks;
 };
 
-inline IterLaunch iter_launch(ht3d_ctx* ctx, int nx, int ny, int nz) {
+inline IterLaunch iter_launch(ht3d_ctx* ctx, int nx, int ny, int nz, int force_variant = 0) {
     IterLaunch L;
+    const int v = force_variant ? force_variant : ctx->dyrel_variant;
+    L.variant = v == HT3D_DYREL_ZMARCH ? HT3D_DYREL_ZMARCH : HT3D_DYREL_CELL;
+    if (L.variant == HT3D_DYREL_CELL) {
+        L.block = dim3(CX_, CY_, CZ_);
+        L.grid = dim3((nx + CX_ - 1) / CX_, (ny + CY_ - 1) / CY_, (nz + CZ_ - 1) / CZ_);
+        L.zchunk = 1;
+        L.nblocks = (long long)L.grid.x * L.grid.y * L.grid.z;
+        return L;
+    }
     L.block = dim3(TX, TY, 1);
     const int gx = (nx + TX - 1) / TX, gy = (ny + TY - 1) / TY;
     const long long tiles = (long long)gx * gy;
@@ -179,6 +260,18 @@ inline IterLaunch iter_launch(ht3d_ctx* ctx, int nx, int ny, int nz) {
     L.grid = dim3(gx, gy, zc);
     L.nblocks = tiles * zc;
     return L;
+}
+
+template <typename T, int MODE>
+inline void launch_iter(ht3d_ctx* ctx, const IterLaunch& L, const T* Xin, T* Xout, const T* R, const T* kx,
+                        const T* ky, const T* kz, const T* PCx, T* F0, T* F, const DyrelScal& sc, const BC6<T>& bc,
+                        int nx, int ny, int nz, double* partials) {
+    if (L.variant == HT3D_DYREL_CELL)
+        HT3D_LAUNCH(ctx, (k_dyrel_cell<T, MODE>), L.grid, L.block, 0, Xin, Xout, R, kx, ky, kz, PCx, F0, F, sc, bc, nx,
+                    ny, nz, partials);
+    else
+        HT3D_LAUNCH(ctx, (k_dyrel_iter<T, MODE>), L.grid, L.block, 0, Xin, Xout, R, kx, ky, kz, PCx, F0, F, sc, bc, nx,
+                    ny, nz, L.zchunk, partials);
 }
 
 }  // namespace
@@ -225,8 +318,8 @@ static int dyrel_iterate_impl(ht3d_ctx* ctx, T* X, const T* R, const T* kx, cons
     T* cur = X;
     T* nxt = X2;
     for (int it = 0; it < n_iter; ++it) {
-        HT3D_LAUNCH(ctx, (k_dyrel_iter<T, MODE_PLAIN>), L.grid, L.block, 0, cur, nxt, R, kx, ky, kz, PCx, F0,
-                    (T*)nullptr, sc, bc, nx, ny, nz, L.zchunk, (double*)nullptr);
+        launch_iter<T, MODE_PLAIN>(ctx, L, cur, nxt, R, kx, ky, kz, PCx, F0, (T*)nullptr, sc, bc, nx, ny, nz,
+                                   (double*)nullptr);
         std::swap(cur, nxt);
     }
     if (cur != X) {
@@ -236,3 +329,19 @@ static int dyrel_iterate_impl(ht3d_ctx* ctx, T* X, const T* R, const T* kx, cons
     return HT3D_OK;
 }
 
+
+// Canonical tree sums of three n-element arrays stored back to back at
+// `terms`; results land in the pinned host buffer (h_result[0..2]).
+inline void tree_sum3(ht3d_ctx* ctx, const double* terms, long long n, double* work) {
+    long long m = (n + 1023) / 1024;
+    double* a = work;
+    double* b = work + 3 * m;
+    HT3D_LAUNCH(ctx, (k_tree_pass<3, true>), (unsigned)m, 1024, 0, terms, n, n, a);
+    while (m > 1) {
+        const long long m2 = (m + 1023) / 1024;
+        HT3D_LAUNCH(ctx, (k_tree_pass<3, false>), (unsigned)m2, 1024, 0, a, m, 0LL, b);
+        std::swap(a, b);
+        m = m2;
+    }
+    ht3d_fetch_results(ctx, a, 3);
+}

@@ -13,8 +13,10 @@ int ht3d_dyrel_solve_fp64(ht3d_ctx* ctx, double* X, const double* R, const doubl
     double* PC = (double*)ht3d_scratch(ctx, SLOT_PC, sizeof(double) * n);
     double* X2 = (double*)ht3d_scratch(ctx, SLOT_X2, sizeof(double) * nex);
     IterLaunch L = iter_launch(ctx, nx, ny, nz);
-    const long long nparts = std::max<long long>(L.nblocks, (long long)((nx + 31) / 32) * ((ny + 7) / 8) * nz);
-    double* parts = (double*)ht3d_scratch(ctx, SLOT_PARTIALS, sizeof(double) * 3 * nparts);
+    const long long nsetup = (long long)((nx + 31) / 32) * ((ny + 7) / 8) * nz;
+    // per-cell check terms (3n) followed by tree-pass work space
+    const long long nwork = 3 * n + 6 * ((n + 1023) / 1024 + 1);
+    double* parts = (double*)ht3d_scratch(ctx, SLOT_PARTIALS, sizeof(double) * std::max(nwork, nsetup));
     double* dres = (double*)ht3d_scratch(ctx, SLOT_RESULT, sizeof(double) * 64);
 
     BC6<double> bc;
@@ -54,20 +56,16 @@ int ht3d_dyrel_solve_fp64(ht3d_ctx* ctx, double* X, const double* R, const doubl
         sc.h2 = S.h2;
         sc.dtau = S.dtau;
         if (chk)
-            HT3D_LAUNCH(ctx, (k_dyrel_iter<double, MODE_CHECK>), L.grid, L.block, 0, cur, nxt, R, kx, ky, kz, PC, F0,
-                        F, sc, bc, nx, ny, nz, L.zchunk, parts);
+            launch_iter<double, MODE_CHECK>(ctx, L, cur, nxt, R, kx, ky, kz, PC, F0, F, sc, bc, nx, ny, nz, parts);
         else if (storef)
-            HT3D_LAUNCH(ctx, (k_dyrel_iter<double, MODE_STOREF>), L.grid, L.block, 0, cur, nxt, R, kx, ky, kz, PC,
-                        F0, F, sc, bc, nx, ny, nz, L.zchunk, parts);
+            launch_iter<double, MODE_STOREF>(ctx, L, cur, nxt, R, kx, ky, kz, PC, F0, F, sc, bc, nx, ny, nz, parts);
         else
-            HT3D_LAUNCH(ctx, (k_dyrel_iter<double, MODE_PLAIN>), L.grid, L.block, 0, cur, nxt, R, kx, ky, kz, PC,
-                        F0, F, sc, bc, nx, ny, nz, L.zchunk, parts);
+            launch_iter<double, MODE_PLAIN>(ctx, L, cur, nxt, R, kx, ky, kz, PC, F0, F, sc, bc, nx, ny, nz, parts);
         std::swap(cur, nxt);
         it_done = iter;
         if (chk) {
             ++checks;
-            HT3D_LAUNCH(ctx, (k_reduce_partials<RED_SUM, 3>), 1, 1024, 0, parts, (int)L.nblocks, dres);
-            ht3d_fetch_results(ctx, dres, 3);
+            tree_sum3(ctx, parts, n, parts + 3 * n);
             const double s_abs = ctx->h_result[0], s_num = ctx->h_result[1], s_den = ctx->h_result[2];
             nF_abs = s_abs / (double)n / sqrt((double)n) * prm->norm_scale;
             if (iter == 1) nF_ini = nF_abs;

@@ -146,7 +146,9 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
     float* ky32 = (float*)ht3d_scratch(ctx, SLOT_F32_KY, sizeof(float) * nfy);
     float* kz32 = (float*)ht3d_scratch(ctx, SLOT_F32_KZ, sizeof(float) * nfz);
     IterLaunch L = iter_launch(ctx, nx, ny, nz);
-    const long long nparts = std::max<long long>(L.nblocks, (long long)((nx + 31) / 32) * ((ny + 7) / 8) * nz);
+    IterLaunch LC = iter_launch(ctx, nx, ny, nz, HT3D_DYREL_ZMARCH);  // layout of the FP64 check kernel
+    const long long nparts = std::max<long long>(std::max(L.nblocks, LC.nblocks),
+                                                 (long long)((nx + 31) / 32) * ((ny + 7) / 8) * nz);
     double* parts = (double*)ht3d_scratch(ctx, SLOT_PARTIALS, sizeof(double) * 3 * nparts);
     double* dres = (double*)ht3d_scratch(ctx, SLOT_RESULT, sizeof(double) * 64);
 
@@ -197,22 +199,20 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
         sc.h2 = S.h2;
         sc.dtau = S.dtau;
         if (chk) {
-            HT3D_LAUNCH(ctx, k_mixed_check, L.grid, L.block, 0, xcur, xnxt, dcur, dnxt, R, kx, ky, kz, invPC, F0s, Fs,
-                        F, Rin, sc, bc, nx, ny, nz, L.zchunk, parts);
+            HT3D_LAUNCH(ctx, k_mixed_check, LC.grid, LC.block, 0, xcur, xnxt, dcur, dnxt, R, kx, ky, kz, invPC, F0s, Fs,
+                        F, Rin, sc, bc, nx, ny, nz, LC.zchunk, parts);
             std::swap(xcur, xnxt);
         } else if (storef) {
-            HT3D_LAUNCH(ctx, (k_dyrel_iter<float, MODE_STOREF>), L.grid, L.block, 0, dcur, dnxt, Rin, kx32, ky32, kz32,
-                        iPC, F0s, Fs, sc, bch, nx, ny, nz, L.zchunk, parts);
+            launch_iter<float, MODE_STOREF>(ctx, L, dcur, dnxt, Rin, kx32, ky32, kz32, iPC, F0s, Fs, sc, bch, nx, ny, nz, parts);
         } else {
-            HT3D_LAUNCH(ctx, (k_dyrel_iter<float, MODE_PLAIN>), L.grid, L.block, 0, dcur, dnxt, Rin, kx32, ky32, kz32,
-                        iPC, F0s, Fs, sc, bch, nx, ny, nz, L.zchunk, parts);
+            launch_iter<float, MODE_PLAIN>(ctx, L, dcur, dnxt, Rin, kx32, ky32, kz32, iPC, F0s, Fs, sc, bch, nx, ny, nz, parts);
         }
         std::swap(dcur, dnxt);
         it_done = iter;
         last_check = chk;
         if (chk) {
             ++checks;
-            HT3D_LAUNCH(ctx, (k_reduce_partials<RED_SUM, 3>), 1, 1024, 0, parts, (int)L.nblocks, dres);
+            HT3D_LAUNCH(ctx, (k_reduce_partials<RED_SUM, 3>), 1, 1024, 0, parts, (int)LC.nblocks, dres);
             ht3d_fetch_results(ctx, dres, 3);
             const double s_abs = ctx->h_result[0], s_num = ctx->h_result[1], s_den = ctx->h_result[2];
             nF_abs = s_abs / (double)n / sqrt((double)n) * prm->norm_scale;

@@ -33,6 +33,7 @@ struct ht3d_ctx {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int sync_each_call = 1;
+    int dyrel_variant = HT3D_DYREL_CELL;  // thread layout of the fused DYREL iteration
     int num_sms = 152;
     unsigned long long launches = 0;
     std::string last_error;

@@ -22,10 +22,12 @@ def main():
     ap.add_argument("--kernel", default="dyrel_f32", choices=["dyrel_f32", "dyrel_f64", "weno_f64", "weno_mixed"])
     ap.add_argument("--n", type=int, default=255)
     ap.add_argument("--iters", type=int, default=5)
+    ap.add_argument("--variant", type=int, default=2, help="DYREL thread layout: 1 z-march tiles, 2 one thread per cell")
     a = ap.parse_args()
     n = a.n
     stream = torch.cuda.Stream()
     ctx = ht.Context(device=0, stream=stream.cuda_stream)
+    ctx.check(ctx.lib.ht3d_ctx_set_tuning(ctx.ptr, abi.TUNE_DYREL_VARIANT, a.variant))
     d = 1.0 / n
     bt, bv = abi.int6(0, 0, 1, 1, 0, 0), abi.dbl6(0, 0, 1, 0, 0, 0)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -50,7 +52,7 @@ def main():
         t = e0.elapsed_time(e1) / 1e3 / a.iters
         s = 4 if a.kernel == "dyrel_f32" else 8
         alg = hrl.bytes_per_iteration(n, n, n, s)
-        print(json.dumps({"kernel": a.kernel, "n": n, "us_per_launch": t * 1e6, "alg_GBs": alg / t / 1e9}))
+        print(json.dumps({"kernel": a.kernel, "variant": a.variant, "n": n, "us_per_launch": t * 1e6, "alg_GBs": alg / t / 1e9}))
     else:
         prec = abi.FP64 if a.kernel == "weno_f64" else abi.MIXED
         T = ht.zeros(n + 2, n + 2, n + 2).uniform_(0, 1)

@@ -56,6 +56,11 @@ extern "C" {
 #define HT3D_WENO_V2_REF 1     /* tools/Weno5_Routines_v2.jl incl. its minus-branch v5 stencil */
 #define HT3D_WENO_V2_FIXED 2   /* v2 loop structure with the textbook v5 stencil */
 
+/* tuning keys for ht3d_ctx_set_tuning */
+#define HT3D_TUNE_DYREL_VARIANT 1   /* thread layout of the fused DYREL iteration: */
+#define HT3D_DYREL_ZMARCH 1         /*   32x8 column tiles marching in z            */
+#define HT3D_DYREL_CELL 2           /*   one thread per cell (default)              */
+
 typedef struct ht3d_ctx ht3d_ctx;
 
 /* DYREL controls (Dimensional/HydroThermal3D_v18.jl:433-439, 292-303) */
@@ -106,6 +111,8 @@ int ht3d_ctx_destroy(ht3d_ctx* ctx);
 int ht3d_ctx_set_stream(ht3d_ctx* ctx, void* stream);
 int ht3d_ctx_set_sync(ht3d_ctx* ctx, int sync_each_call);
 int ht3d_ctx_synchronize(ht3d_ctx* ctx);
+/* set a tuning knob (HT3D_TUNE_*); results never depend on it */
+int ht3d_ctx_set_tuning(ht3d_ctx* ctx, int key, int value);
 /* number of CUDA kernels this ctx has launched (monotonic) */
 unsigned long long ht3d_ctx_launch_count(const ht3d_ctx* ctx);
 const char* ht3d_ctx_last_error(const ht3d_ctx* ctx);

@@ -789,6 +789,51 @@ void orc_RayleighQuotientDenominator(double* G, const double* F0, double dtau, i
 }  // extern "C"
 
 // ===========================================================================
+// Canonical summation order of the DYREL norm and Rayleigh-quotient sums:
+// a 32-ary tree over the linear cell index.  Groups of 32 consecutive values
+// are combined by the butterfly-free "shift-down" tree (offsets 16,8,4,2,1:
+// v[l] = v[l] + v[l+off] for l < off), 32 group results by the same tree, and
+// the resulting per-1024 partials again, level by level, padding with zeros.
+// libht3d evaluates its FP64 solver sums in exactly this order (one 1024-
+// thread block per group of 1024, warp shuffles), so the plain FP64 solver is
+// reproducible bit for bit.
+// ===========================================================================
+static inline double warp_tree(double* v) {
+    for (int off = 16; off > 0; off >>= 1)
+        for (int l = 0; l < off; ++l) v[l] = v[l] + v[l + off];
+    return v[0];
+}
+static double tree_sum(const double* a, i64 n) {
+    if (n <= 0) return 0.0;
+    std::vector<double> cur(a, a + n);
+    do {
+        const i64 m = ((i64)cur.size() + 1023) / 1024;
+        std::vector<double> nxt(m);
+#pragma omp parallel for schedule(static)
+        for (i64 g = 0; g < m; ++g) {
+            double w[32];
+            for (int wi = 0; wi < 32; ++wi) {
+                double v[32];
+                for (int l = 0; l < 32; ++l) {
+                    const i64 idx = g * 1024 + wi * 32 + l;
+                    v[l] = idx < (i64)cur.size() ? cur[idx] : 0.0;
+                }
+                w[wi] = warp_tree(v);
+            }
+            nxt[g] = warp_tree(w);
+        }
+        cur.swap(nxt);
+    } while (cur.size() > 1);
+    return cur[0];
+}
+static double tree_sum_abs(const double* a, i64 n) {
+    std::vector<double> b(a, a + n);
+    for (auto& x : b) x = std::fabs(x);
+    return tree_sum(b.data(), n);
+}
+extern "C" double orc_tree_sum(const double* a, i64 n) { return tree_sum(a, n); }
+
+// ===========================================================================
 // Solver drivers.
 // ===========================================================================
 extern "C" {
@@ -852,16 +897,16 @@ int orc_dyrel_solve_dimless(double* X, const double* R, const double* kx, const 
         if (check) {
             ++checks;
             orc_Multiply(dumc.data(), F, PC.data(), n);
-            nF_abs = orc_sum_abs(dumc.data(), n) / (double)n / std::sqrt((double)n) * prm->norm_scale;
+            nF_abs = tree_sum_abs(dumc.data(), n) / (double)n / std::sqrt((double)n) * prm->norm_scale;
             if (iter == 1) nF_ini = nF_abs;
             nF_rel = nF_abs / nF_ini;
             if (std::isnan(nF_abs)) { status = ORC_ERR_NAN; break; }
             if (nF_rel > 100) { status = ORC_ERR_DIVERGED; break; }
             if (iter > 1) {
                 orc_RayleighQuotientNumerator(dumc.data(), F0, Fit.data(), F, dtau, n);
-                lmin = std::fabs(orc_sum(dumc.data(), n));
+                lmin = std::fabs(tree_sum(dumc.data(), n));
                 orc_RayleighQuotientDenominator(dumc.data(), F0, dtau, n);
-                lmin /= std::fabs(orc_sum(dumc.data(), n));
+                lmin /= std::fabs(tree_sum(dumc.data(), n));
                 c = 2.0 * std::sqrt(lmin) * prm->cfact;
                 h1 = (2 - c * dtau) / (2 + c * dtau);
                 h2 = 2 * dtau / (2 + c * dtau);
@@ -934,6 +979,176 @@ int orc_step_hrl(double* Tc_ex, double* Pc_ex, const double* ktv, const double* 
         const double vmax = std::max(std::max(orc_max_abs(Vx, (nx + 1) * ny * nz), orc_max_abs(Vy, nx * (ny + 1) * nz)),
                                      orc_max_abs(Vz, nx * ny * (nz + 1)));
         p->dt = p->dt_fact * 1.0 / 6.1 * std::min(std::min(p->dx, p->dy), p->dz) / vmax;
+    }
+    return ORC_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Dimensional model (Dimensional/HydroThermal3D_v18.jl) -- one time step of
+// the driver loop :404-572 with the kernels of
+// Dimensional/kernels_HT3D_dimensional.jl and AdvectWithWeno5_v2.
+// ===========================================================================
+struct orc_v18_params;
+extern "C" {
+struct orc_v18_params {
+    double dx, dy, dz, ymin;
+    double dt, time;
+    double phi_i, k_fact, delta, g, Qt, qyS;
+    double Ttop, Tbot, Ptop, Pbot, T_pluton;
+    double C_adv;
+    double sc_T, sc_L, sc_t, sc_eta, sc_sigma, sc_rho, sc_C, sc_kt;
+    int it, thermal, hydro, advection, dt_constant, weno_variant;
+    orc_dyrel_params thermal_dyrel, darcy_dyrel;
+    int n_adv;  // out: advection sub-steps taken
+    int pad_;
+};
+}  // extern "C"
+
+// shared DYREL loop for the two dimensional solves; `iteration` performs the
+// kernels of one pseudo-iteration (v18:451-455 / :510-514) given h1,h2,dtau.
+template <typename IterFn>
+static int dyrel_loop(double* X, double* F, double* F0, const double* PC, double lmax, const orc_dyrel_params* prm,
+                      IterFn&& iteration, orc_dyrel_stats* st, i64 nx, i64 ny, i64 nz) {
+    const i64 n = nx * ny * nz;
+    std::vector<double> Xit(n), Fit(n), dumc(n);
+    double lmin = lmax / prm->lmin_ratio;
+    const double dtau = 2.0 / std::sqrt(lmax) * prm->cfl;
+    double c = 2.0 * std::sqrt(lmin) * prm->cfact;
+    double h1 = (2 - c * dtau) / (2 + c * dtau), h2 = 2 * dtau / (2 + c * dtau);
+    orc_ResetA(F, F0, n);
+    double nF_abs = 0., nF_rel = 0., nF_ini = 0.;
+    int it_done = 0, converged = 0, status = ORC_OK, checks = 0;
+    for (int iter = 1; iter <= prm->nitmax; ++iter) {
+        const bool check = (iter % prm->nitout == 0) || iter <= 2;
+        if (check) orc_SwapDYREL(Xit.data(), Fit.data(), X, F, nx, ny, nz);
+        iteration(h1, h2, dtau);
+        it_done = iter;
+        if (check) {
+            ++checks;
+            orc_Multiply(dumc.data(), F, PC, n);
+            nF_abs = tree_sum_abs(dumc.data(), n) / (double)n / std::sqrt((double)n) * prm->norm_scale;
+            if (iter == 1) nF_ini = nF_abs;
+            nF_rel = nF_abs / nF_ini;
+            if (std::isnan(nF_abs)) { status = ORC_ERR_NAN; break; }
+            if (nF_rel > 100) { status = ORC_ERR_DIVERGED; break; }
+            if (iter > 1) {
+                orc_RayleighQuotientNumerator(dumc.data(), F0, Fit.data(), F, dtau, n);
+                lmin = std::fabs(tree_sum(dumc.data(), n));
+                orc_RayleighQuotientDenominator(dumc.data(), F0, dtau, n);
+                lmin /= std::fabs(tree_sum(dumc.data(), n));
+                c = 2.0 * std::sqrt(lmin) * prm->cfact;
+                h1 = (2 - c * dtau) / (2 + c * dtau);
+                h2 = 2 * dtau / (2 + c * dtau);
+            }
+            if (nF_abs < prm->tol_abs || nF_rel < prm->tol_rel) { converged = 1; break; }
+        }
+    }
+    if (st) {
+        st->iters = it_done; st->converged = converged; st->status = status; st->checks = checks;
+        st->nF_abs = nF_abs; st->nF_rel = nF_rel; st->nF_ini = nF_ini; st->lambda_min = lmin; st->lambda_max = lmax;
+        st->h1 = h1; st->h2 = h2; st->dtau = dtau;
+    }
+    return status;
+}
+
+extern "C" {
+int orc_step_v18(double* T, double* P, const double* phc, const double* phv, const double* wN, const double* kmul,
+                 double* Vx, double* Vy, double* Vz, orc_v18_params* p, orc_dyrel_stats* st_T, orc_dyrel_stats* st_P,
+                 i64 nx, i64 ny, i64 nz) {
+    const i64 n = nx * ny * nz, nv = (nx + 1) * (ny + 1) * (nz + 1), nex = (nx + 2) * (ny + 2) * (nz + 2);
+    const i64 nfx = (nx + 1) * ny * nz, nfy = nx * (ny + 1) * nz, nfz = nx * ny * (nz + 1);
+    const double dx = p->dx, dy = p->dy, dz = p->dz, _dx = 1.0 / dx, _dy = 1.0 / dy, _dz = 1.0 / dz;
+    double dt = p->dt;
+    const double _dt = 1.0 / dt;
+    const double transient = p->it == 0 ? 0.0 : 1.0;
+    std::vector<double> Tc0(n), Pc0(n), kv(nv, 1.0), dumc(n, 1.0), kx(nfx), ky(nfy), kz(nfz), rC(n, 0.0), PC(n, 1.0),
+        Xc0(n), F(n), F0(n), qx(nfx), qy(nfy), qz(nfz);
+    if (p->it == 1)  // introduce the pluton (v18:414-416)
+        for (i64 t = 0; t < nex; ++t)
+            if (phc[t] == 3.0) T[t] = p->T_pluton;
+    orc_InitThermal_dim(Tc0.data(), T, nx, ny, nz);
+    orc_InitThermal_dim(Pc0.data(), P, nx, ny, nz);
+    int s = ORC_OK;
+    if (p->thermal) {  // v18:424-479
+        orc_ComputeThermalConductivity(kv.data(), T, phv, p->phi_i, p->sc_kt, p->sc_T, nx, ny, nz);
+        orc_SmoothConductivityV2C(dumc.data(), kv.data(), nx, ny, nz);
+        orc_SmoothConductivityC2V(kv.data(), dumc.data(), nx, ny, nz);
+        orc_InitConductivity(kx.data(), ky.data(), kz.data(), kv.data(), nx, ny, nz);
+        orc_ComputeRhoCeffective(rC.data(), T, P, phc, p->phi_i, p->sc_T, p->sc_sigma, p->sc_C, p->sc_rho, nx, ny, nz);
+        orc_GershgorinPoisson(Xc0.data(), PC.data(), rC.data(), kx.data(), ky.data(), kz.data(), transient, dt, dx, dy,
+                              dz, nx, ny, nz);
+        const double lmax = orc_max(Xc0.data(), n);
+        s = dyrel_loop(T, F.data(), F0.data(), PC.data(), lmax, &p->thermal_dyrel,
+                       [&](double h1, double h2, double dtau) {
+                           orc_SetTemperatureBCs_dim(T, ky.data(), wN, phc, p->qyS, _dy, p->Ttop, nx, ny, nz);
+                           orc_ComputeFlux(qx.data(), qy.data(), qz.data(), kx.data(), ky.data(), kz.data(), T, _dx,
+                                           _dy, _dz, nx, ny, nz);
+                           orc_ResidualTemperatureLinearised(F.data(), T, Tc0.data(), rC.data(), phc, PC.data(),
+                                                             qx.data(), qy.data(), qz.data(), p->Qt, transient, _dt,
+                                                             _dx, _dy, _dz, nx, ny, nz);
+                           orc_DYRELUpdate(F0.data(), T, F.data(), h1, h2, dtau, nx, ny, nz);
+                       },
+                       st_T, nx, ny, nz);
+        if (s) return s;
+    }
+    if (p->hydro) {  // v18:481-538
+        orc_ComputeHydroConductivity(kv.data(), T, P, phv, p->ymin, dy, p->k_fact, p->delta, p->sc_sigma, p->sc_T,
+                                     p->sc_L, p->sc_t, p->sc_eta, 1, kmul, nx, ny, nz);
+        orc_SmoothConductivityV2C(dumc.data(), kv.data(), nx, ny, nz);
+        orc_SmoothConductivityC2V(kv.data(), dumc.data(), nx, ny, nz);
+        orc_InitConductivity(kx.data(), ky.data(), kz.data(), kv.data(), nx, ny, nz);
+        orc_phi_rhof(rC.data(), T, P, phc, p->phi_i, p->sc_rho, p->sc_T, p->sc_sigma, 0, 1, nx, ny, nz);
+        orc_GershgorinPoisson(Xc0.data(), PC.data(), rC.data(), kx.data(), ky.data(), kz.data(), transient, dt, dx, dy,
+                              dz, nx, ny, nz);
+        const double lmax = orc_max(Xc0.data(), n);
+        orc_phi_rhof(Xc0.data(), Tc0.data(), Pc0.data(), phc, p->phi_i, p->sc_rho, p->sc_T, p->sc_sigma, 1, 0, nx, ny, nz);
+        orc_ComputeFluidDensity(kv.data(), T, P, phv, p->sc_sigma, p->sc_T, p->sc_rho, nx, ny, nz);
+        s = dyrel_loop(P, F.data(), F0.data(), PC.data(), lmax, &p->darcy_dyrel,
+                       [&](double h1, double h2, double dtau) {
+                           orc_phi_rhof(rC.data(), T, P, phc, p->phi_i, p->sc_rho, p->sc_T, p->sc_sigma, 0, 0, nx, ny, nz);
+                           orc_SetPressureBCs_dim(P, wN, phc, p->Ptop, nx, ny, nz);
+                           orc_ComputeDarcyFlux(qx.data(), qy.data(), qz.data(), kv.data(), kx.data(), ky.data(),
+                                                kz.data(), P, p->g, _dx, _dy, _dz, nx, ny, nz);
+                           orc_ResidualFluidPressure(F.data(), phc, rC.data(), Xc0.data(), PC.data(), qx.data(),
+                                                     qy.data(), qz.data(), transient, _dt, _dx, _dy, _dz, nx, ny, nz);
+                           orc_DYRELUpdate(F0.data(), P, F.data(), h1, h2, dtau, nx, ny, nz);
+                       },
+                       st_P, nx, ny, nz);
+        if (s) return s;
+    }
+    // velocity (v18:543-548): k/mu, smoothed, and the Darcy flux
+    orc_ComputeHydroConductivity(kv.data(), T, P, phv, p->ymin, dy, p->k_fact, p->delta, p->sc_sigma, p->sc_T, p->sc_L,
+                                 p->sc_t, p->sc_eta, 2, kmul, nx, ny, nz);
+    orc_SmoothConductivityV2C(dumc.data(), kv.data(), nx, ny, nz);
+    orc_SmoothConductivityC2V(kv.data(), dumc.data(), nx, ny, nz);
+    orc_InitConductivity(kx.data(), ky.data(), kz.data(), kv.data(), nx, ny, nz);
+    orc_ComputeFluidDensity(kv.data(), T, P, phv, p->sc_sigma, p->sc_T, p->sc_rho, nx, ny, nz);
+    orc_ComputeDarcyFlux(Vx, Vy, Vz, kv.data(), kx.data(), ky.data(), kz.data(), P, p->g, _dx, _dy, _dz, nx, ny, nz);
+    p->n_adv = 0;
+    if (p->it > 0) {  // v18:550-572
+        p->time += dt;
+        if (p->advection) {
+            const double vmax = std::max(std::max(orc_max_abs(Vx, nfx), orc_max_abs(Vy, nfy)), orc_max_abs(Vz, nfz));
+            const double dt_adv = p->C_adv * 1.0 / 6.1 * std::min(std::min(dx, dy), dz) / vmax;
+            const int bt[6] = {0, 0, 1, 1, 0, 0};
+            const double bv[6] = {0.0, 0.0, p->Tbot, p->Ttop, 0.0, 0.0};
+            const int quirk = p->weno_variant == 1;
+            if (!p->dt_constant) {
+                p->dt = dt_adv;
+                orc_AdvectWithWeno5_v2(T, Vx, Vy, Vz, p->dt, _dx, _dy, _dz, bt, bv, quirk, nx, ny, nz);
+                p->n_adv = 1;
+            } else {
+                const double na = std::ceil(dt / dt_adv);
+                if (!(na >= 1.0 && na <= 32767.0)) return 1;  // Int16(ceil(dt/dt_adv)) would throw
+                const int nt_adv = (int)na;
+                const double dt_adv1 = dt / nt_adv;
+                for (int ia = 0; ia < nt_adv; ++ia)
+                    orc_AdvectWithWeno5_v2(T, Vx, Vy, Vz, dt_adv1, _dx, _dy, _dz, bt, bv, quirk, nx, ny, nz);
+                p->n_adv = nt_adv;
+            }
+        }
     }
     return ORC_OK;
 }

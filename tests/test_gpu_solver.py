@@ -65,6 +65,31 @@ def test_fused_dyrel_fixed_iterations_fp64(ctx, orc, n, bc, cX):
     assert abs(std.nF_abs - sto.nF_abs) <= 1e-10 * max(sto.nF_abs, 1e-6 * sto.nF_ini)
 
 
+@pytest.mark.parametrize("variant", [1, 2])
+@pytest.mark.parametrize("n", [(5, 4, 3), (40, 37, 33), (70, 20, 9)])
+def test_fp64_solver_is_bitwise_reproducible(ctx, orc, n, variant):
+    """The plain FP64 form rounds like the reference (no FMA, F/PC) and sums
+    its checks in the oracle's canonical tree order: bit-identical results."""
+    nx, ny, nz = n
+    X, R, k = problem(n, seed=23)
+    types, vals = BCS["thermal"]
+    prm = abi.DyrelParams.reference(nitout=7)
+    d = (1.0 / nx, 1.0 / ny, 1.0 / nz)
+    Xo, Fo, F0o = X.copy(order="F"), orc.zeros(nx, ny, nz), orc.zeros(nx, ny, nz)
+    so, sto = orc.dyrel_solve_dimless(Xo, R, *k, 30.0, *d, types, vals, prm, Fo, F0o, n_iter_fixed=40)
+    ctx.check(ctx.lib.ht3d_ctx_set_tuning(ctx.ptr, 1, variant))
+    try:
+        Xd, Fd, F0d = ht.from_numpy(X), ht.zeros(nx, ny, nz), ht.zeros(nx, ny, nz)
+        std = api.dyrel_solve_dimless(ctx, Xd, ht.from_numpy(R), *[ht.from_numpy(a) for a in k], 30.0, *d, types,
+                                      vals, prm, Fd, F0d, abi.FP64, n_iter_fixed=40)
+    finally:
+        ctx.check(ctx.lib.ht3d_ctx_set_tuning(ctx.ptr, 1, 2))
+    assert std.nF_abs == sto.nF_abs and std.lambda_min == sto.lambda_min and std.h1 == sto.h1
+    m = no_edges_mask(X.shape)
+    np.testing.assert_array_equal(ht.to_numpy(Xd)[m], Xo[m])
+    np.testing.assert_array_equal(ht.to_numpy(F0d), F0o)
+
+
 @pytest.mark.parametrize("n,bc,cX", [((31, 31, 31), "thermal", 200.0), ((24, 20, 28), "neumann", 0.0)])
 def test_fused_dyrel_converged_solve(ctx, orc, n, bc, cX):
     """Full solve with the reference stop test: same iteration count, same solution."""
