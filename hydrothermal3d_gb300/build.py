@@ -19,8 +19,10 @@ LIB = os.path.join(HERE, "libht3d.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3", "--expt-relaxed-constexpr",
-          "-I", INCLUDE]
+# host code: no FP contraction either (aarch64 g++ would fuse a*b+c by default,
+# changing the DYREL parameters h1/h2 in the last bit)
+COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3", "-Xcompiler",
+          "-ffp-contract=off", "--expt-relaxed-constexpr", "-I", INCLUDE]
 # translation units that restate reference kernels statement by statement
 NO_FMA = {"kernels_dimless.cu", "kernels_dim.cu", "dyrel_fp64.cu", "step.cu", "weno.cu"}
 

@@ -100,6 +100,24 @@ typedef struct ht3d_hrl_params {
     ht3d_dyrel_params thermal, darcy;
 } ht3d_hrl_params;
 
+/* Dimensional time step (see ht3d_step_v18); values in the reference's scaled
+   units (Dimensional/HydroThermal3D_v18.jl:135-312). */
+typedef struct ht3d_v18_params {
+    double dx, dy, dz, ymin;
+    double dt;                 /* in: dt; out: dt_adv when dt_constant == 0 */
+    double time;               /* in/out: model time, advanced by dt when it > 0 */
+    double phi_i, k_fact, delta, g, Qt, qyS;
+    double Ttop, Tbot, Ptop, Pbot, T_pluton;
+    double C_adv;              /* advection multiplier (v18 "C"): dt_adv = C/6.1*min(dx,dy,dz)/max|V| */
+    double sc_T, sc_L, sc_t, sc_eta, sc_sigma, sc_rho, sc_C, sc_kt;   /* scaling (scale_me!) */
+    int it;                    /* time-step index: 0 = steady initialisation (transient = 0); 1 inserts the pluton */
+    int thermal, hydro, advection, dt_constant;
+    int weno_variant;          /* HT3D_WENO_V2_REF reproduces AdvectWithWeno5_v2 */
+    ht3d_dyrel_params thermal_dyrel, darcy_dyrel;   /* norm_scale: sc.rho*sc.C*sc.T/sc.t and sc.rho/sc.t */
+    int n_adv;                 /* out: advection sub-steps taken */
+    int pad_;
+} ht3d_v18_params;
+
 /* ------------------------------------------------------------------ */
 /* library / context                                                   */
 /* ------------------------------------------------------------------ */
@@ -120,6 +138,7 @@ const char* ht3d_ctx_last_error(const ht3d_ctx* ctx);
 int ht3d_sizeof_dyrel_params(void);
 int ht3d_sizeof_dyrel_stats(void);
 int ht3d_sizeof_hrl_params(void);
+int ht3d_sizeof_v18_params(void);
 
 /* ------------------------------------------------------------------ */
 /* Reductions (tools/Macros.jl:20-25: maximum_g, minimum_g, mean_g,    */
@@ -205,6 +224,76 @@ int ht3d_RayleighQuotientNumerator(ht3d_ctx* ctx, double* G, const double* Fc0, 
 int ht3d_RayleighQuotientDenominator(ht3d_ctx* ctx, double* G, const double* Fc0, double dtau, long long n);
 
 /* ------------------------------------------------------------------ */
+/* Dimensional kernels (Dimensional/kernels_HT3D_dimensional.jl) and   */
+/* material laws (Dimensional/HydroThermal3D_v18.jl:29-39).            */
+/* Boundary kernels use snapshot semantics: every rule reads the other */
+/* cells as they were before the call (the reference races there).     */
+/* ------------------------------------------------------------------ */
+/* ComputeThermalConductivity   :40-50 (ktv at vertices) */
+int ht3d_ComputeThermalConductivity(ht3d_ctx* ctx, double* ktv, const double* Tce, const double* phv, double phi0,
+                                    double scale_kt, double scale_T, int nx, int ny, int nz);
+/* ComputeHydroConductivity     :52-86 (mode 1 rho*k/mu, 2 k/mu, 3 k).  kmul_v (vertex
+   field, may be NULL) multiplies the permeability law kF(y) for heterogeneous
+   permeability; NULL is the reference kernel. */
+int ht3d_ComputeHydroConductivity(ht3d_ctx* ctx, double* kfv, const double* Tce, const double* Pce, const double* phv,
+                                  double ymin, double dy, double k_fact, double delta, double scale_sigma,
+                                  double scale_T, double scale_L, double scale_t, double scale_eta, int mode,
+                                  const double* kmul_v, int nx, int ny, int nz);
+/* ComputeFluidDensity          :88-104 */
+int ht3d_ComputeFluidDensity(ht3d_ctx* ctx, double* rhofv, const double* Tce, const double* Pce, const double* phv,
+                             double scale_sigma, double scale_T, double scale_rho, int nx, int ny, int nz);
+/* SmoothConductivityV2C        :111-114 */
+int ht3d_SmoothConductivityV2C(ht3d_ctx* ctx, double* ktc, const double* ktv, int nx, int ny, int nz);
+/* SmoothConductivityC2V        :116-119 */
+int ht3d_SmoothConductivityC2V(ht3d_ctx* ctx, double* ktv, const double* ktc, int nx, int ny, int nz);
+/* InitConductivity!            :133-138 */
+int ht3d_InitConductivity(ht3d_ctx* ctx, double* kx, double* ky, double* kz, const double* ktv, int nx, int ny, int nz);
+/* ComputeρCeffective!          :148-160 */
+int ht3d_ComputeRhoCeffective(ht3d_ctx* ctx, double* rhoC_eff, const double* Tc_ex, const double* Pc_ex,
+                              const double* phc_ex, double phi_i, double sca_T, double sca_sigma, double sca_C,
+                              double sca_rho, int nx, int ny, int nz);
+/* ResidualTemperatureLinearised!  :162-181 */
+int ht3d_ResidualTemperatureLinearised(ht3d_ctx* ctx, double* F, const double* Tc_ex, const double* Tc_old,
+                                       const double* rhoC_eff, const double* phc_ex, const double* PC,
+                                       const double* qx, const double* qy, const double* qz, double Qt,
+                                       double transient, double _dt, double _dx, double _dy, double _dz, int nx,
+                                       int ny, int nz);
+/* SetTemperatureBCs! (dimensional)  :183-205; the reference's unused arguments are kept */
+int ht3d_SetTemperatureBCs(ht3d_ctx* ctx, double* Tc_ex, const double* ky, const double* wN, const double* phc_ex,
+                           double qyS, double _dy, double kS, double TS, double TN, double y_plateau, double a2,
+                           double b2, double dTdy, double dx, double dy, int sticky_air, double sca_T, double sca_kT,
+                           double phi_i, int nx, int ny, int nz);
+/* SetPressureBCs! (dimensional)     :291-314 */
+int ht3d_SetPressureBCs_dim(ht3d_ctx* ctx, double* Pc_ex, const double* wN, const double* phc_ex, double PS,
+                            double PN, double y_plateau, double a2, double b2, double rhof, double g, double dx,
+                            double dy, int sticky_air, int nx, int ny, int nz);
+/* ϕρf                          :225-235 */
+int ht3d_PhiRhof(ht3d_ctx* ctx, double* phirhofc, const double* Tc_ex, const double* Pc_ex, const double* phc_ex,
+                 double phi_i, double scale_rho, double scale_T, double scale_sigma, int nx, int ny, int nz);
+/* ϕρf_old                      :237-247 */
+int ht3d_PhiRhofOld(ht3d_ctx* ctx, double* phirhofc, const double* Tc0, const double* Pc0, const double* phc_ex,
+                    double phi_i, double scale_rho, double scale_T, double scale_sigma, int nx, int ny, int nz);
+/* ϕdρdP!                       :249-259 */
+int ht3d_PhiDrhodP(ht3d_ctx* ctx, double* phidrhodP, const double* Tc_ex, const double* Pc_ex, const double* phc_ex,
+                   double phi_i, double scale_rho, double scale_T, double scale_sigma, int nx, int ny, int nz);
+/* ComputeDarcyFlux!            :266-272 */
+int ht3d_ComputeDarcyFlux(ht3d_ctx* ctx, double* qx, double* qy, double* qz, const double* rhofv, const double* kx,
+                          const double* ky, const double* kz, const double* Pf, double g, double _dx, double _dy,
+                          double _dz, int nx, int ny, int nz);
+/* ResidualFluidPressure!       :274-289 */
+int ht3d_ResidualFluidPressure(ht3d_ctx* ctx, double* F, const double* phc_ex, const double* phirhofc,
+                               const double* phirhofc0, const double* PC, const double* qx, const double* qy,
+                               const double* qz, double transient, double _dt, double _dx, double _dy, double _dz,
+                               int nx, int ny, int nz);
+/* Init_vel! (dimensional)      :328-333 */
+int ht3d_Init_vel_dim(ht3d_ctx* ctx, double* Vx, double* Vy, double* Vz, const double* qx, const double* qy,
+                      const double* qz, const double* rhofv, int nx, int ny, int nz);
+/* material laws (Dimensional/HydroThermal3D_v18.jl:29-39) evaluated elementwise:
+   which 0 kTs(T), 1 kTf(T), 2 Cf(T), 3 Cs(T), 4 ρs(T), 5 ρf_C(T_C,p), 6 dρdP_C(T_C,p),
+   7 μf(T), 8 kF(y,δ), 9 ϕ(phase,ϕ0); b may be NULL for one-argument laws */
+int ht3d_material_law(ht3d_ctx* ctx, int which, const double* a, const double* b, double* out, long long n);
+
+/* ------------------------------------------------------------------ */
 /* WENO5 advection                                                     */
 /* ------------------------------------------------------------------ */
 /* V{x,y,z}PlusMinus!   tools/Weno5_Routines.jl:5-42 (axis 0,1,2) */
@@ -277,6 +366,17 @@ int ht3d_dyrel_iterate_f32(ht3d_ctx* ctx, float* X_ex, const float* R, const flo
 int ht3d_step_hrl(ht3d_ctx* ctx, double* Tc_ex, double* Pc_ex, const double* ktv, const double* kfv, double* Vx,
                   double* Vy, double* Vz, ht3d_hrl_params* p, ht3d_dyrel_stats* st_thermal,
                   ht3d_dyrel_stats* st_darcy, int precision, int nx, int ny, int nz);
+
+/* One time step of the dimensional model, Dimensional/HydroThermal3D_v18.jl:404-572:
+   pluton insertion at it == 1, thermal DYREL solve (conductivity, smoothing,
+   ρC_eff, Gershgorin), Darcy DYREL solve (ρk/μ, ϕ∂ρ/∂P, ϕρf_old, ρf), Darcy
+   velocity and WENO5-v2 advection with sub-stepping.  phc_ex (ex) and phv
+   (vertices) are phase codes, wN the immersed-surface weights (nx+2, nz+2),
+   kmul_v an optional vertex multiplier of kF(y) (NULL = reference law).
+   Fused FP64 kernels with the reference's rounding. */
+int ht3d_step_v18(ht3d_ctx* ctx, double* Tc_ex, double* Pc_ex, const double* phc_ex, const double* phv,
+                  const double* wN, const double* kmul_v, double* Vx, double* Vy, double* Vz, ht3d_v18_params* p,
+                  ht3d_dyrel_stats* st_thermal, ht3d_dyrel_stats* st_darcy, int nx, int ny, int nz);
 
 #ifdef __cplusplus
 }
