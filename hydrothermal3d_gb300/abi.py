@@ -8,6 +8,7 @@ BC_NEUMANN, BC_DIRICHLET, BC_PERIODIC = 0, 1, 2
 WENO_V1, WENO_V2_REF, WENO_V2_FIXED = 0, 1, 2
 RED_SUM, RED_SUM_ABS, RED_MAX, RED_MIN, RED_MAX_ABS = 0, 1, 2, 3, 4
 TUNE_DYREL_VARIANT = 1
+TUNE_MIXED_REFRESH = 2
 DYREL_ZMARCH, DYREL_CELL = 1, 2
 
 
@@ -87,3 +88,12 @@ def int6(*v):
 
 def dbl6(*v):
     return Dbl6(*[float(x) for x in v])
+
+
+class V18Params(ctypes.Structure):
+    """ht3d_v18_params: one time step of the dimensional model (Dimensional/HydroThermal3D_v18.jl)."""
+    _fields_ = [(f, ctypes.c_double) for f in (
+        "dx", "dy", "dz", "ymin", "dt", "time", "phi_i", "k_fact", "delta", "g", "Qt", "qyS", "Ttop", "Tbot", "Ptop",
+        "Pbot", "T_pluton", "C_adv", "sc_T", "sc_L", "sc_t", "sc_eta", "sc_sigma", "sc_rho", "sc_C", "sc_kt")] + [
+        (f, ctypes.c_int) for f in ("it", "thermal", "hydro", "advection", "dt_constant", "weno_variant")] + [
+        ("thermal_dyrel", DyrelParams), ("darcy_dyrel", DyrelParams), ("n_adv", ctypes.c_int), ("pad_", ctypes.c_int)]

@@ -82,8 +82,10 @@ def from_numpy(a, device="cuda"):
     """Copy a numpy array (any order) into a column-major device tensor."""
     import numpy as np
     a = np.asarray(a, dtype=np.float64)
-    if a.ndim == 2:
-        a = a[:, :, None]
+    if a.ndim == 2:  # column-major 2-D (e.g. the immersed-surface weights wN)
+        t = torch.zeros((a.shape[1], a.shape[0]), dtype=torch.float64, device=device).t()
+        t.copy_(torch.from_numpy(np.ascontiguousarray(a.T)).t())
+        return t
     t = zeros(*a.shape, device=device)
     t.copy_(torch.from_numpy(np.ascontiguousarray(a.transpose(2, 1, 0))).permute(2, 1, 0))
     return t
@@ -384,4 +386,122 @@ def step_hrl(ctx, Tc_ex, Pc_ex, ktv, kfv, Vx, Vy, Vz, params, precision=abi.FP64
     ctx.call("ht3d_step_hrl", _ptr(Tc_ex, S["ex"]), _ptr(Pc_ex, S["ex"]), _ptr(ktv, S["v"]), _ptr(kfv, S["v"]),
              _ptr(Vx, S["fx"]), _ptr(Vy, S["fy"]), _ptr(Vz, S["fz"]), ctypes.byref(params), ctypes.byref(st_t),
              ctypes.byref(st_d), precision, nx, ny, nz)
+    return st_t, st_d
+
+
+# ------------------------------------------------------ dimensional kernels
+def ComputeThermalConductivity(ctx, ktv, Tce, phv, phi0, scale_kt, scale_T):
+    nx, ny, nz = _cells_ex(Tce, "Tce"); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_ComputeThermalConductivity", _ptr(ktv, S["v"]), _ptr(Tce, S["ex"]), _ptr(phv, S["v"]), phi0,
+             scale_kt, scale_T, nx, ny, nz)
+
+
+def ComputeHydroConductivity(ctx, kfv, Tce, Pce, phv, ymin, dy, k_fact, delta, scale_sigma, scale_T, scale_L,
+                             scale_t, scale_eta, mode, kmul=None):
+    nx, ny, nz = _cells_ex(Tce, "Tce"); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_ComputeHydroConductivity", _ptr(kfv, S["v"]), _ptr(Tce, S["ex"]), _ptr(Pce, S["ex"]),
+             _ptr(phv, S["v"]), ymin, dy, k_fact, delta, scale_sigma, scale_T, scale_L, scale_t, scale_eta, mode,
+             None if kmul is None else _ptr(kmul, S["v"]), nx, ny, nz)
+
+
+def ComputeFluidDensity(ctx, rhofv, Tce, Pce, phv, scale_sigma, scale_T, scale_rho):
+    nx, ny, nz = _cells_ex(Tce, "Tce"); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_ComputeFluidDensity", _ptr(rhofv, S["v"]), _ptr(Tce, S["ex"]), _ptr(Pce, S["ex"]),
+             _ptr(phv, S["v"]), scale_sigma, scale_T, scale_rho, nx, ny, nz)
+
+
+def SmoothConductivityV2C(ctx, ktc, ktv):
+    nx, ny, nz = _cells(ktc)
+    ctx.call("ht3d_SmoothConductivityV2C", _ptr(ktc), _ptr(ktv, (nx + 1, ny + 1, nz + 1)), nx, ny, nz)
+
+
+def SmoothConductivityC2V(ctx, ktv, ktc):
+    nx, ny, nz = _cells(ktc)
+    ctx.call("ht3d_SmoothConductivityC2V", _ptr(ktv, (nx + 1, ny + 1, nz + 1)), _ptr(ktc), nx, ny, nz)
+
+
+def InitConductivity(ctx, kx, ky, kz, ktv):
+    nx, ny, nz = (int(s) - 1 for s in ktv.shape); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_InitConductivity", _ptr(kx, S["fx"]), _ptr(ky, S["fy"]), _ptr(kz, S["fz"]), _ptr(ktv), nx, ny, nz)
+
+
+def ComputeRhoCeffective(ctx, rhoC_eff, Tc_ex, Pc_ex, phc_ex, phi_i, sca_T, sca_sigma, sca_C, sca_rho):
+    nx, ny, nz = _cells(rhoC_eff); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_ComputeRhoCeffective", _ptr(rhoC_eff), _ptr(Tc_ex, S["ex"]), _ptr(Pc_ex, S["ex"]),
+             _ptr(phc_ex, S["ex"]), phi_i, sca_T, sca_sigma, sca_C, sca_rho, nx, ny, nz)
+
+
+def ResidualTemperatureLinearised(ctx, F, Tc_ex, Tc_old, rhoC_eff, phc_ex, PC, qx, qy, qz, Qt, transient, _dt, _dx,
+                                  _dy, _dz):
+    nx, ny, nz = _cells(F); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_ResidualTemperatureLinearised", _ptr(F), _ptr(Tc_ex, S["ex"]), _ptr(Tc_old, S["c"]),
+             _ptr(rhoC_eff, S["c"]), _ptr(phc_ex, S["ex"]), _ptr(PC, S["c"]), _ptr(qx, S["fx"]), _ptr(qy, S["fy"]),
+             _ptr(qz, S["fz"]), Qt, transient, _dt, _dx, _dy, _dz, nx, ny, nz)
+
+
+def SetTemperatureBCs(ctx, Tc_ex, ky, wN, phc_ex, qyS, _dy, kS, TS, TN, y_plateau=0.0, a2=0.0, b2=0.0, dTdy=0.0,
+                      dx=0.0, dy=0.0, sticky_air=0, sca_T=1.0, sca_kT=1.0, phi_i=0.0):
+    nx, ny, nz = _cells_ex(Tc_ex, "Tc_ex"); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_SetTemperatureBCs", _ptr(Tc_ex), _ptr(ky, S["fy"]), _ptr(wN, (nx + 2, nz + 2)),
+             _ptr(phc_ex, S["ex"]), qyS, _dy, kS, TS, TN, y_plateau, a2, b2, dTdy, dx, dy, int(sticky_air), sca_T,
+             sca_kT, phi_i, nx, ny, nz)
+
+
+def SetPressureBCs_dim(ctx, Pc_ex, wN, phc_ex, PS, PN, y_plateau=0.0, a2=0.0, b2=0.0, rhof=0.0, g=0.0, dx=0.0,
+                       dy=0.0, sticky_air=0):
+    nx, ny, nz = _cells_ex(Pc_ex, "Pc_ex"); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_SetPressureBCs_dim", _ptr(Pc_ex), _ptr(wN, (nx + 2, nz + 2)), _ptr(phc_ex, S["ex"]), PS, PN,
+             y_plateau, a2, b2, rhof, g, dx, dy, int(sticky_air), nx, ny, nz)
+
+
+def _phirhof(name, ctx, out, T, P, phc_ex, phi_i, scale_rho, scale_T, scale_sigma):
+    nx, ny, nz = _cells(out); S = _shapes(nx, ny, nz)
+    ctx.call(name, _ptr(out), _ptr(T), _ptr(P), _ptr(phc_ex, S["ex"]), phi_i, scale_rho, scale_T, scale_sigma,
+             nx, ny, nz)
+
+
+def PhiRhof(ctx, phirhofc, Tc_ex, Pc_ex, phc_ex, phi_i, scale_rho, scale_T, scale_sigma):
+    _phirhof("ht3d_PhiRhof", ctx, phirhofc, Tc_ex, Pc_ex, phc_ex, phi_i, scale_rho, scale_T, scale_sigma)
+
+
+def PhiRhofOld(ctx, phirhofc, Tc0, Pc0, phc_ex, phi_i, scale_rho, scale_T, scale_sigma):
+    _phirhof("ht3d_PhiRhofOld", ctx, phirhofc, Tc0, Pc0, phc_ex, phi_i, scale_rho, scale_T, scale_sigma)
+
+
+def PhiDrhodP(ctx, phidrhodP, Tc_ex, Pc_ex, phc_ex, phi_i, scale_rho, scale_T, scale_sigma):
+    _phirhof("ht3d_PhiDrhodP", ctx, phidrhodP, Tc_ex, Pc_ex, phc_ex, phi_i, scale_rho, scale_T, scale_sigma)
+
+
+def ComputeDarcyFlux(ctx, qx, qy, qz, rhofv, kx, ky, kz, Pf, g, _dx, _dy, _dz):
+    nx, ny, nz = _cells_ex(Pf, "Pf"); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_ComputeDarcyFlux", _ptr(qx, S["fx"]), _ptr(qy, S["fy"]), _ptr(qz, S["fz"]), _ptr(rhofv, S["v"]),
+             _ptr(kx, S["fx"]), _ptr(ky, S["fy"]), _ptr(kz, S["fz"]), _ptr(Pf, S["ex"]), g, _dx, _dy, _dz, nx, ny, nz)
+
+
+def ResidualFluidPressure(ctx, F, phc_ex, phirhofc, phirhofc0, PC, qx, qy, qz, transient, _dt, _dx, _dy, _dz):
+    nx, ny, nz = _cells(F); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_ResidualFluidPressure", _ptr(F), _ptr(phc_ex, S["ex"]), _ptr(phirhofc, S["c"]),
+             _ptr(phirhofc0, S["c"]), _ptr(PC, S["c"]), _ptr(qx, S["fx"]), _ptr(qy, S["fy"]), _ptr(qz, S["fz"]),
+             transient, _dt, _dx, _dy, _dz, nx, ny, nz)
+
+
+def Init_vel_dim(ctx, Vx, Vy, Vz, qx, qy, qz, rhofv):
+    nx, ny, nz = (int(s) - 1 for s in rhofv.shape); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_Init_vel_dim", _ptr(Vx, S["fx"]), _ptr(Vy, S["fy"]), _ptr(Vz, S["fz"]), _ptr(qx, S["fx"]),
+             _ptr(qy, S["fy"]), _ptr(qz, S["fz"]), _ptr(rhofv, S["v"]), nx, ny, nz)
+
+
+def material_law(ctx, which, a, b=None):
+    out = torch.empty_like(a)
+    ctx.call("ht3d_material_law", which, _ptr(a), None if b is None else _ptr(b), _ptr(out), _numel(a))
+    return out
+
+
+def step_v18(ctx, Tc_ex, Pc_ex, phc_ex, phv, wN, kmul, Vx, Vy, Vz, params):
+    nx, ny, nz = _cells_ex(Tc_ex, "Tc_ex"); S = _shapes(nx, ny, nz)
+    st_t, st_d = abi.DyrelStats(), abi.DyrelStats()
+    ctx.call("ht3d_step_v18", _ptr(Tc_ex, S["ex"]), _ptr(Pc_ex, S["ex"]), _ptr(phc_ex, S["ex"]), _ptr(phv, S["v"]),
+             _ptr(wN, (nx + 2, nz + 2)), None if kmul is None else _ptr(kmul, S["v"]), _ptr(Vx, S["fx"]),
+             _ptr(Vy, S["fy"]), _ptr(Vz, S["fz"]), ctypes.byref(params), ctypes.byref(st_t), ctypes.byref(st_d),
+             nx, ny, nz)
     return st_t, st_d

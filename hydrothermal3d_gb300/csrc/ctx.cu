@@ -154,6 +154,11 @@ int ht3d_ctx_set_tuning(ht3d_ctx* ctx, int key, int value) {
         ctx->dyrel_variant = value;
         return HT3D_OK;
     }
+    if (key == HT3D_TUNE_MIXED_REFRESH) {
+        if (value < 0) return HT3D_ERR_ARG;
+        ctx->mixed_refresh = value;
+        return HT3D_OK;
+    }
     return HT3D_ERR_ARG;
 }
 

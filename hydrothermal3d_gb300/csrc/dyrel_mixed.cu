@@ -192,13 +192,18 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
     int it_done = 0, converged = 0, status = HT3D_OK, checks = 0;
     bool last_check = false;
     const int nmax = n_iter_fixed > 0 ? n_iter_fixed : prm->nitmax;
+    const int refresh_every = ctx->mixed_refresh;
     for (int iter = 1; iter <= nmax; ++iter) {
         const bool chk = is_check(iter, prm->nitout);
+        // defect-correction refresh between the reference's checks: fold D into X
+        // and recompute the FP64 residual so the FP32 iteration never works
+        // below its own precision (no stop test, no parameter update)
+        const bool refresh = !chk && refresh_every > 0 && iter % refresh_every == 0;
         const bool storef = !chk && (iter == nmax || is_check(iter + 1, prm->nitout));
         sc.h1 = S.h1;
         sc.h2 = S.h2;
         sc.dtau = S.dtau;
-        if (chk) {
+        if (chk || refresh) {
             HT3D_LAUNCH(ctx, k_mixed_check, LC.grid, LC.block, 0, xcur, xnxt, dcur, dnxt, R, kx, ky, kz, invPC, F0s, Fs,
                         F, Rin, sc, bc, nx, ny, nz, LC.zchunk, parts);
             std::swap(xcur, xnxt);

@@ -34,6 +34,7 @@ struct ht3d_ctx {
     bool own_stream = false;
     int sync_each_call = 1;
     int dyrel_variant = HT3D_DYREL_CELL;  // thread layout of the fused DYREL iteration
+    int mixed_refresh = 64;               // FP64 defect-correction cadence of the mixed solver
     int num_sms = 152;
     unsigned long long launches = 0;
     std::string last_error;

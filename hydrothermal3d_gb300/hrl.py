@@ -15,6 +15,10 @@ Boundary conditions (Alban_v6.jl:108-130, 153-159):
             (Dimensionless/kernels_HT3D.jl:164-177)
 Time step: dt0 = min(dx,dy,dz)^2/6.1 (Dimensionless/HydroThermal3D_v7.jl:68),
 then dt = dt_fact/6.1*min(dx,dy,dz)/max|V| after each step (v7.jl:220).
+dt_fact defaults to 1: with v7's value 10 the next step's dt is set from a
+velocity that the onset of convection then multiplies by ~30, the CFL number
+reaches ~50 and WENO5/SSP-RK2 blows up within five steps (T leaves [0, 1]);
+with 1 the onset peaks near CFL 7 and the run settles at CFL 0.17.
 """
 import numpy as np
 
@@ -39,7 +43,7 @@ def initial_fields(nx, ny, nz, seed=1, amp=1e-3, Tbot=1.0, Ttop=0.0, L=(1.0, 1.0
     return T, P, ktv, kfv
 
 
-def params(nx, ny, nz, Ra=1000.0, tol=1e-8, nitmax=10000, nitout=1000, dt_fact=10.0, weno_variant=abi.WENO_V1,
+def params(nx, ny, nz, Ra=1000.0, tol=1e-8, nitmax=10000, nitout=1000, dt_fact=1.0, weno_variant=abi.WENO_V1,
            L=(1.0, 1.0, 1.0), Tbot=1.0, Ttop=0.0, advection=True, dt_adapt=True):
     Lx, Ly, Lz = L
     dx, dy, dz = Lx / nx, Ly / ny, Lz / nz

@@ -1,0 +1,111 @@
+"""Set-up of the dimensional workload (the kernels and driver logic of
+Dimensional/HydroThermal3D_v18.jl) on a synthetic box.
+
+scaling() restates `scaling`/`scale_me!` (Dimensional/kernels_HT3D_dimensional.jl:3-36)
+with the v18 characteristic values (T 500 K, V 1e-9 m/s, L 700 m, eta 1e10 Pa s).
+
+box() builds the benchmark box: x 10 km, y (vertical) 10 km below the surface
+at y = 0, z 5 km; T linear from T_bot to T_top; hydrostatic pressure; crust
+everywhere with the top ghost row as air (phase 1, held at T_top / P_top);
+permeability log10 k ~ N(mean, sigma) with a Gaussian correlation length,
+built on the host in FP64 from seeded white noise filtered by FFT.  The
+reference's depth law kF(y) = 5e-16 exp(y/delta) is neutralised (delta -> inf)
+and the field enters ComputeHydroConductivity as the vertex multiplier kmul.
+"""
+import math
+
+import numpy as np
+
+from . import abi
+
+
+def scaling(T=500.0, V=1e-9, L=700.0, eta=1e10):
+    s = dict(T=T, V=V, L=L, eta=eta)
+    s["t"] = L / V
+    s["a"] = V / s["t"]
+    s["eps"] = 1.0 / s["t"]
+    s["sigma"] = eta / s["t"]
+    s["m"] = s["sigma"] * L * s["t"] ** 2
+    s["rho"] = s["m"] / L ** 3
+    s["F"] = s["m"] * L / s["t"] ** 2
+    s["J"] = s["m"] * L ** 2 / s["t"] ** 2
+    s["W"] = s["J"] / s["t"]
+    s["C"] = s["J"] / s["m"] / T
+    s["kt"] = s["W"] / L / T
+    s["kf"] = L ** 2
+    return s
+
+
+def lognormal_field(shape, spacing, mean=-15.0, sigma=0.5, corr=500.0, seed=2):
+    """log10 k with a Gaussian covariance of length `corr` (m), FFT-filtered
+    white noise normalised to the requested mean and standard deviation."""
+    rng = np.random.default_rng(seed)
+    w = rng.standard_normal(shape)
+    k2 = 0.0
+    for ax, (n, h) in enumerate(zip(shape, spacing)):
+        f = np.fft.fftfreq(n, d=h) * 2 * np.pi
+        sh = [1] * len(shape)
+        sh[ax] = n
+        k2 = k2 + (f.reshape(sh)) ** 2
+    g = np.real(np.fft.ifftn(np.fft.fftn(w) * np.exp(-k2 * corr ** 2 / 4.0)))
+    g = (g - g.mean()) / (g.std() if g.std() > 0 else 1.0)
+    return mean + sigma * g
+
+
+def box(nx, ny, nz, Lx=10e3, Ly=10e3, Lz=5e3, T_bot_C=600.0, T_top_C=20.0, seed=2, log10k_mean=-15.0,
+        log10k_sigma=0.5, corr=500.0, tol=1e-10, nitout=1000, nitmax=10000, dt_s=1e11, cfl_adv=0.5,
+        weno_variant=abi.WENO_V2_REF):
+    sc = scaling()
+    L = sc["L"]
+    xmin, xmax = 0.0, Lx / L
+    ymin, ymax = -Ly / L, 0.0
+    zmin, zmax = 0.0, Lz / L
+    dx, dy, dz = (xmax - xmin) / nx, (ymax - ymin) / ny, (zmax - zmin) / nz
+    Ttop = (T_top_C + 273.15) / sc["T"]
+    Tbot = (T_bot_C + 273.15) / sc["T"]
+    Ptop = 1e5 / sc["sigma"]
+    g = -9.81 / (L / sc["t"] ** 2)
+    rho_w = 1000.0 / sc["rho"]
+    Pbot = Ptop - rho_w * g * (ymax - ymin)
+    yce = np.linspace(ymin - dy / 2, ymax + dy / 2, ny + 2)
+    T = np.empty((nx + 2, ny + 2, nz + 2), order="F")
+    T[...] = (Ttop + (Ttop - Tbot) * (yce - ymax) / (ymax - ymin))[None, :, None]
+    P = np.empty((nx + 2, ny + 2, nz + 2), order="F")
+    P[...] = (Ptop - rho_w * g * (ymax - yce))[None, :, None]
+    phc = np.zeros((nx + 2, ny + 2, nz + 2), order="F")
+    phc[:, -1, :] = 1.0  # air above the surface
+    T[:, -1, :] = Ttop
+    P[:, -1, :] = Ptop
+    phv = np.zeros((nx + 1, ny + 1, nz + 1), order="F")
+    wN = np.full((nx + 2, nz + 2), 0.5, order="F")
+    lk = lognormal_field((nx + 1, ny + 1, nz + 1), (dx * L, dy * L, dz * L), log10k_mean, log10k_sigma, corr, seed)
+    kmul = np.asfortranarray(10.0 ** lk / 5e-16)
+    # basal heat flux consistent with the initial gradient and the rock conductivity at the base
+    kT_base = 3.1138 - 0.0023 * (Tbot * sc["T"])
+    qyS_SI = kT_base * (T_bot_C - T_top_C) / Ly
+    p = abi.V18Params()
+    p.dx, p.dy, p.dz, p.ymin = dx, dy, dz, ymin
+    p.dt = dt_s / sc["t"]
+    p.time = 0.0
+    p.phi_i, p.k_fact, p.delta, p.g, p.Qt = 1e-2, 50.0, 1e30 / L, g, 0.0
+    p.qyS = qyS_SI / (sc["W"] / L ** 2)
+    p.Ttop, p.Tbot, p.Ptop, p.Pbot = Ttop, Tbot, Ptop, Pbot
+    p.T_pluton = (700.0 + 273.15) / sc["T"]
+    p.C_adv = cfl_adv * 6.1
+    p.sc_T, p.sc_L, p.sc_t, p.sc_eta = sc["T"], sc["L"], sc["t"], sc["eta"]
+    p.sc_sigma, p.sc_rho, p.sc_C, p.sc_kt = sc["sigma"], sc["rho"], sc["C"], sc["kt"]
+    p.it, p.thermal, p.hydro, p.advection, p.dt_constant = 0, 1, 1, 1, 1
+    p.weno_variant = weno_variant
+    p.thermal_dyrel = abi.DyrelParams.reference(tol=tol, nitmax=nitmax, nitout=nitout,
+                                                norm_scale=sc["rho"] * sc["C"] * sc["T"] / sc["t"])
+    p.darcy_dyrel = abi.DyrelParams.reference(tol=tol, nitmax=nitmax, nitout=nitout, norm_scale=sc["rho"] / sc["t"])
+    return dict(T=T, P=P, phc=phc, phv=phv, wN=wN, kmul=kmul, params=p)
+
+
+def bytes_per_iteration(nx, ny, nz, s=8):
+    """Algorithmic bytes of one dimensional pseudo-iteration: thermal updates
+    {T, F0} and reads {kx, ky, kz, T0, rhoC, PC} + phase (1 B): 10 N s + N;
+    Darcy updates {P, F0} and reads {kx, ky, kz, T, phirhof0, rhof(y-face), PC}
+    + phase: 11 N s + N.  Returns (thermal, darcy)."""
+    N = nx * ny * nz
+    return 10 * N * s + N, 11 * N * s + N

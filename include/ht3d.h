@@ -60,6 +60,9 @@ extern "C" {
 #define HT3D_TUNE_DYREL_VARIANT 1   /* thread layout of the fused DYREL iteration: */
 #define HT3D_DYREL_ZMARCH 1         /*   32x8 column tiles marching in z            */
 #define HT3D_DYREL_CELL 2           /*   one thread per cell (default)              */
+#define HT3D_TUNE_MIXED_REFRESH 2   /* mixed form: FP64 defect-correction refresh every N
+                                       inner iterations between checks (default 64; 0 = only
+                                       at the reference's check iterations)             */
 
 typedef struct ht3d_ctx ht3d_ctx;
 

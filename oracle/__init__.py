@@ -115,3 +115,16 @@ def step_hrl(T, P, ktv, kfv, Vx, Vy, Vz, params):
     s = fn(_p(T), _p(P), _p(ktv), _p(kfv), _p(Vx), _p(Vy), _p(Vz), ctypes.byref(params), ctypes.byref(st_t),
            ctypes.byref(st_d), ctypes.c_longlong(nx), ctypes.c_longlong(ny), ctypes.c_longlong(nz))
     return s, st_t, st_d
+
+
+def step_v18(T, P, phc, phv, wN, kmul, Vx, Vy, Vz, params):
+    """One dimensional (v18) time step. Returns (status, stats_thermal, stats_darcy)."""
+    from hydrothermal3d_gb300.abi import DyrelStats
+    nx, ny, nz = (s - 2 for s in T.shape)
+    st_t, st_d = DyrelStats(), DyrelStats()
+    fn = load().orc_step_v18
+    fn.restype = ctypes.c_int
+    s = fn(_p(T), _p(P), _p(phc), _p(phv), _p(wN), _p(kmul) if kmul is not None else None, _p(Vx), _p(Vy), _p(Vz),
+           ctypes.byref(params), ctypes.byref(st_t), ctypes.byref(st_d), ctypes.c_longlong(nx), ctypes.c_longlong(ny),
+           ctypes.c_longlong(nz))
+    return s, st_t, st_d

@@ -1,0 +1,168 @@
+"""GPU parity of the dimensional (v18) kernels and time step against the oracle.
+
+The material laws call pow/exp, whose last bit may differ between CUDA's and
+the host's math library; granular kernels are therefore compared at 1e-13
+(relative, max-norm), full solves at 1e-10."""
+import numpy as np
+import pytest
+
+import hydrothermal3d_gb300 as ht
+from hydrothermal3d_gb300 import api, abi, v18
+from conftest import rel_err, no_edges_mask
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-13
+
+
+def setup(n=(9, 8, 7), seed=3):
+    b = v18.box(*n, seed=seed, nitout=50, tol=1e-9)
+    rng = np.random.default_rng(seed)
+    # phases: mostly crust, a fault (2), a pluton (3), air on top, an immersed layer (-1)
+    nx, ny, nz = n
+    phc = b["phc"].copy(order="F")
+    phc[3:5, 2:4, 2:4] = 2.0
+    phc[5:7, 3:5, 3:5] = 3.0
+    phc[:, -2, :] = -1.0
+    phv = np.asfortranarray(np.where(rng.uniform(size=(nx + 1, ny + 1, nz + 1)) < 0.2, 2.0, 0.0))
+    phv[:, -1, :] = 1.0
+    b["phc2"], b["phv2"] = phc, phv
+    b["wN2"] = np.asfortranarray(rng.uniform(0.3, 0.9, (nx + 2, nz + 2)))
+    return b
+
+
+def test_material_laws(ctx, orc):
+    rng = np.random.default_rng(1)
+    a = np.asfortranarray(rng.uniform(300, 900, (50, 1, 1)))
+    b = np.asfortranarray(rng.uniform(1e5, 3e8, (50, 1, 1)))
+    for which in range(10):
+        aa = a - 273.15 if which in (5, 6) else (np.asfortranarray(rng.uniform(-5, 0, a.shape)) if which == 8 else a)
+        bb = b if which in (5, 6) else (np.full(a.shape, 3.0, order="F") if which == 8 else b)
+        if which == 9:
+            aa = np.asfortranarray(rng.integers(-1, 4, a.shape).astype(float))
+            bb = np.full(a.shape, 0.01, order="F")
+        got = ht.to_numpy(api.material_law(ctx, which, ht.from_numpy(aa), ht.from_numpy(bb)))
+        ref = np.array([orc.law(which, x, y) for x, y in zip(aa.ravel(), bb.ravel())]).reshape(aa.shape)
+        assert rel_err(got, ref) <= TOL, which
+
+
+def test_property_kernels(ctx, orc):
+    b = setup()
+    p = b["params"]
+    nx, ny, nz = (s - 2 for s in b["T"].shape)
+    T, P, phc, phv = b["T"], b["P"], b["phc2"], b["phv2"]
+    Td, Pd, phcd, phvd = ht.from_numpy(T), ht.from_numpy(P), ht.from_numpy(phc), ht.from_numpy(phv)
+    kv, kvd = np.zeros((nx + 1, ny + 1, nz + 1), order="F"), ht.zeros(nx + 1, ny + 1, nz + 1)
+    orc.call("ComputeThermalConductivity", kv, T, phv, p.phi_i, p.sc_kt, p.sc_T, nx, ny, nz)
+    api.ComputeThermalConductivity(ctx, kvd, Td, phvd, p.phi_i, p.sc_kt, p.sc_T)
+    assert rel_err(ht.to_numpy(kvd), kv) <= TOL
+    import ctypes
+    for mode in (1, 2, 3):
+        for kmul in (None, b["kmul"]):
+            orc.call("ComputeHydroConductivity", kv, T, P, phv, p.ymin, p.dy, p.k_fact, 3000.0 / p.sc_L, p.sc_sigma,
+                     p.sc_T, p.sc_L, p.sc_t, p.sc_eta, ctypes.c_int(mode), kmul, nx, ny, nz)
+            api.ComputeHydroConductivity(ctx, kvd, Td, Pd, phvd, p.ymin, p.dy, p.k_fact, 3000.0 / p.sc_L, p.sc_sigma,
+                                         p.sc_T, p.sc_L, p.sc_t, p.sc_eta, mode,
+                                         None if kmul is None else ht.from_numpy(kmul))
+            assert rel_err(ht.to_numpy(kvd), kv) <= TOL, mode
+    orc.call("ComputeFluidDensity", kv, T, P, phv, p.sc_sigma, p.sc_T, p.sc_rho, nx, ny, nz)
+    api.ComputeFluidDensity(ctx, kvd, Td, Pd, phvd, p.sc_sigma, p.sc_T, p.sc_rho)
+    assert rel_err(ht.to_numpy(kvd), kv) <= TOL
+    c, cd = np.zeros((nx, ny, nz), order="F"), ht.zeros(nx, ny, nz)
+    orc.call("SmoothConductivityV2C", c, kv, nx, ny, nz)
+    api.SmoothConductivityV2C(ctx, cd, kvd)
+    assert rel_err(ht.to_numpy(cd), c) <= TOL
+    orc.call("SmoothConductivityC2V", kv, c, nx, ny, nz)
+    api.SmoothConductivityC2V(ctx, kvd, cd)
+    assert rel_err(ht.to_numpy(kvd), kv) <= TOL
+    k = [np.zeros(s, order="F") for s in ((nx + 1, ny, nz), (nx, ny + 1, nz), (nx, ny, nz + 1))]
+    kd = [ht.zeros(*a.shape) for a in k]
+    orc.call("InitConductivity", *k, kv, nx, ny, nz)
+    api.InitConductivity(ctx, *kd, kvd)
+    for a, bb in zip(kd, k):
+        assert rel_err(ht.to_numpy(a), bb) <= TOL
+    rC, rCd = np.zeros((nx, ny, nz), order="F"), ht.zeros(nx, ny, nz)
+    orc.call("ComputeRhoCeffective", rC, T, P, phc, p.phi_i, p.sc_T, p.sc_sigma, p.sc_C, p.sc_rho, nx, ny, nz)
+    api.ComputeRhoCeffective(ctx, rCd, Td, Pd, phcd, p.phi_i, p.sc_T, p.sc_sigma, p.sc_C, p.sc_rho)
+    assert rel_err(ht.to_numpy(rCd), rC) <= TOL
+    for name, args, cell in (("PhiRhof", (T, P), 0), ("PhiDrhodP", (T, P), 0)):
+        o, od = np.zeros((nx, ny, nz), order="F"), ht.zeros(nx, ny, nz)
+        orc.call("phi_rhof", o, *args, phc, p.phi_i, p.sc_rho, p.sc_T, p.sc_sigma, ctypes.c_int(cell),
+                 ctypes.c_int(1 if name == "PhiDrhodP" else 0), nx, ny, nz)
+        getattr(api, name)(ctx, od, Td, Pd, phcd, p.phi_i, p.sc_rho, p.sc_T, p.sc_sigma)
+        assert rel_err(ht.to_numpy(od), o) <= TOL, name
+
+
+def test_boundary_kernels_snapshot_semantics(ctx, orc):
+    b = setup()
+    p = b["params"]
+    nx, ny, nz = (s - 2 for s in b["T"].shape)
+    rng = np.random.default_rng(9)
+    ky = np.asfortranarray(rng.uniform(0.5, 2, (nx, ny + 1, nz)))
+    T = b["T"] + np.asfortranarray(rng.uniform(-0.01, 0.01, b["T"].shape))
+    To, Td = T.copy(order="F"), ht.from_numpy(T)
+    orc.call("SetTemperatureBCs_dim", To, ky, b["wN2"], b["phc2"], p.qyS, 1 / p.dy, p.Ttop, nx, ny, nz)
+    api.SetTemperatureBCs(ctx, Td, ht.from_numpy(ky), ht.from_numpy(b["wN2"]), ht.from_numpy(b["phc2"]), p.qyS,
+                          1 / p.dy, 1.0, p.Tbot, p.Ttop)
+    np.testing.assert_array_equal(ht.to_numpy(Td), To)
+    P = b["P"] * (1 + np.asfortranarray(rng.uniform(-0.01, 0.01, b["P"].shape)))
+    Po, Pd = P.copy(order="F"), ht.from_numpy(P)
+    orc.call("SetPressureBCs_dim", Po, b["wN2"], b["phc2"], p.Ptop, nx, ny, nz)
+    api.SetPressureBCs_dim(ctx, Pd, ht.from_numpy(b["wN2"]), ht.from_numpy(b["phc2"]), p.Pbot, p.Ptop)
+    np.testing.assert_array_equal(ht.to_numpy(Pd), Po)
+
+
+def test_flux_and_residual_kernels(ctx, orc):
+    b = setup()
+    p = b["params"]
+    nx, ny, nz = (s - 2 for s in b["T"].shape)
+    rng = np.random.default_rng(10)
+    k = [np.asfortranarray(rng.uniform(0.5, 2, s)) for s in ((nx + 1, ny, nz), (nx, ny + 1, nz), (nx, ny, nz + 1))]
+    kd = [ht.from_numpy(a) for a in k]
+    rfv = np.asfortranarray(rng.uniform(0.9, 1.1, (nx + 1, ny + 1, nz + 1)))
+    q = [np.zeros(a.shape, order="F") for a in k]
+    qd = [ht.zeros(*a.shape) for a in k]
+    h = (1 / p.dx, 1 / p.dy, 1 / p.dz)
+    orc.call("ComputeDarcyFlux", *q, rfv, *k, b["P"], p.g, *h, nx, ny, nz)
+    api.ComputeDarcyFlux(ctx, *qd, ht.from_numpy(rfv), *kd, ht.from_numpy(b["P"]), p.g, *h)
+    for a, bb in zip(qd, q):
+        assert rel_err(ht.to_numpy(a), bb) <= TOL
+    F, Fd = np.zeros((nx, ny, nz), order="F"), ht.zeros(nx, ny, nz)
+    prf, prf0, PC = (np.asfortranarray(rng.uniform(0.5, 1.5, (nx, ny, nz))) for _ in range(3))
+    orc.call("ResidualFluidPressure", F, b["phc2"], prf, prf0, PC, *q, 1.0, 3.0, *h, nx, ny, nz)
+    api.ResidualFluidPressure(ctx, Fd, ht.from_numpy(b["phc2"]), ht.from_numpy(prf), ht.from_numpy(prf0),
+                              ht.from_numpy(PC), *qd, 1.0, 3.0, *h)
+    assert rel_err(ht.to_numpy(Fd), F) <= TOL
+    T0 = np.asfortranarray(b["T"][1:-1, 1:-1, 1:-1] * 0.99)
+    orc.call("ResidualTemperatureLinearised", F, b["T"], T0, prf, b["phc2"], PC, *q, 0.5, 1.0, 3.0, *h, nx, ny, nz)
+    api.ResidualTemperatureLinearised(ctx, Fd, ht.from_numpy(b["T"]), ht.from_numpy(T0), ht.from_numpy(prf),
+                                      ht.from_numpy(b["phc2"]), ht.from_numpy(PC), *qd, 0.5, 1.0, 3.0, *h)
+    assert rel_err(ht.to_numpy(Fd), F) <= TOL
+    V = [np.zeros(a.shape, order="F") for a in k]
+    Vd = [ht.zeros(*a.shape) for a in k]
+    orc.call("Init_vel_dim", *V, *q, rfv, nx, ny, nz)
+    api.Init_vel_dim(ctx, *Vd, *qd, ht.from_numpy(rfv))
+    for a, bb in zip(Vd, V):
+        assert rel_err(ht.to_numpy(a), bb) <= TOL
+
+
+@pytest.mark.parametrize("n", [(8, 9, 6), (24, 20, 12)])
+def test_step_v18_matches_oracle(ctx, orc, n):
+    b = setup(n)
+    nx, ny, nz = n
+    V = [np.zeros(s, order="F") for s in ((nx + 1, ny, nz), (nx, ny + 1, nz), (nx, ny, nz + 1))]
+    T, P = b["T"].copy(order="F"), b["P"].copy(order="F")
+    Td, Pd = ht.from_numpy(T), ht.from_numpy(P)
+    Vd = [ht.zeros(*v.shape) for v in V]
+    phc, phv, wN, kmul = b["phc"], b["phv"], b["wN"], b["kmul"]
+    args_d = (ht.from_numpy(phc), ht.from_numpy(phv), ht.from_numpy(wN), ht.from_numpy(kmul))
+    p_o, p_d = b["params"], v18.box(*n, seed=3, nitout=50, tol=1e-9)["params"]
+    for it in range(3):
+        p_o.it = p_d.it = it
+        s, st_t, st_p = orc.step_v18(T, P, phc, phv, wN, kmul, *V, p_o)
+        assert s == 0
+        gt, gp = api.step_v18(ctx, Td, Pd, *args_d, *Vd, p_d)
+        assert gt.status == 0 and gp.status == 0
+        assert abs(gt.iters - st_t.iters) <= p_o.thermal_dyrel.nitout and abs(gp.iters - st_p.iters) <= p_o.darcy_dyrel.nitout
+        assert p_d.n_adv == p_o.n_adv
+        assert rel_err(ht.to_numpy(Td)[1:-1, 1:-1, 1:-1], T[1:-1, 1:-1, 1:-1]) <= 1e-10
+        assert rel_err(ht.to_numpy(Pd)[1:-1, 1:-1, 1:-1], P[1:-1, 1:-1, 1:-1]) <= 1e-10
