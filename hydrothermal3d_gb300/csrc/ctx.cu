@@ -44,7 +44,7 @@ static double reduce_impl(ht3d_ctx* ctx, const T* a, long long n, int op, double
     long long want = (n + threads - 1) / threads;
     int blocks = (int)std::min<long long>(want, (long long)ctx->num_sms * 4);
     if (blocks < 1) blocks = 1;
-    double* parts = (double*)ht3d_scratch(ctx, SLOT_PARTIALS, sizeof(double) * 4096 * 4);
+    double* parts = (double*)ht3d_scratch(ctx, SLOT_REDUCE, sizeof(double) * 4096 * 4);
     double* out = d_out ? d_out : (double*)ht3d_scratch(ctx, SLOT_RESULT, sizeof(double) * 64);
     switch (op) {
 #define RCASE(OPV)                                                                      \
@@ -150,7 +150,7 @@ int ht3d_ctx_set_sync(ht3d_ctx* ctx, int sync_each_call) {
 int ht3d_ctx_set_tuning(ht3d_ctx* ctx, int key, int value) {
     if (!ctx) return HT3D_ERR_ARG;
     if (key == HT3D_TUNE_DYREL_VARIANT) {
-        if (value != HT3D_DYREL_ZMARCH && value != HT3D_DYREL_CELL) return HT3D_ERR_ARG;
+        if (value != 0 && value != HT3D_DYREL_ZMARCH && value != HT3D_DYREL_CELL) return HT3D_ERR_ARG;
         ctx->dyrel_variant = value;
         return HT3D_OK;
     }

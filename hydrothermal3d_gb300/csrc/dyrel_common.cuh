@@ -239,9 +239,14 @@ struct IterLaunch {
     long long nblocks;
 };
 
-inline IterLaunch iter_launch(ht3d_ctx* ctx, int nx, int ny, int nz, int force_variant = 0) {
+// elem_bytes selects the default layout when the context leaves it open
+// (measured on GB300 at 255^3: FP64 is FP64-ALU bound and prefers the z-march
+// tiles, FP32 is latency bound and prefers one thread per cell)
+inline IterLaunch iter_launch(ht3d_ctx* ctx, int nx, int ny, int nz, int force_variant = 0, int elem_bytes = 8) {
     IterLaunch L;
-    const int v = force_variant ? force_variant : ctx->dyrel_variant;
+    const int v = force_variant ? force_variant
+                                : (ctx->dyrel_variant ? ctx->dyrel_variant
+                                                      : (elem_bytes == 8 ? HT3D_DYREL_ZMARCH : HT3D_DYREL_CELL));
     L.variant = v == HT3D_DYREL_ZMARCH ? HT3D_DYREL_ZMARCH : HT3D_DYREL_CELL;
     if (L.variant == HT3D_DYREL_CELL) {
         L.block = dim3(CX_, CY_, CZ_);
@@ -313,7 +318,7 @@ static int dyrel_iterate_impl(ht3d_ctx* ctx, T* X, const T* R, const T* kx, cons
         bc.dir[f] = bc_type6[f];
         bc.val2[f] = (T)(2.0 * bc_val6[f]);
     }
-    IterLaunch L = iter_launch(ctx, nx, ny, nz);
+    IterLaunch L = iter_launch(ctx, nx, ny, nz, 0, (int)sizeof(T));
     DyrelScal sc{h1, h2, dtau, cX, 1.0 / dx, 1.0 / dy, 1.0 / dz};
     T* cur = X;
     T* nxt = X2;

@@ -145,7 +145,7 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
     float* kx32 = (float*)ht3d_scratch(ctx, SLOT_F32_KX, sizeof(float) * nfx);
     float* ky32 = (float*)ht3d_scratch(ctx, SLOT_F32_KY, sizeof(float) * nfy);
     float* kz32 = (float*)ht3d_scratch(ctx, SLOT_F32_KZ, sizeof(float) * nfz);
-    IterLaunch L = iter_launch(ctx, nx, ny, nz);
+    IterLaunch L = iter_launch(ctx, nx, ny, nz, 0, 4);
     IterLaunch LC = iter_launch(ctx, nx, ny, nz, HT3D_DYREL_ZMARCH);  // layout of the FP64 check kernel
     const long long nparts = std::max<long long>(std::max(L.nblocks, LC.nblocks),
                                                  (long long)((nx + 31) / 32) * ((ny + 7) / 8) * nz);

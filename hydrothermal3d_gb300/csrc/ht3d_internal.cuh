@@ -13,8 +13,12 @@
 // ---------------------------------------------------------------------------
 // Context
 // ---------------------------------------------------------------------------
+// A slot grows by free + malloc, so a pointer taken from a slot is invalid
+// once anything asks the same slot for more bytes: each user below owns its
+// slot for the duration of a call.
 enum ScratchSlot {
-    SLOT_PARTIALS = 0,  // per-block reduction partials (double)
+    SLOT_PARTIALS = 0,  // solver check terms / per-block partials (double)
+    SLOT_REDUCE,        // partials of ht3d_reduce_device (used between solver phases)
     SLOT_RESULT,        // final reduction results (double[64])
     SLOT_X2,            // ping-pong ghosted field
     SLOT_PC,            // Jacobi diagonal / inverse diagonal
@@ -33,7 +37,7 @@ struct ht3d_ctx {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int sync_each_call = 1;
-    int dyrel_variant = HT3D_DYREL_CELL;  // thread layout of the fused DYREL iteration
+    int dyrel_variant = 0;                // thread layout of the fused DYREL iteration (0 = per precision)
     int mixed_refresh = 64;               // FP64 defect-correction cadence of the mixed solver
     int num_sms = 152;
     unsigned long long launches = 0;

@@ -22,7 +22,8 @@ def main():
     ap.add_argument("--kernel", default="dyrel_f32", choices=["dyrel_f32", "dyrel_f64", "weno_f64", "weno_mixed"])
     ap.add_argument("--n", type=int, default=255)
     ap.add_argument("--iters", type=int, default=5)
-    ap.add_argument("--variant", type=int, default=2, help="DYREL thread layout: 1 z-march tiles, 2 one thread per cell")
+    ap.add_argument("--variant", type=int, default=0,
+                    help="DYREL thread layout: 0 per precision, 1 z-march tiles, 2 one thread per cell")
     a = ap.parse_args()
     n = a.n
     stream = torch.cuda.Stream()

@@ -80,6 +80,10 @@ def box(nx, ny, nz, Lx=10e3, Ly=10e3, Lz=5e3, T_bot_C=600.0, T_top_C=20.0, seed=
     wN = np.full((nx + 2, nz + 2), 0.5, order="F")
     lk = lognormal_field((nx + 1, ny + 1, nz + 1), (dx * L, dy * L, dz * L), log10k_mean, log10k_sigma, corr, seed)
     kmul = np.asfortranarray(10.0 ** lk / 5e-16)
+    # impermeable basement: the reference's bottom pressure rule P[ghost] = P[inner]
+    # is an outflow boundary under gravity; zero permeability on the bottom vertex
+    # row makes the bottom face (whose ky averages only that row) no-flow
+    kmul[:, 0, :] = 0.0
     # basal heat flux consistent with the initial gradient and the rock conductivity at the base
     kT_base = 3.1138 - 0.0023 * (Tbot * sc["T"])
     qyS_SI = kT_base * (T_bot_C - T_top_C) / Ly
@@ -96,9 +100,13 @@ def box(nx, ny, nz, Lx=10e3, Ly=10e3, Lz=5e3, T_bot_C=600.0, T_top_C=20.0, seed=
     p.sc_sigma, p.sc_rho, p.sc_C, p.sc_kt = sc["sigma"], sc["rho"], sc["C"], sc["kt"]
     p.it, p.thermal, p.hydro, p.advection, p.dt_constant = 0, 1, 1, 1, 1
     p.weno_variant = weno_variant
+    # relative tolerance only: in the reference's scaled units an absolute norm
+    # of 1e-10 is reached long before convergence (v18 itself uses 1e-18)
     p.thermal_dyrel = abi.DyrelParams.reference(tol=tol, nitmax=nitmax, nitout=nitout,
                                                 norm_scale=sc["rho"] * sc["C"] * sc["T"] / sc["t"])
+    p.thermal_dyrel.tol_abs = 0.0
     p.darcy_dyrel = abi.DyrelParams.reference(tol=tol, nitmax=nitmax, nitout=nitout, norm_scale=sc["rho"] / sc["t"])
+    p.darcy_dyrel.tol_abs = 0.0
     return dict(T=T, P=P, phc=phc, phv=phv, wN=wN, kmul=kmul, params=p)
 
 

@@ -57,9 +57,10 @@ extern "C" {
 #define HT3D_WENO_V2_FIXED 2   /* v2 loop structure with the textbook v5 stencil */
 
 /* tuning keys for ht3d_ctx_set_tuning */
-#define HT3D_TUNE_DYREL_VARIANT 1   /* thread layout of the fused DYREL iteration: */
-#define HT3D_DYREL_ZMARCH 1         /*   32x8 column tiles marching in z            */
-#define HT3D_DYREL_CELL 2           /*   one thread per cell (default)              */
+#define HT3D_TUNE_DYREL_VARIANT 1   /* thread layout of the fused DYREL iteration:   */
+#define HT3D_DYREL_AUTO 0           /*   per precision: z-march FP64, per-cell FP32  */
+#define HT3D_DYREL_ZMARCH 1         /*   32x8 column tiles marching in z              */
+#define HT3D_DYREL_CELL 2           /*   one thread per cell                          */
 #define HT3D_TUNE_MIXED_REFRESH 2   /* mixed form: FP64 defect-correction refresh every N
                                        inner iterations between checks (default 64; 0 = only
                                        at the reference's check iterations)             */

@@ -83,7 +83,7 @@ def test_fp64_solver_is_bitwise_reproducible(ctx, orc, n, variant):
         std = api.dyrel_solve_dimless(ctx, Xd, ht.from_numpy(R), *[ht.from_numpy(a) for a in k], 30.0, *d, types,
                                       vals, prm, Fd, F0d, abi.FP64, n_iter_fixed=40)
     finally:
-        ctx.check(ctx.lib.ht3d_ctx_set_tuning(ctx.ptr, 1, 2))
+        ctx.check(ctx.lib.ht3d_ctx_set_tuning(ctx.ptr, 1, 0))
     assert std.nF_abs == sto.nF_abs and std.lambda_min == sto.lambda_min and std.h1 == sto.h1
     m = no_edges_mask(X.shape)
     np.testing.assert_array_equal(ht.to_numpy(Xd)[m], Xo[m])
