@@ -2,7 +2,7 @@
 import ctypes
 
 OK = 0
-ERR_ARG, ERR_CUDA, ERR_NAN, ERR_DIVERGED, ERR_MAXITER, ERR_TIMEOUT, ERR_NOMEM = 1, 2, 3, 4, 5, 6, 7
+ERR_ARG, ERR_CUDA, ERR_NAN, ERR_DIVERGED, ERR_MAXITER, ERR_TIMEOUT, ERR_NOMEM, ERR_SCRATCH = 1, 2, 3, 4, 5, 6, 7, 8
 FP64, MIXED = 0, 1
 BC_NEUMANN, BC_DIRICHLET, BC_PERIODIC = 0, 1, 2
 WENO_V1, WENO_V2_REF, WENO_V2_FIXED = 0, 1, 2

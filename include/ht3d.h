@@ -41,6 +41,7 @@ extern "C" {
 #define HT3D_ERR_MAXITER 5     /* reserved: the reference does not error at nitmax */
 #define HT3D_ERR_TIMEOUT 6     /* a bounded device wait gave up */
 #define HT3D_ERR_NOMEM 7
+#define HT3D_ERR_SCRATCH 8     /* grid larger than the static scratch of ht3d_dyrel_iterate_noalloc */
 
 /* precision forms */
 #define HT3D_FP64 0            /* plain FP64, reproduces the reference */
@@ -361,6 +362,28 @@ int ht3d_dyrel_iterate_f32(ht3d_ctx* ctx, float* X_ex, const float* R, const flo
                            const float* kz, const float* invPC, float* F0, double cX, double dx, double dy, double dz,
                            const int* bc_type6, const double* bc_val6, double h1, double h2, double dtau, int n_iter,
                            int nx, int ny, int nz);
+
+/* Allocation-free variant of ht3d_dyrel_iterate, for callers that cannot let
+   a library allocate device memory (their allocator owns the device heap, or
+   memory management is frozen while they run).  No reference counterpart: the
+   reference allocates its arrays with @zeros and never needs this.
+   Same arguments as ht3d_dyrel_iterate (PC is the Jacobi diagonal, not its
+   inverse) without a ctx, plus the cudaStream_t to launch on; results are
+   identical to ht3d_dyrel_iterate's.
+   - Scratch: one static device array of 2^20 doubles (8 MiB) in the library,
+     present on every device that loads it until the process exits.  Grids with
+     (nx+2)(ny+2)(nz+2) > 1048576 are rejected with HT3D_ERR_SCRATCH.
+   - Never calls cudaMalloc, cudaFree or any allocating routine.
+   - The first call on a device looks up the array's device address with that
+     device current; make that first call before any stream capture.
+   - Asynchronous: returns after queueing its kernels on `stream`.
+   - All calls share the one array, whose contents persist between calls
+     (nothing is read before it is written); calls that overlap on the GPU,
+     on any stream, race on it. */
+int ht3d_dyrel_iterate_noalloc(double* X_ex, const double* R, const double* kx, const double* ky, const double* kz,
+                               const double* PC, double* F0, double cX, double dx, double dy, double dz,
+                               const int* bc_type6, const double* bc_val6, double h1, double h2, double dtau,
+                               int n_iter, int nx, int ny, int nz, void* stream);
 
 /* One time step of the dimensionless Horton-Rogers-Lapwood model:
    thermal DYREL solve, Darcy DYREL solve, Init_vel!, WENO5 advection and the
