@@ -25,6 +25,16 @@ namespace {
 struct DyrelScal {
     double h1, h2, dtau, cX, _dx, _dy, _dz;
 };
+// The same scalars in the kernel's arithmetic type.  They are converted on
+// the host: on GB300 a double->float conversion runs on the FP64 pipe, and
+// seven of them per thread made the FP32 iteration FP64-bound.
+template <typename T>
+struct DyrelScalT {
+    T h1, h2, dtau, cX, _dx, _dy, _dz;
+    DyrelScalT() = default;
+    explicit DyrelScalT(const DyrelScal& s)
+        : h1((T)s.h1), h2((T)s.h2), dtau((T)s.dtau), cX((T)s.cX), _dx((T)s._dx), _dy((T)s._dy), _dz((T)s._dz) {}
+};
 
 template <typename T>
 struct BC6 {
@@ -46,13 +56,13 @@ __global__ void __launch_bounds__(TX* TY) k_dyrel_iter(const T* __restrict__ Xin
                                                        const T* __restrict__ R, const T* __restrict__ kx,
                                                        const T* __restrict__ ky, const T* __restrict__ kz,
                                                        const T* __restrict__ PCx, T* __restrict__ F0,
-                                                       T* __restrict__ F, DyrelScal s, BC6<T> bc, int nx, int ny,
+                                                       T* __restrict__ F, DyrelScalT<T> s, BC6<T> bc, int nx, int ny,
                                                        int nz, int zchunk, double* __restrict__ partials) {
     const int i = blockIdx.x * TX + threadIdx.x;
     const int j = blockIdx.y * TY + threadIdx.y;
     const int k0 = blockIdx.z * zchunk;
     const int k1 = min(nz, k0 + zchunk);
-    const T h1 = (T)s.h1, h2 = (T)s.h2, dtau = (T)s.dtau, cX = (T)s.cX, _dx = (T)s._dx, _dy = (T)s._dy, _dz = (T)s._dz;
+    const T h1 = s.h1, h2 = s.h2, dtau = s.dtau, cX = s.cX, _dx = s._dx, _dy = s._dy, _dz = s._dz;
     if (i < nx && j < ny && k0 < k1) {
         const int n1 = nx + 2, n2 = ny + 2;
         const long long pl = (long long)n1 * n2;  // ex plane
@@ -122,12 +132,12 @@ __global__ void __launch_bounds__(CX_* CY_* CZ_) k_dyrel_cell(const T* __restric
                                                              const T* __restrict__ R, const T* __restrict__ kx,
                                                              const T* __restrict__ ky, const T* __restrict__ kz,
                                                              const T* __restrict__ PCx, T* __restrict__ F0,
-                                                             T* __restrict__ F, DyrelScal s, BC6<T> bc, int nx, int ny,
+                                                             T* __restrict__ F, DyrelScalT<T> s, BC6<T> bc, int nx, int ny,
                                                              int nz, double* __restrict__ partials) {
     const int i = blockIdx.x * CX_ + threadIdx.x;
     const int j = blockIdx.y * CY_ + threadIdx.y;
     const int k = blockIdx.z * CZ_ + threadIdx.z;
-    const T h1 = (T)s.h1, h2 = (T)s.h2, dtau = (T)s.dtau, cX = (T)s.cX, _dx = (T)s._dx, _dy = (T)s._dy, _dz = (T)s._dz;
+    const T h1 = s.h1, h2 = s.h2, dtau = s.dtau, cX = s.cX, _dx = s._dx, _dy = s._dy, _dz = s._dz;
     if (i < nx && j < ny && k < nz) {
         const int n1 = nx + 2, n2 = ny + 2;
         const int pl = n1 * n2;
@@ -271,11 +281,12 @@ template <typename T, int MODE>
 inline void launch_iter(ht3d_ctx* ctx, const IterLaunch& L, const T* Xin, T* Xout, const T* R, const T* kx,
                         const T* ky, const T* kz, const T* PCx, T* F0, T* F, const DyrelScal& sc, const BC6<T>& bc,
                         int nx, int ny, int nz, double* partials) {
+    const DyrelScalT<T> st(sc);
     if (L.variant == HT3D_DYREL_CELL)
-        HT3D_LAUNCH(ctx, (k_dyrel_cell<T, MODE>), L.grid, L.block, 0, Xin, Xout, R, kx, ky, kz, PCx, F0, F, sc, bc, nx,
+        HT3D_LAUNCH(ctx, (k_dyrel_cell<T, MODE>), L.grid, L.block, 0, Xin, Xout, R, kx, ky, kz, PCx, F0, F, st, bc, nx,
                     ny, nz, partials);
     else
-        HT3D_LAUNCH(ctx, (k_dyrel_iter<T, MODE>), L.grid, L.block, 0, Xin, Xout, R, kx, ky, kz, PCx, F0, F, sc, bc, nx,
+        HT3D_LAUNCH(ctx, (k_dyrel_iter<T, MODE>), L.grid, L.block, 0, Xin, Xout, R, kx, ky, kz, PCx, F0, F, st, bc, nx,
                     ny, nz, L.zchunk, partials);
 }
 

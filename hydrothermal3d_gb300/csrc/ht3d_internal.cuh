@@ -38,7 +38,7 @@ struct ht3d_ctx {
     bool own_stream = false;
     int sync_each_call = 1;
     int dyrel_variant = 0;                // thread layout of the fused DYREL iteration (0 = per precision)
-    int mixed_refresh = 64;               // FP64 defect-correction cadence of the mixed solver
+    int mixed_refresh = 256;              // FP64 defect-correction cadence of the mixed solver
     int num_sms = 152;
     unsigned long long launches = 0;
     std::string last_error;

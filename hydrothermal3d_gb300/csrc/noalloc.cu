@@ -70,7 +70,7 @@ extern "C" int ht3d_dyrel_iterate_noalloc(double* X_ex, const double* R, const d
     const int s = scratch_for_current_device(&scratch);
     if (s != HT3D_OK) return s;
     cudaStream_t st = (cudaStream_t)stream;
-    const DyrelScal sc{h1, h2, dtau, cX, 1.0 / dx, 1.0 / dy, 1.0 / dz};
+    const DyrelScalT<double> sc(DyrelScal{h1, h2, dtau, cX, 1.0 / dx, 1.0 / dy, 1.0 / dz});
     const dim3 blk(CX_, CY_, CZ_), grd((nx + CX_ - 1) / CX_, (ny + CY_ - 1) / CY_, (nz + CZ_ - 1) / CZ_);
     double* cur = X_ex;
     double* nxt = scratch;

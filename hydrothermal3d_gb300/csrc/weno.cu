@@ -9,75 +9,9 @@
 //    rules (no (n+6)^3 buffer, no v1..v5 temporaries), the RK averaging fused
 //    into the second stage.
 #include "ht3d_internal.cuh"
+#include "weno_core.cuh"
 
 namespace {
-
-// ----------------------------------------------------------------- WENO core
-// dFdx_Weno5! body, tools/Weno5_Routines.jl:51-66 (FP64, reference order)
-__device__ __forceinline__ double weno5_ref(double v1, double v2, double v3, double v4, double v5) {
-    const double p1 = v1 / 3.0 - 7.0 / 6.0 * v2 + 11.0 / 6.0 * v3;
-    const double p2 = -v2 / 6.0 + 5.0 / 6.0 * v3 + v4 / 3.0;
-    const double p3 = v3 / 3.0 + 5.0 / 6.0 * v4 - v5 / 6.0;
-    const double maxV = fmax(fmax(fmax(fmax(v1 * v1, v2 * v2), v3 * v3), v4 * v4), v5 * v5);
-    const double e = 1e-99 + 1e-6 * maxV;
-    const double a1 = v1 - 2.0 * v2 + v3, b1 = v1 - 4.0 * v2 + 3.0 * v3;
-    const double a2 = v2 - 2.0 * v3 + v4, b2 = v2 - v4;
-    const double a3 = v3 - 2.0 * v4 + v5, b3 = 3.0 * v3 - 4.0 * v4 + v5;
-    double w1 = 13.0 / 12.0 * (a1 * a1) + 1.0 / 4.0 * (b1 * b1);
-    double w2 = 13.0 / 12.0 * (a2 * a2) + 1.0 / 4.0 * (b2 * b2);
-    double w3 = 13.0 / 12.0 * (a3 * a3) + 1.0 / 4.0 * (b3 * b3);
-    w1 = 0.1 / ((w1 + e) * (w1 + e));
-    w2 = 0.6 / ((w2 + e) * (w2 + e));
-    w3 = 0.3 / ((w3 + e) * (w3 + e));
-    const double w = (w1 + w2 + w3);
-    w1 = w1 / w;
-    w2 = w2 / w;
-    w3 = w3 / w;
-    return w1 * p1 + w2 * p2 + w3 * p3;
-}
-
-// FP32 form for the mixed-precision path.  The reference's epsilon floor
-// 1e-99 underflows in FP32; 1e-18 is the smallest floor whose square stays a
-// normal FP32 number, so a flat field still yields the linear weights.
-__device__ __forceinline__ float weno5_f32(float v1, float v2, float v3, float v4, float v5) {
-    const float p1 = v1 * (1.0f / 3.0f) - (7.0f / 6.0f) * v2 + (11.0f / 6.0f) * v3;
-    const float p2 = -v2 * (1.0f / 6.0f) + (5.0f / 6.0f) * v3 + v4 * (1.0f / 3.0f);
-    const float p3 = v3 * (1.0f / 3.0f) + (5.0f / 6.0f) * v4 - v5 * (1.0f / 6.0f);
-    const float maxV = fmaxf(fmaxf(fmaxf(fmaxf(v1 * v1, v2 * v2), v3 * v3), v4 * v4), v5 * v5);
-    const float e = 1e-18f + 1e-6f * maxV;
-    const float a1 = v1 - 2.0f * v2 + v3, b1 = v1 - 4.0f * v2 + 3.0f * v3;
-    const float a2 = v2 - 2.0f * v3 + v4, b2 = v2 - v4;
-    const float a3 = v3 - 2.0f * v4 + v5, b3 = 3.0f * v3 - 4.0f * v4 + v5;
-    const float s1 = (13.0f / 12.0f) * (a1 * a1) + 0.25f * (b1 * b1) + e;
-    const float s2 = (13.0f / 12.0f) * (a2 * a2) + 0.25f * (b2 * b2) + e;
-    const float s3 = (13.0f / 12.0f) * (a3 * a3) + 0.25f * (b3 * b3) + e;
-    const float w1 = 0.1f / (s1 * s1), w2 = 0.6f / (s2 * s2), w3 = 0.3f / (s3 * s3);
-    const float iw = 1.0f / (w1 + w2 + w3);
-    return (w1 * p1 + w2 * p2 + w3 * p3) * iw;
-}
-
-struct WenoBC {
-    int typeL, typeR;
-    double valL, valR;
-};
-
-// value at position p (-3 <= p <= n+2) along the sweep axis of a line whose
-// inner value at index m is line[m*stride]; ghost rules of
-// Boundaries_*_Weno5! (Neumann mirror, Dirichlet 2v-mirror, periodic wrap).
-__device__ __forceinline__ double line_at(const double* __restrict__ line, long long stride, int p, int n,
-                                          const WenoBC& bc) {
-    if (p < 0) {
-        if (bc.typeL == HT3D_BC_PERIODIC) return line[(long long)(n + p) * stride];
-        const double v = line[(long long)(-1 - p) * stride];
-        return bc.typeL == HT3D_BC_DIRICHLET ? 2 * bc.valL - v : v;
-    }
-    if (p >= n) {
-        if (bc.typeR == HT3D_BC_PERIODIC) return line[(long long)(p - n) * stride];
-        const double v = line[(long long)(2 * n - 1 - p) * stride];
-        return bc.typeR == HT3D_BC_DIRICHLET ? 2 * bc.valR - v : v;
-    }
-    return line[(long long)p * stride];
-}
 
 // One SSP-RK2 stage along AXIS on ghosted (ex) fields.
 //   PREC 0: FP64 reference-order arithmetic (parity form; this translation

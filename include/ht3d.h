@@ -63,7 +63,7 @@ extern "C" {
 #define HT3D_DYREL_ZMARCH 1         /*   32x8 column tiles marching in z              */
 #define HT3D_DYREL_CELL 2           /*   one thread per cell                          */
 #define HT3D_TUNE_MIXED_REFRESH 2   /* mixed form: FP64 defect-correction refresh every N
-                                       inner iterations between checks (default 64; 0 = only
+                                       inner iterations between checks (default 256; 0 = only
                                        at the reference's check iterations)             */
 
 typedef struct ht3d_ctx ht3d_ctx;
@@ -333,6 +333,13 @@ int ht3d_TimeAveraging_v2(ht3d_ctx* ctx, double* Fc_ex, const double* Fold, doub
 int ht3d_weno5_advect(ht3d_ctx* ctx, double* Tc_ex, const double* Vx, const double* Vy, const double* Vz, double dt,
                       double _dx, double _dy, double _dz, const int* bc_type6, const double* bc_val6, int variant,
                       int precision, int nx, int ny, int nz);
+
+/* FP32 storage and arithmetic variant of ht3d_weno5_advect (float fields of the
+   same shapes); the weights' epsilon floor is 1e-18 instead of the reference's
+   1e-99, which underflows in FP32.  For the standalone large-grid sweep. */
+int ht3d_weno5_advect_f32(ht3d_ctx* ctx, float* Tc_ex, const float* Vx, const float* Vy, const float* Vz, double dt,
+                          double _dx, double _dy, double _dz, const int* bc_type6, const double* bc_val6, int variant,
+                          int nx, int ny, int nz);
 
 /* ------------------------------------------------------------------ */
 /* Fused DYREL solver (replaces the loop Dimensional/HydroThermal3D_v18.jl:448-477
