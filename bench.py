@@ -222,6 +222,10 @@ def run_ours(a):
                 api.step_hrl(ctx, Td, Pd, ktd, kfd, *Vd, p, prec)
             torch.cuda.synchronize()
             barrier(ws)
+            # the mixed solver times its FP32 inner-iteration runs on the ctx
+            # stream during the timed steps (the roofline's kernel duration)
+            ctx.set_tuning(abi.TUNE_TIME_INNER, 1 if prec == abi.MIXED else 0)
+            ctx.inner_timing(reset=True)
             l0 = ctx.launches
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             iters, nbytes = [], 0
@@ -236,7 +240,9 @@ def run_ours(a):
                 torch.cuda.synchronize()
             barrier(ws)
             ms = e0.elapsed_time(e1)
-        return dict(ms=ms, bytes=nbytes, iters=iters, launches=ctx.launches - l0, T=Td, P=Pd, params=p)
+            inner = ctx.inner_timing(reset=True)
+            ctx.set_tuning(abi.TUNE_TIME_INNER, 0)
+        return dict(ms=ms, bytes=nbytes, iters=iters, launches=ctx.launches - l0, T=Td, P=Pd, params=p, inner=inner)
 
     sampler = ClockSampler(dev)
     mixed = run_form(abi.MIXED, a.steps, a.warmup, sampler)
@@ -268,8 +274,9 @@ def run_ours(a):
         out["mixed_error_vs_fp64_gpu"].update(one_step_error(ctx, stream, a, fp64, ktd, kfd, Vd))
     out["clocks"] = sampler.summary()
 
-    # --- roofline of the dominant kernel: the FP32 fused DYREL iteration
-    out["roofline"] = roofline(ctx, stream, n)
+    # --- roofline of the dominant kernel: the FP32 inner DYREL iteration of
+    # the mixed form, timed live inside the timed steps above
+    out["roofline"] = roofline(ctx, stream, n, mixed["inner"], mixed["ms"])
 
     # --- end to end through the public API with host buffers (mixed form)
     out["e2e"] = e2e(ctx, stream, a, ktd, kfd, Vd)
@@ -320,60 +327,41 @@ class _Null:
         return False
 
 
-def roofline(ctx, stream, n, iters=40):
+def roofline(ctx, stream, n, inner, step_ms, iters=20):
     import torch
     import hydrothermal3d_gb300 as ht
     from hydrothermal3d_gb300 import abi, hrl
-    N = n ** 3
-    f32 = torch.float32
-    X = ht.zeros(n + 2, n + 2, n + 2, dtype=f32)
-    X.uniform_(0, 1)
-    R = ht.zeros(n, n, n, dtype=f32)
-    R.uniform_(-1, 1)
-    k = [ht.ones(n + 1, n, n, dtype=f32), ht.ones(n, n + 1, n, dtype=f32), ht.ones(n, n, n + 1, dtype=f32)]
-    iPC = ht.ones(n, n, n, dtype=f32) * (1.0 / (6 * n * n))
-    F0 = ht.zeros(n, n, n, dtype=f32)
-    bt, bv = abi.int6(0, 0, 1, 1, 0, 0), abi.dbl6(0, 0, 1, 0, 0, 0)
-    d = 1.0 / n
-    args = lambda m: (X.data_ptr(), R.data_ptr(), k[0].data_ptr(), k[1].data_ptr(), k[2].data_ptr(), iPC.data_ptr(),
-                      F0.data_ptr(), 0.0, d, d, d, bt, bv, 0.99, 0.05, 0.01, m, n, n, n)
-    torch.cuda.synchronize()
-    ctx.call("ht3d_dyrel_iterate_f32", *args(4))
-    ctx.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    ctx.call("ht3d_dyrel_iterate_f32", *args(iters))
-    e1.record(stream)
-    torch.cuda.synchronize()
-    t = e0.elapsed_time(e1) / 1e3 / iters
+    inner_ms, inner_launches = inner
+    t = inner_ms / 1e3 / max(1, inner_launches)
     alg = hrl.bytes_per_iteration(n, n, n, 4)
     peak = measured_peak()
     achieved = alg / t / 1e9
-    res = {"kernel": "k_dyrel_iter<float,PLAIN> (mixed-form pseudo-iteration)", "bound": "hbm",
+    res = {"kernel": "k_mixed_inner (FP32 pseudo-iteration of the mixed form)", "bound": "hbm",
            "achieved": achieved, "peak": peak[0], "unit": "GB/s", "frac": achieved / peak[0], "peak_source": peak[1],
-           "traffic": profile_traffic("dyrel_iter_f32"), "us_per_launch": t * 1e6,
-           "alg_bytes_per_launch": alg}
-    # FP64 form's kernel for comparison (FP64-ALU bound on GB300)
-    X64 = X.double()
-    R64, k64, iPC64, F064 = R.double(), [a.double() for a in k], iPC.double(), F0.double()
-    X64c = ht.zeros(n + 2, n + 2, n + 2)
-    X64c.copy_(X64)
-    R64c = ht.zeros(n, n, n); R64c.copy_(R64)
-    k64c = [ht.zeros(*a.shape) for a in k64]
-    for a, b in zip(k64c, k64):
-        a.copy_(b)
-    iPCc = ht.zeros(n, n, n); iPCc.copy_(iPC64)
+           "traffic": profile_traffic("mixed_inner_f32"), "us_per_launch": t * 1e6,
+           "alg_bytes_per_launch": alg, "launches_timed": inner_launches,
+           "share_of_timed_region": inner_ms / step_ms if step_ms else None,
+           "timing": "CUDA events on the ctx stream around every run of consecutive inner launches inside the "
+                     "timed steps (HT3D_TUNE_TIME_INNER)"}
+    X64c = ht.zeros(n + 2, n + 2, n + 2).uniform_(0, 1)
+    R64c = ht.zeros(n, n, n).uniform_(-1, 1)
+    k64c = [ht.ones(n + 1, n, n), ht.ones(n, n + 1, n), ht.ones(n, n, n + 1)]
+    iPCc = ht.ones(n, n, n) * (6.0 * n * n)
     F0c = ht.zeros(n, n, n)
+    bt, bv = abi.int6(0, 0, 1, 1, 0, 0), abi.dbl6(0, 0, 1, 0, 0, 0)
+    d = 1.0 / n
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # FP64 form's kernel for comparison (FP64-ALU bound on GB300)
     a64 = lambda m: (X64c.data_ptr(), R64c.data_ptr(), k64c[0].data_ptr(), k64c[1].data_ptr(), k64c[2].data_ptr(),
                      iPCc.data_ptr(), F0c.data_ptr(), 0.0, d, d, d, bt, bv, 0.99, 0.05, 0.01, m, n, n, n)
     torch.cuda.synchronize()
     ctx.call("ht3d_dyrel_iterate", *a64(2))
     ctx.synchronize()
     e0.record(stream)
-    ctx.call("ht3d_dyrel_iterate", *a64(iters // 2))
+    ctx.call("ht3d_dyrel_iterate", *a64(iters))
     e1.record(stream)
     torch.cuda.synchronize()
-    t64 = e0.elapsed_time(e1) / 1e3 / (iters // 2)
+    t64 = e0.elapsed_time(e1) / 1e3 / iters
     alg64 = hrl.bytes_per_iteration(n, n, n, 8)
     res["fp64_kernel"] = {"kernel": "k_dyrel_iter<double,PLAIN>", "us_per_launch": t64 * 1e6,
                           "achieved_GBs": alg64 / t64 / 1e9, "frac_hbm": alg64 / t64 / 1e9 / peak[0],

@@ -9,6 +9,7 @@ WENO_V1, WENO_V2_REF, WENO_V2_FIXED = 0, 1, 2
 RED_SUM, RED_SUM_ABS, RED_MAX, RED_MIN, RED_MAX_ABS = 0, 1, 2, 3, 4
 TUNE_DYREL_VARIANT = 1
 TUNE_MIXED_REFRESH = 2
+TUNE_TIME_INNER = 3
 DYREL_ZMARCH, DYREL_CELL = 1, 2
 
 

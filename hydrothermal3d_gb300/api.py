@@ -56,6 +56,15 @@ class Context:
     def launches(self):
         return int(self.lib.ht3d_ctx_launch_count(self.ptr))
 
+    def set_tuning(self, key, value):
+        self.check(self.lib.ht3d_ctx_set_tuning(self.ptr, int(key), int(value)))
+
+    def inner_timing(self, reset=False):
+        """(ms, launches) of the mixed solver's event-timed inner-iteration runs."""
+        ms, nl = ctypes.c_double(), ctypes.c_ulonglong()
+        self.check(self.lib.ht3d_ctx_inner_timing(self.ptr, ctypes.byref(ms), ctypes.byref(nl), int(bool(reset))))
+        return ms.value, nl.value
+
     def close(self):
         if self.ptr:
             self.lib.ht3d_ctx_destroy(self.ptr)

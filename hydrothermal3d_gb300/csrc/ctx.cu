@@ -121,6 +121,7 @@ int ht3d_ctx_destroy(ht3d_ctx* ctx) {
     for (int s = 0; s < SLOT_COUNT; ++s)
         if (ctx->slot_ptr[s]) cudaFree(ctx->slot_ptr[s]);
     if (ctx->h_result) cudaFreeHost(ctx->h_result);
+    for (cudaEvent_t ev : ctx->events) cudaEventDestroy(ev);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return HT3D_OK;
@@ -160,7 +161,23 @@ int ht3d_ctx_set_tuning(ht3d_ctx* ctx, int key, int value) {
         ctx->mixed_refresh = value;
         return HT3D_OK;
     }
+    if (key == HT3D_TUNE_TIME_INNER) {
+        if (value != 0 && value != 1) return HT3D_ERR_ARG;
+        ctx->time_inner = value;
+        return HT3D_OK;
+    }
     return HT3D_ERR_ARG;
+}
+
+int ht3d_ctx_inner_timing(ht3d_ctx* ctx, double* ms, unsigned long long* launches, int reset) {
+    if (!ctx) return HT3D_ERR_ARG;
+    if (ms) *ms = ctx->inner_ms;
+    if (launches) *launches = ctx->inner_launches;
+    if (reset) {
+        ctx->inner_ms = 0.0;
+        ctx->inner_launches = 0;
+    }
+    return HT3D_OK;
 }
 
 int ht3d_ctx_synchronize(ht3d_ctx* ctx) {

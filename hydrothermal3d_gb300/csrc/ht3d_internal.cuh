@@ -39,6 +39,10 @@ struct ht3d_ctx {
     int sync_each_call = 1;
     int dyrel_variant = 0;                // thread layout of the fused DYREL iteration (0 = per precision)
     int mixed_refresh = 256;              // FP64 defect-correction cadence of the mixed solver
+    int time_inner = 0;                   // time the mixed solver's inner-iteration runs
+    std::vector<cudaEvent_t> events;      // event pool of the inner-iteration timer
+    double inner_ms = 0.0;                // accumulated device time of the timed runs
+    unsigned long long inner_launches = 0;  // inner-iteration launches inside them
     int num_sms = 152;
     unsigned long long launches = 0;
     std::string last_error;

@@ -4,8 +4,11 @@
   ncu --set full --clock-control none -k regex:k_dyrel_iter -s 2 -c 1 -o out \\
       python -m hydrothermal3d_gb300.profile_kernels --kernel dyrel_f32 --n 255 --iters 5
 
-Kernels: dyrel_f32 (mixed-form pseudo-iteration), dyrel_f64 (plain FP64
-pseudo-iteration), weno_f64 / weno_mixed (one fused WENO5 advection).
+Kernels: dyrel_f32 (FP32 pseudo-iteration on the reference layout),
+dyrel_f64 (plain FP64 pseudo-iteration), mixed_solve (a mixed-form DYREL
+solve of --iters pseudo-iterations: two FP64 checks, then the padded FP32
+inner kernel k_mixed_inner), weno_f64 / weno_mixed (one fused WENO5
+advection).
 Prints the average time per launch measured with CUDA events.
 """
 import argparse
@@ -19,7 +22,7 @@ from hydrothermal3d_gb300 import abi, hrl
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--kernel", default="dyrel_f32", choices=["dyrel_f32", "dyrel_f64", "weno_f64", "weno_mixed"])
+    ap.add_argument("--kernel", default="dyrel_f32", choices=["dyrel_f32", "dyrel_f64", "mixed_solve", "weno_f64", "weno_mixed"])
     ap.add_argument("--n", type=int, default=255)
     ap.add_argument("--iters", type=int, default=5)
     ap.add_argument("--variant", type=int, default=0,
@@ -54,6 +57,23 @@ def main():
         s = 4 if a.kernel == "dyrel_f32" else 8
         alg = hrl.bytes_per_iteration(n, n, n, s)
         print(json.dumps({"kernel": a.kernel, "variant": a.variant, "n": n, "us_per_launch": t * 1e6, "alg_GBs": alg / t / 1e9}))
+    elif a.kernel == "mixed_solve":
+        from hydrothermal3d_gb300 import api
+        X = ht.zeros(n + 2, n + 2, n + 2).uniform_(0, 1)
+        R = ht.zeros(n, n, n).uniform_(-1, 1)
+        k = [ht.ones(n + 1, n, n), ht.ones(n, n + 1, n), ht.ones(n, n, n + 1)]
+        F, F0 = ht.zeros(n, n, n), ht.zeros(n, n, n)
+        prm = abi.DyrelParams.reference()
+        ctx.set_tuning(abi.TUNE_TIME_INNER, 1)
+        with torch.cuda.stream(stream):
+            api.dyrel_solve_dimless(ctx, X, R, *k, float(n * n), d, d, d, (0, 0, 1, 1, 0, 0), (0, 0, 1, 0, 0, 0), prm,
+                                    F, F0, abi.MIXED, n_iter_fixed=a.iters)
+        torch.cuda.synchronize()
+        ms, nl = ctx.inner_timing(reset=True)
+        t = ms / 1e3 / max(1, nl)
+        alg = hrl.bytes_per_iteration(n, n, n, 4)
+        print(json.dumps({"kernel": "k_mixed_inner", "n": n, "inner_launches": nl, "us_per_launch": t * 1e6,
+                          "alg_GBs": alg / t / 1e9}))
     else:
         prec = abi.FP64 if a.kernel == "weno_f64" else abi.MIXED
         T = ht.zeros(n + 2, n + 2, n + 2).uniform_(0, 1)

@@ -65,6 +65,9 @@ extern "C" {
 #define HT3D_TUNE_MIXED_REFRESH 2   /* mixed form: FP64 defect-correction refresh every N
                                        inner iterations between checks (default 256; 0 = only
                                        at the reference's check iterations)             */
+#define HT3D_TUNE_TIME_INNER 3      /* 1: the mixed solver brackets every run of consecutive
+                                       FP32 inner-iteration launches with CUDA events on the
+                                       ctx stream (read back by ht3d_ctx_inner_timing)    */
 
 typedef struct ht3d_ctx ht3d_ctx;
 
@@ -138,6 +141,9 @@ int ht3d_ctx_synchronize(ht3d_ctx* ctx);
 int ht3d_ctx_set_tuning(ht3d_ctx* ctx, int key, int value);
 /* number of CUDA kernels this ctx has launched (monotonic) */
 unsigned long long ht3d_ctx_launch_count(const ht3d_ctx* ctx);
+/* device time (ms) and launch count of the mixed solver's timed inner-iteration
+   runs since the last reset (HT3D_TUNE_TIME_INNER); reset != 0 clears them */
+int ht3d_ctx_inner_timing(ht3d_ctx* ctx, double* ms, unsigned long long* launches, int reset);
 const char* ht3d_ctx_last_error(const ht3d_ctx* ctx);
 /* sizes of the parameter structs, for binding checks */
 int ht3d_sizeof_dyrel_params(void);

@@ -190,3 +190,46 @@ def test_step_hrl_mixed_error_vs_oracle(ctx, orc):
         # the same dt sequence keeps the comparison meaningful
         p_d.dt = p_o.dt
     assert rel_err(ht.to_numpy(Td)[inner], T[inner]) <= 1e-6
+
+
+@pytest.mark.parametrize("n", [(1, 1, 1), (3, 2, 2), (4, 5, 3), (31, 7, 5), (36, 5, 4), (127, 3, 2), (129, 6, 3)])
+@pytest.mark.parametrize("bc", ["thermal", "mixedbc"])
+@pytest.mark.parametrize("niter", [40, 32, 37])
+def test_mixed_fixed_iterations_track_fp64(ctx, orc, n, bc, niter):
+    """The mixed form's padded FP32 inner kernel (4 cells per thread, warp
+    shuffles across quads, scalar loads at warp and row edges) follows the
+    FP64 iteration: the update X - X0 after 32-40 pseudo-iterations matches the
+    oracle's to FP32 accuracy, and the face ghosts hold the BC of the state
+    before the last iteration like the reference's.  Sizes cover nx < 4,
+    nx % 4 == 0, rows that end inside a warp, nx + 1 = 128 and rows longer
+    than one warp; the last iteration is a check (40), an FP64 refresh (32)
+    or an FP32 inner iteration (37)."""
+    nx, ny, nz = n
+    X, R, k = problem(n, seed=31)
+    types, vals = BCS[bc]
+    prm = abi.DyrelParams.reference(nitout=10)
+    d = (1.0 / nx, 0.8 / ny, 1.1 / nz)
+    Xo, Fo, F0o = X.copy(order="F"), orc.zeros(nx, ny, nz), orc.zeros(nx, ny, nz)
+    so, sto = orc.dyrel_solve_dimless(Xo, R, *k, 40.0, *d, types, vals, prm, Fo, F0o, n_iter_fixed=niter)
+    ctx.set_tuning(abi.TUNE_MIXED_REFRESH, 8)
+    ctx.set_tuning(abi.TUNE_TIME_INNER, 1)
+    ctx.inner_timing(reset=True)
+    try:
+        Xd, Fd, F0d = ht.from_numpy(X), ht.zeros(nx, ny, nz), ht.zeros(nx, ny, nz)
+        std = api.dyrel_solve_dimless(ctx, Xd, ht.from_numpy(R), *[ht.from_numpy(a) for a in k], 40.0, *d, types,
+                                      vals, prm, Fd, F0d, abi.MIXED, n_iter_fixed=niter)
+        ms, launches = ctx.inner_timing(reset=True)
+    finally:
+        ctx.set_tuning(abi.TUNE_MIXED_REFRESH, 256)
+        ctx.set_tuning(abi.TUNE_TIME_INNER, 0)
+    assert so == 0 and std.status == 0 and std.iters == niter and std.checks == sto.checks
+    # checks at 1, 2 and every 10th iteration, FP64 refreshes at every other 8th
+    fp64_iters = [it for it in range(1, niter + 1) if it <= 2 or it % 10 == 0 or it % 8 == 0]
+    assert launches == niter - len(fp64_iters) and ms > 0.0
+    m = no_edges_mask(X.shape)
+    inner = (slice(1, -1),) * 3
+    du_ref, du = (Xo - X)[inner], (ht.to_numpy(Xd) - X)[inner]
+    assert rel_err(du, du_ref) <= 1e-4
+    assert rel_err(ht.to_numpy(Xd), Xo, m) <= 1e-6
+    assert rel_err(ht.to_numpy(F0d), F0o) <= 1e-4
+    assert rel_err(ht.to_numpy(Fd), Fo) <= 1e-3
