@@ -10,6 +10,8 @@ RED_SUM, RED_SUM_ABS, RED_MAX, RED_MIN, RED_MAX_ABS = 0, 1, 2, 3, 4
 TUNE_DYREL_VARIANT = 1
 TUNE_MIXED_REFRESH = 2
 TUNE_TIME_INNER = 3
+TUNE_ENS_BLOCK = 4
+TUNE_ENS_GRAPH = 5
 DYREL_ZMARCH, DYREL_CELL = 1, 2
 
 
@@ -80,6 +82,27 @@ class HrlParams(ctypes.Structure):
         ("dt_fact", ctypes.c_double),
         ("thermal", DyrelParams),
         ("darcy", DyrelParams),
+        ("dt_max", ctypes.c_double),
+    ]
+
+
+class Instance(ctypes.Structure):
+    """ht3d_instance: one member of an ensemble (the arguments of one ht3d_step_hrl)."""
+    _fields_ = [
+        ("Tc_ex", ctypes.c_void_p),
+        ("Pc_ex", ctypes.c_void_p),
+        ("ktv", ctypes.c_void_p),
+        ("kfv", ctypes.c_void_p),
+        ("Vx", ctypes.c_void_p),
+        ("Vy", ctypes.c_void_p),
+        ("Vz", ctypes.c_void_p),
+        ("params", ctypes.POINTER(HrlParams)),
+        ("st_thermal", ctypes.POINTER(DyrelStats)),
+        ("st_darcy", ctypes.POINTER(DyrelStats)),
+        ("nx", ctypes.c_int),
+        ("ny", ctypes.c_int),
+        ("nz", ctypes.c_int),
+        ("status", ctypes.c_int),
     ]
 
 

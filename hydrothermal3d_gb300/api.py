@@ -398,6 +398,37 @@ def step_hrl(ctx, Tc_ex, Pc_ex, ktv, kfv, Vx, Vy, Vz, params, precision=abi.FP64
     return st_t, st_d
 
 
+class Member:
+    """One ensemble member: device fields (torch, column-major FP64) and its
+    host HrlParams; step statistics land in st_thermal / st_darcy."""
+
+    def __init__(self, Tc_ex, Pc_ex, ktv, kfv, Vx, Vy, Vz, params):
+        self.Tc_ex, self.Pc_ex, self.ktv, self.kfv = Tc_ex, Pc_ex, ktv, kfv
+        self.Vx, self.Vy, self.Vz = Vx, Vy, Vz
+        self.params = params
+        self.st_thermal, self.st_darcy = abi.DyrelStats(), abi.DyrelStats()
+        self.status = abi.OK
+
+
+def ensemble_step(ctx, members, precision=abi.MIXED):
+    """One time step of every member (ht3d_ensemble_step); returns the statuses.
+    Raises on the first failing member like step_hrl does."""
+    arr = (abi.Instance * len(members))()
+    for rec, m in zip(arr, members):
+        nx, ny, nz = _cells_ex(m.Tc_ex, "Tc_ex"); S = _shapes(nx, ny, nz)
+        rec.Tc_ex, rec.Pc_ex = _ptr(m.Tc_ex, S["ex"], "Tc_ex"), _ptr(m.Pc_ex, S["ex"], "Pc_ex")
+        rec.ktv, rec.kfv = _ptr(m.ktv, S["v"], "ktv"), _ptr(m.kfv, S["v"], "kfv")
+        rec.Vx, rec.Vy, rec.Vz = _ptr(m.Vx, S["fx"], "Vx"), _ptr(m.Vy, S["fy"], "Vy"), _ptr(m.Vz, S["fz"], "Vz")
+        rec.params = ctypes.pointer(m.params)
+        rec.st_thermal, rec.st_darcy = ctypes.pointer(m.st_thermal), ctypes.pointer(m.st_darcy)
+        rec.nx, rec.ny, rec.nz = nx, ny, nz
+    st = ctx.lib.ht3d_ensemble_step(ctx.ptr, arr, len(members), precision)
+    for rec, m in zip(arr, members):
+        m.status = rec.status
+    ctx.check(st)
+    return [m.status for m in members]
+
+
 # ------------------------------------------------------ dimensional kernels
 def ComputeThermalConductivity(ctx, ktv, Tce, phv, phi0, scale_kt, scale_T):
     nx, ny, nz = _cells_ex(Tce, "Tce"); S = _shapes(nx, ny, nz)

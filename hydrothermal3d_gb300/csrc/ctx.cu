@@ -122,6 +122,10 @@ int ht3d_ctx_destroy(ht3d_ctx* ctx) {
         if (ctx->slot_ptr[s]) cudaFree(ctx->slot_ptr[s]);
     if (ctx->h_result) cudaFreeHost(ctx->h_result);
     for (cudaEvent_t ev : ctx->events) cudaEventDestroy(ev);
+    for (cudaEvent_t ev : ctx->tune_events) cudaEventDestroy(ev);
+    for (cudaGraphExec_t g : ctx->ens_graph)
+        if (g) cudaGraphExecDestroy(g);
+    if (ctx->h_ens) cudaFreeHost(ctx->h_ens);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return HT3D_OK;
@@ -161,6 +165,16 @@ int ht3d_ctx_set_tuning(ht3d_ctx* ctx, int key, int value) {
         ctx->mixed_refresh = value;
         return HT3D_OK;
     }
+    if (key == HT3D_TUNE_ENS_BLOCK) {
+        if (value != 0 && value != 64 && value != 128 && value != 256) return HT3D_ERR_ARG;
+        ctx->ens_block = value;
+        return HT3D_OK;
+    }
+    if (key == HT3D_TUNE_ENS_GRAPH) {
+        if (value != 0 && value != 1) return HT3D_ERR_ARG;
+        ctx->ens_graphs = value;
+        return HT3D_OK;
+    }
     if (key == HT3D_TUNE_TIME_INNER) {
         if (value != 0 && value != 1) return HT3D_ERR_ARG;
         ctx->time_inner = value;
@@ -193,6 +207,7 @@ const char* ht3d_ctx_last_error(const ht3d_ctx* ctx) { return ctx ? ctx->last_er
 int ht3d_sizeof_dyrel_params(void) { return (int)sizeof(ht3d_dyrel_params); }
 int ht3d_sizeof_dyrel_stats(void) { return (int)sizeof(ht3d_dyrel_stats); }
 int ht3d_sizeof_hrl_params(void) { return (int)sizeof(ht3d_hrl_params); }
+int ht3d_sizeof_instance(void) { return (int)sizeof(ht3d_instance); }
 
 int ht3d_reduce(ht3d_ctx* ctx, const double* a, long long n, int op, double* out) {
     return ht3d_guard(ctx, [&]() {

@@ -1,5 +1,6 @@
 // Mixed-precision DYREL solver (FP32 inner iterations, FP64 defect correction).
 #include "dyrel_common.cuh"
+#include "ensemble_internal.cuh"
 
 // ---------------------------------------------------------------------------
 // Mixed-precision DYREL.
@@ -66,27 +67,28 @@ __device__ __forceinline__ float c4(const float4& v, int m) {
     return m == 0 ? v.x : (m == 1 ? v.y : (m == 2 ? v.z : v.w));
 }
 
-// FP32 inner iteration of the mixed solver on the padded layout.  Thread t
-// of plane k owns quad q = t % nq (cells 4q..4q+3) of row j = t / nq and
-// moves every field with 16-byte loads; the x-neighbours across the quad
-// edges come from the adjacent lanes (same row) by warp shuffles, or from a
-// scalar load at a warp edge.  The Jacobi diagonal (the Gershgorin D of the
-// operator, sum of k/dx^2 over the six faces + cX) is recomputed from the
-// face conductivities already in registers instead of being streamed.
+// FP32 inner iteration of the mixed solver on the padded layout, for the
+// quad of cells 4q..4q+3 of row j, plane k (t = q + nq*j is the thread's
+// position in the plane).  Every field moves with 16-byte loads; the
+// x-neighbours across the quad edges come from the adjacent lanes (same
+// row) by warp shuffles, or from a scalar load at a warp edge.  The Jacobi
+// diagonal (the Gershgorin D of the operator, sum of k/dx^2 over the six
+// faces + cX) is recomputed from the face conductivities already in
+// registers instead of being streamed.
 //     F = (Rin + cX D + div q(D)) / diag ;  F0 = h1 F0 + h2 F ;  D -= dtau F0
+// All 32 lanes of the warp must call it.  Lanes past the grid (j >= ny, or
+// live == false) take part with in-bounds loads and store nothing.
 template <bool STOREF>
-__global__ void __launch_bounds__(256) k_mixed_inner(const float* __restrict__ Din, float* __restrict__ Dout,
-                                                     const float* __restrict__ Rin, const float* __restrict__ kx,
-                                                     const float* __restrict__ ky, const float* __restrict__ kz,
-                                                     float* __restrict__ F0, float* __restrict__ F,
-                                                     DyrelScalT<float> s, BC6<float> bc, Pad p) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int k = blockIdx.y;
-    const int lane = threadIdx.x & 31;
+__device__ __forceinline__ void mixed_quad(const float* __restrict__ Din, float* __restrict__ Dout,
+                                           const float* __restrict__ Rin, const float* __restrict__ kx,
+                                           const float* __restrict__ ky, const float* __restrict__ kz,
+                                           float* __restrict__ F0, float* __restrict__ F, const DyrelScalT<float>& s,
+                                           const BC6<float>& bc, const Pad& p, int t, int k, int lane,
+                                           bool live = true) {
     const int q = t % p.nq;
     int j = t / p.nq;
-    const bool act = j < p.ny;
-    if (!act) j = p.ny - 1;  // stays in the shuffles, loads in-bounds data, stores nothing
+    const bool act = live && j < p.ny;
+    if (j >= p.ny) j = p.ny - 1;
     const int i0 = 4 * q;
     const long long base = i0 + (long long)p.PX * j + p.plane * k;
     const float4 d = *reinterpret_cast<const float4*>(Din + base);
@@ -145,6 +147,68 @@ __global__ void __launch_bounds__(256) k_mixed_inner(const float* __restrict__ D
     *reinterpret_cast<float4*>(F0 + base) = make_float4(outF0[0], outF0[1], outF0[2], outF0[3]);
     *reinterpret_cast<float4*>(Dout + base) = make_float4(outD[0], outD[1], outD[2], outD[3]);
     if (STOREF) *reinterpret_cast<float4*>(F + base) = make_float4(outF[0], outF[1], outF[2], outF[3]);
+}
+
+// One instance: thread t of plane k = blockIdx.y handles quad t of the plane.
+template <bool STOREF>
+__global__ void __launch_bounds__(256, 4) k_mixed_inner(const float* __restrict__ Din, float* __restrict__ Dout,
+                                                        const float* __restrict__ Rin, const float* __restrict__ kx,
+                                                        const float* __restrict__ ky, const float* __restrict__ kz,
+                                                        float* __restrict__ F0, float* __restrict__ F,
+                                                        DyrelScalT<float> s, BC6<float> bc, Pad p) {
+    mixed_quad<STOREF>(Din, Dout, Rin, kx, ky, kz, F0, F, s, bc, p, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y,
+                       threadIdx.x & 31);
+}
+
+// ---------------------------------------------------------------------------
+// Batched inner iteration over an ensemble of independent instances.  One
+// launch covers up to kEnsMaxPerLaunch members: the concatenation of their
+// grids: BS quads per block over each member's (quad, row, plane) range.
+// The members' records travel by value in the kernel parameters (constant bank), so a
+// block finds its member and fields without a dependent global load before
+// its first field load.
+// ---------------------------------------------------------------------------
+struct EnsInner {
+    float* D[2];  // correction ping-pong: read D[parity], write D[parity ^ 1]
+    const float* Rin;
+    float* F0;
+    float* F;
+    const float* kx;
+    const float* ky;
+    const float* kz;
+    Pad P;
+    DyrelScalT<float> s;
+    BC6<float> bc;
+};
+constexpr int kEnsMaxPerLaunch = 120;
+struct EnsLaunch {
+    int n;                                // members in this launch
+    int nblk;                             // blocks of this launch
+    int block0[kEnsMaxPerLaunch + 1];     // first block of each member (block0[n] = nblk)
+    int quads[kEnsMaxPerLaunch];          // quads per plane (nq * ny) of each member
+    EnsInner rec[kEnsMaxPerLaunch];
+};
+static_assert(sizeof(EnsLaunch) <= 32000, "batched launch parameters exceed the 32 KB kernel parameter space");
+
+template <bool STOREF, int BS>
+__global__ void __launch_bounds__(BS) k_ens_inner(const __grid_constant__ EnsLaunch L, int parity) {
+    // member of this block: binary search of the block offsets
+    int lo = 0, hi = L.n;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if ((int)blockIdx.x >= L.block0[mid]) lo = mid;
+        else hi = mid;
+    }
+    const EnsInner& e = L.rec[lo];
+    // the member's quads in (quad, row, plane) order, BS per block across planes
+    const long long tg = (long long)(blockIdx.x - L.block0[lo]) * BS + threadIdx.x;
+    const int pq = L.quads[lo];  // quads per plane
+    int k = (int)(tg / pq);
+    const int t = (int)(tg - (long long)k * pq);
+    const bool live = k < e.P.nz;
+    if (!live) k = e.P.nz - 1;
+    mixed_quad<STOREF>(e.D[parity], e.D[parity ^ 1], e.Rin, e.kx, e.ky, e.kz, e.F0, e.F, e.s, e.bc, e.P, t, k,
+                       threadIdx.x & 31, live);
 }
 
 // FP64 check iteration of the mixed solver (see above).  FP64 fields in the
@@ -420,6 +484,438 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
         st->lambda_max = S.lmax; st->h1 = S.h1; st->h2 = S.h2; st->dtau = S.dtau;
     }
     return status;
+}
+
+
+// ---------------------------------------------------------------------------
+// Batched mixed solve (see ensemble_internal.cuh).  The schedule, the
+// kernels and the reductions of every instance are those of
+// ht3d_dyrel_solve_mixed; only the FP32 inner iterations of all instances
+// share one launch per group of kEnsMaxPerLaunch members (or one CUDA graph
+// of kEnsGraphIters iterations).
+// ---------------------------------------------------------------------------
+namespace {
+
+struct Carve {
+    char* base;
+    size_t off = 0;
+    template <typename T>
+    T* take(size_t count) {
+        off = (off + 255) & ~(size_t)255;
+        T* p = base ? reinterpret_cast<T*>(base + off) : nullptr;
+        off += sizeof(T) * (count ? count : 1);
+        return p;
+    }
+};
+
+constexpr int kEnsBS[3] = {64, 128, 256};
+constexpr int kEnsGraphIters = 16;
+constexpr int kEnsTuneRounds = 2;  // timed launches per block size
+
+template <bool STOREF>
+void ens_launch_raw(cudaStream_t st, int cfg, const EnsLaunch& L, int parity) {
+    const unsigned g = (unsigned)L.nblk;
+    if (cfg == 0) k_ens_inner<STOREF, 64><<<g, 64, 0, st>>>(L, parity);
+    else if (cfg == 1) k_ens_inner<STOREF, 128><<<g, 128, 0, st>>>(L, parity);
+    else k_ens_inner<STOREF, 256><<<g, 256, 0, st>>>(L, parity);
+}
+
+template <bool STOREF>
+int ens_launch_all(cudaStream_t st, int cfg, const std::vector<EnsLaunch>& groups, int parity) {
+    for (const EnsLaunch& L : groups) ens_launch_raw<STOREF>(st, cfg, L, parity);
+    return (int)groups.size();
+}
+
+struct EnsHost {
+    Pad P;
+    IterLaunch LC;
+    double* invPC;
+    double* X2;
+    float* f32[8];  // Da, Db, F0, F, Rin, kx, ky, kz
+    double* xcur;
+    double* xnxt;
+    DyrelState S;
+    DyrelScal sc;
+    BC6<double> bc;
+    BC6<float> bch;
+    bool used, active, last_fp64;
+    int it_done, checks, converged, status;
+    double nF_abs, nF_rel, nF_ini;
+};
+
+unsigned long long mix_sig(unsigned long long h, unsigned long long v) {
+    return (h ^ v) * 0x100000001b3ULL + 0x9e3779b97f4a7c15ULL;
+}
+
+// Captures the two graphs (windows starting on parity 0 and 1) of the
+// current launch groups; false when the stream cannot be captured.
+bool ens_capture(ht3d_ctx* ctx, unsigned long long sig, int cfg, const std::vector<EnsLaunch>& groups) {
+    if (ctx->ens_graph_sig == sig && ctx->ens_graph[0] && ctx->ens_graph[1]) return true;
+    for (auto& g : ctx->ens_graph)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+    ctx->ens_graph_sig = 0;
+    for (int p = 0; p < 2; ++p) {
+        if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        for (int g = 0; g < kEnsGraphIters; ++g) ens_launch_all<false>(ctx->stream, cfg, groups, (p + g) & 1);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+        if (e != cudaSuccess || !graph) {
+            cudaGetLastError();
+            return false;
+        }
+        const cudaError_t ei = cudaGraphInstantiate(&ctx->ens_graph[p], graph, 0);
+        cudaGraphDestroy(graph);
+        if (ei != cudaSuccess) {
+            cudaGetLastError();
+            ctx->ens_graph[p] = nullptr;
+            return false;
+        }
+    }
+    ctx->ens_graph_sig = sig;
+    return true;
+}
+
+}  // namespace
+
+void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
+    std::vector<EnsHost> H(n);
+    int nitout = 0, nitmax = 0, nused = 0;
+    for (int q = 0; q < n; ++q) {
+        H[q].used = in[q].status == 0;
+        if (!H[q].used) continue;
+        HT3D_REQUIRE(in[q].prm && in[q].prm->nitout > 0 && in[q].prm->nitmax > 0, "DYREL parameters");
+        if (nused == 0) {
+            nitout = in[q].prm->nitout;
+            nitmax = in[q].prm->nitmax;
+        }
+        HT3D_REQUIRE(in[q].prm->nitout == nitout && in[q].prm->nitmax == nitmax,
+                     "ensemble instances must share nitout and nitmax");
+        ++nused;
+    }
+    if (nused == 0) return;
+
+    // ---- per-instance scratch (FP64 check fields, padded FP32 fields)
+    auto carve_solve = [&](Carve& c) {
+        for (int q = 0; q < n; ++q) {
+            if (!H[q].used) continue;
+            EnsHost& h = H[q];
+            const EnsSolveInst& I = in[q];
+            h.P = make_pad(I.nx, I.ny, I.nz);
+            h.invPC = c.take<double>((size_t)I.nx * I.ny * I.nz);
+            h.X2 = c.take<double>((size_t)(I.nx + 2) * (I.ny + 2) * (I.nz + 2));
+            for (auto& f : h.f32) f = c.take<float>((size_t)h.P.size);
+        }
+    };
+    long long maxparts = 1;
+    for (int q = 0; q < n; ++q) {
+        if (!H[q].used) continue;
+        const EnsSolveInst& I = in[q];
+        ht3d_check_dims(I.nx, I.ny, I.nz, 1);
+        HT3D_REQUIRE(I.X && I.R && I.kx && I.ky && I.kz && I.F && I.F0 && I.bc_type6 && I.bc_val6, "null argument");
+        const Pad P = make_pad(I.nx, I.ny, I.nz);
+        HT3D_REQUIRE(P.size < (1LL << 31), "grid too large for the padded FP32 layout");
+        HT3D_REQUIRE(((long long)P.nq * I.ny * I.nz + kEnsBS[0] - 1) / kEnsBS[0] < (1LL << 30),
+                     "member too large for the batched launch");
+        H[q].LC = iter_launch(ctx, I.nx, I.ny, I.nz, HT3D_DYREL_ZMARCH);
+        maxparts = std::max(maxparts, std::max<long long>(H[q].LC.nblocks, (long long)((I.nx + 31) / 32) *
+                                                                               ((I.ny + 7) / 8) * I.nz));
+    }
+    {
+        Carve dry{nullptr};
+        carve_solve(dry);
+        Carve real{(char*)ht3d_scratch(ctx, SLOT_ENS_SOLVE, dry.off)};
+        carve_solve(real);
+    }
+    double* dres = (double*)ht3d_scratch(ctx, SLOT_ENS_TAB, sizeof(double) * 4 * (size_t)n);
+    double* parts = (double*)ht3d_scratch(ctx, SLOT_PARTIALS, sizeof(double) * 3 * maxparts);
+    // pinned staging of the results
+    const size_t hbytes = sizeof(double) * 4 * (size_t)n;
+    HT3D_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (ctx->h_ens_bytes < hbytes) {
+        if (ctx->h_ens) HT3D_CUDA(cudaFreeHost(ctx->h_ens));
+        ctx->h_ens = nullptr;
+        ctx->h_ens_bytes = 0;
+        HT3D_CUDA(cudaMallocHost(&ctx->h_ens, hbytes));
+        ctx->h_ens_bytes = hbytes;
+    }
+    double* hres = (double*)ctx->h_ens;
+
+    // ---- set-up of every instance (Gershgorin bound, FP32 copies)
+    const dim3 b2(32, 8, 1);
+    for (int q = 0; q < n; ++q) {
+        EnsHost& h = H[q];
+        if (!h.used) continue;
+        const EnsSolveInst& I = in[q];
+        const int nx = I.nx, ny = I.ny, nz = I.nz;
+        for (int f = 0; f < 6; ++f) {
+            HT3D_REQUIRE(I.bc_type6[f] == HT3D_BC_NEUMANN || I.bc_type6[f] == HT3D_BC_DIRICHLET,
+                         "face BC type must be 0 or 1");
+            h.bc.dir[f] = h.bch.dir[f] = I.bc_type6[f];
+            h.bc.val2[f] = 2.0 * I.bc_val6[f];
+            h.bch.val2[f] = 0.0f;
+        }
+        const dim3 gc((nx + 31) / 32, (ny + 7) / 8, nz);
+        const double transient = I.cX != 0.0 ? 1.0 : 0.0, dt = I.cX != 0.0 ? 1.0 / I.cX : 1.0;
+        HT3D_LAUNCH(ctx, k_dyrel_setup<1>, gc, b2, 0, I.kx, I.ky, I.kz, 1.0, transient, dt, I.dx, I.dy, I.dz, nx, ny, nz,
+                    h.invPC, parts);
+        HT3D_LAUNCH(ctx, (k_reduce_partials<RED_MAX, 1>), 1, 1024, 0, parts, (int)(gc.x * gc.y * gc.z), dres + q);
+        const size_t pbytes = sizeof(float) * (size_t)h.P.size;
+        for (float* a : h.f32) HT3D_CUDA(cudaMemsetAsync(a, 0, pbytes, ctx->stream));
+        HT3D_LAUNCH(ctx, k_pack, dim3((nx + 1 + 31) / 32, (ny + 7) / 8, nz), b2, 0, h.f32[5], I.kx, nx + 1, ny, nz, h.P);
+        HT3D_LAUNCH(ctx, k_pack, dim3((nx + 31) / 32, (ny + 1 + 7) / 8, nz), b2, 0, h.f32[6], I.ky, nx, ny + 1, nz, h.P);
+        HT3D_LAUNCH(ctx, k_pack, dim3((nx + 31) / 32, (ny + 7) / 8, nz + 1), b2, 0, h.f32[7], I.kz, nx, ny, nz + 1, h.P);
+    }
+    HT3D_CUDA(cudaMemcpyAsync(hres, dres, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    HT3D_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (int q = 0; q < n; ++q) {
+        EnsHost& h = H[q];
+        if (!h.used) continue;
+        const EnsSolveInst& I = in[q];
+        dyrel_init_params(I.prm, hres[q], h.S);
+        h.sc.cX = I.cX;
+        h.sc._dx = 1.0 / I.dx;
+        h.sc._dy = 1.0 / I.dy;
+        h.sc._dz = 1.0 / I.dz;
+        h.sc.h1 = h.S.h1;
+        h.sc.h2 = h.S.h2;
+        h.sc.dtau = h.S.dtau;
+        h.xcur = I.X;
+        h.xnxt = h.X2;
+        h.active = true;
+        h.last_fp64 = false;
+        h.it_done = 0;
+        h.checks = 0;
+        h.converged = 0;
+        h.status = HT3D_OK;
+        h.nF_abs = h.nF_rel = h.nF_ini = 0.0;
+    }
+
+    // ---- launch groups of the members still iterating, for each block size;
+    // rebuilt when a check changes the members' scalars or stops a member
+    std::vector<EnsLaunch> groups[3];
+    unsigned long long version = 0;
+    auto build_groups = [&]() {
+        version = ++ctx->ens_version;
+        for (int c = 0; c < 3; ++c) {
+            groups[c].clear();
+            for (int q = 0; q < n; ++q) {
+                const EnsHost& h = H[q];
+                if (!h.active) continue;
+                if (groups[c].empty() || groups[c].back().n == kEnsMaxPerLaunch) {
+                    groups[c].emplace_back();
+                    std::memset(&groups[c].back(), 0, sizeof(EnsLaunch));
+                }
+                EnsLaunch& L = groups[c].back();
+                const long long pq = (long long)h.P.nq * in[q].ny;
+                const long long nb_q = (pq * in[q].nz + kEnsBS[c] - 1) / kEnsBS[c];
+                if ((long long)L.nblk + nb_q >= (1LL << 31) - 1) {  // start a new group before the count overflows
+                    groups[c].emplace_back();
+                    std::memset(&groups[c].back(), 0, sizeof(EnsLaunch));
+                }
+                EnsLaunch& G = groups[c].back();
+                const int m = G.n++;
+                G.block0[m] = G.nblk;
+                G.quads[m] = (int)pq;
+                G.nblk += (int)nb_q;
+                G.block0[m + 1] = G.nblk;
+                EnsInner& e = G.rec[m];
+                e.D[0] = h.f32[0];
+                e.D[1] = h.f32[1];
+                e.F0 = h.f32[2];
+                e.F = h.f32[3];
+                e.Rin = h.f32[4];
+                e.kx = h.f32[5];
+                e.ky = h.f32[6];
+                e.kz = h.f32[7];
+                e.P = h.P;
+                e.s = DyrelScalT<float>(h.sc);
+                e.bc = h.bch;
+            }
+        }
+    };
+    build_groups();
+
+    // ---- block size: fixed, tuned earlier for this ensemble shape, or tuned now
+    unsigned long long shape = 0xcbf29ce484222325ULL;
+    for (int q = 0; q < n; ++q)
+        if (H[q].used) shape = mix_sig(mix_sig(mix_sig(mix_sig(shape, q), in[q].nx), in[q].ny), in[q].nz);
+    int cfg = -1;
+    auto cfg_of = [](int bs) { return bs == 64 ? 0 : (bs == 128 ? 1 : 2); };
+    if (ctx->ens_block) cfg = cfg_of(ctx->ens_block);
+    else if (ctx->ens_tune_key == shape && ctx->ens_tune_bs) cfg = cfg_of(ctx->ens_tune_bs);
+    bool tuning = cfg < 0;
+    int tune_n = 0;
+    if (tuning)
+        while ((int)ctx->tune_events.size() < 2 * 3 * kEnsTuneRounds) {
+            cudaEvent_t ev;
+            HT3D_CUDA(cudaEventCreate(&ev));
+            ctx->tune_events.push_back(ev);
+        }
+    bool graphs = ctx->ens_graphs != 0;
+
+    const int refresh_every = ctx->mixed_refresh;
+    auto is_fp64 = [&](int it) { return is_check(it, nitout) || (refresh_every > 0 && it % refresh_every == 0); };
+    auto is_storef = [&](int it) { return !is_fp64(it) && (it == nitmax || is_check(it + 1, nitout)); };
+    InnerTimer timer(ctx);
+    int nactive = nused;
+    for (int iter = 1; iter <= nitmax && nactive > 0; ++iter) {
+        const int parity = (iter - 1) & 1;  // correction buffer of every instance still iterating
+        const bool chk = is_check(iter, nitout);
+        if (is_fp64(iter)) {
+            timer.end();
+            for (int q = 0; q < n; ++q) {
+                EnsHost& h = H[q];
+                if (!h.active) continue;
+                h.sc.h1 = h.S.h1;
+                h.sc.h2 = h.S.h2;
+                h.sc.dtau = h.S.dtau;
+                const EnsSolveInst& I = in[q];
+                HT3D_LAUNCH(ctx, k_mixed_check, h.LC.grid, h.LC.block, 0, h.xcur, h.xnxt, h.f32[parity],
+                            h.f32[parity ^ 1], I.R, I.kx, I.ky, I.kz, h.invPC, h.f32[2], h.f32[3], I.F, h.f32[4], h.sc,
+                            h.bc, h.P, h.LC.zchunk, parts);
+                std::swap(h.xcur, h.xnxt);
+                h.it_done = iter;
+                h.last_fp64 = true;
+                if (chk)
+                    HT3D_LAUNCH(ctx, (k_reduce_partials<RED_SUM, 3>), 1, 1024, 0, parts, (int)h.LC.nblocks,
+                                dres + 3 * q);
+            }
+        } else {
+            timer.begin();
+            const bool storef = is_storef(iter);
+            int window = 1;
+            if (!storef && !tuning && graphs) {
+                window = 0;
+                while (window < kEnsGraphIters && iter + window <= nitmax && !is_fp64(iter + window) &&
+                       !is_storef(iter + window))
+                    ++window;
+                if (window == kEnsGraphIters) {
+                    graphs = ens_capture(ctx, mix_sig(version, cfg), cfg, groups[cfg]);
+                    if (!graphs) window = 1;
+                } else {
+                    window = 1;
+                }
+            }
+            if (window == kEnsGraphIters) {
+                HT3D_CUDA(cudaGraphLaunch(ctx->ens_graph[parity], ctx->stream));
+                ctx->launches += (unsigned long long)kEnsGraphIters * groups[cfg].size();
+                for (int g = 0; g < kEnsGraphIters; ++g) timer.count();
+            } else {
+                int c = tuning ? 1 : cfg;
+                const bool timed = tuning && !storef;
+                if (timed) {
+                    c = tune_n % 3;
+                    HT3D_CUDA(cudaEventRecord(ctx->tune_events[2 * tune_n], ctx->stream));
+                }
+                const int nl = storef ? ens_launch_all<true>(ctx->stream, c, groups[c], parity)
+                                      : ens_launch_all<false>(ctx->stream, c, groups[c], parity);
+                ctx->launches += nl;
+                timer.count();
+                if (timed) {
+                    HT3D_CUDA(cudaEventRecord(ctx->tune_events[2 * tune_n + 1], ctx->stream));
+                    if (++tune_n == 3 * kEnsTuneRounds) {
+                        HT3D_CUDA(cudaEventSynchronize(ctx->tune_events[2 * tune_n - 1]));
+                        float best = 0.f;
+                        for (int cc = 0; cc < 3; ++cc) {
+                            float sum = 0.f;
+                            for (int r = 0; r < kEnsTuneRounds; ++r) {
+                                float ms = 0.f;
+                                const int t = r * 3 + cc;
+                                HT3D_CUDA(cudaEventElapsedTime(&ms, ctx->tune_events[2 * t], ctx->tune_events[2 * t + 1]));
+                                sum += ms;
+                            }
+                            if (cc == 0 || sum < best) {
+                                best = sum;
+                                cfg = cc;
+                            }
+                        }
+                        tuning = false;
+                        ctx->ens_tune_key = shape;
+                        ctx->ens_tune_bs = kEnsBS[cfg];
+                    }
+                }
+            }
+            for (int q = 0; q < n; ++q)
+                if (H[q].active) {
+                    H[q].it_done = iter + window - 1;
+                    H[q].last_fp64 = false;
+                }
+            iter += window - 1;
+        }
+        if (chk) {
+            HT3D_CUDA(cudaMemcpyAsync(hres, dres, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
+            HT3D_CUDA(cudaStreamSynchronize(ctx->stream));
+            for (int q = 0; q < n; ++q) {
+                EnsHost& h = H[q];
+                if (!h.active) continue;
+                const ht3d_dyrel_params* prm = in[q].prm;
+                const double nc = (double)in[q].nx * in[q].ny * in[q].nz;
+                ++h.checks;
+                const double s_abs = hres[3 * q], s_num = hres[3 * q + 1], s_den = hres[3 * q + 2];
+                h.nF_abs = s_abs / nc / sqrt(nc) * prm->norm_scale;
+                if (iter == 1) h.nF_ini = h.nF_abs;
+                h.nF_rel = h.nF_abs / h.nF_ini;
+                bool stop = false;
+                if (std::isnan(h.nF_abs)) {
+                    h.status = HT3D_ERR_NAN;
+                    stop = true;
+                } else if (h.nF_rel > 100) {
+                    h.status = HT3D_ERR_DIVERGED;
+                    stop = true;
+                } else {
+                    if (iter > 1) {
+                        h.S.lmin = fabs(s_num) / fabs(s_den);
+                        h.S.c = 2.0 * sqrt(h.S.lmin) * prm->cfact;
+                        h.S.h1 = (2 - h.S.c * h.S.dtau) / (2 + h.S.c * h.S.dtau);
+                        h.S.h2 = 2 * h.S.dtau / (2 + h.S.c * h.S.dtau);
+                    }
+                    if (h.nF_abs < prm->tol_abs || h.nF_rel < prm->tol_rel) {
+                        h.converged = 1;
+                        stop = true;
+                    }
+                }
+                if (stop) {
+                    h.active = false;
+                    --nactive;
+                }
+                h.sc.h1 = h.S.h1;
+                h.sc.h2 = h.S.h2;
+                h.sc.dtau = h.S.dtau;
+            }
+            if (nactive > 0) build_groups();
+        }
+    }
+    timer.end();
+    // ---- final fold and outputs of every instance
+    for (int q = 0; q < n; ++q) {
+        EnsHost& h = H[q];
+        if (!h.used) continue;
+        const EnsSolveInst& I = in[q];
+        const int nx = I.nx, ny = I.ny, nz = I.nz;
+        const dim3 gc((nx + 31) / 32, (ny + 7) / 8, nz);
+        const int dc = h.it_done & 1;  // current correction buffer after it_done iterations
+        HT3D_LAUNCH(ctx, k_mixed_fold, gc, b2, 0, h.xcur, h.f32[dc], h.last_fp64 ? nullptr : h.f32[dc ^ 1], h.bc, h.P);
+        if (h.xcur != I.X) {
+            dim3 g((nx + 2 + 31) / 32, (ny + 2 + 7) / 8, nz + 2);
+            HT3D_LAUNCH(ctx, k_copy_ex_faces<double>, g, b2, 0, I.X, h.xcur, nx, ny, nz);
+        }
+        HT3D_LAUNCH(ctx, k_unpack, gc, b2, 0, I.F0, h.f32[2], h.P);
+        if (!h.last_fp64) HT3D_LAUNCH(ctx, k_unpack, gc, b2, 0, I.F, h.f32[3], h.P);
+        if (I.st) {
+            ht3d_dyrel_stats* st = I.st;
+            st->iters = h.it_done; st->converged = h.converged; st->status = h.status; st->checks = h.checks;
+            st->nF_abs = h.nF_abs; st->nF_rel = h.nF_rel; st->nF_ini = h.nF_ini; st->lambda_min = h.S.lmin;
+            st->lambda_max = h.S.lmax; st->h1 = h.S.h1; st->h2 = h.S.h2; st->dtau = h.S.dtau;
+        }
+        in[q].status = h.status;
+    }
+    timer.collect();
 }
 
 

@@ -29,6 +29,9 @@ enum ScratchSlot {
     SLOT_STEP_R, SLOT_STEP_F, SLOT_STEP_F0, SLOT_STEP_TY, SLOT_STEP_KX, SLOT_STEP_KY, SLOT_STEP_KZ,
     SLOT_WENO_T0, SLOT_WENO_T1, SLOT_WENO_T2, SLOT_WENO_V,
     SLOT_AUX0, SLOT_AUX1, SLOT_AUX2, SLOT_AUX3,
+    SLOT_ENS_SOLVE,     // batched solve: per-instance FP64 and padded FP32 fields
+    SLOT_ENS_TAB,       // batched solve: per-instance check results
+    SLOT_ENS_STEP,      // ensemble step: per-instance residual, flux and conductivity fields
     SLOT_COUNT
 };
 
@@ -43,6 +46,17 @@ struct ht3d_ctx {
     std::vector<cudaEvent_t> events;      // event pool of the inner-iteration timer
     double inner_ms = 0.0;                // accumulated device time of the timed runs
     unsigned long long inner_launches = 0;  // inner-iteration launches inside them
+    // batched ensemble solve
+    int ens_block = 0;                    // threads per block of the batched kernel (0 = autotune)
+    int ens_graphs = 1;                   // replay windows of inner iterations as CUDA graphs
+    unsigned long long ens_tune_key = 0;  // ensemble signature the tuned block size belongs to
+    int ens_tune_bs = 0;
+    std::vector<cudaEvent_t> tune_events;
+    unsigned long long ens_version = 0;   // bumped whenever the batched launch parameters change
+    unsigned long long ens_graph_sig = 0; // launch parameters the captured graphs carry
+    cudaGraphExec_t ens_graph[2] = {nullptr, nullptr};  // windows starting on parity 0 / 1
+    void* h_ens = nullptr;                // pinned staging (instance records, results)
+    size_t h_ens_bytes = 0;
     int num_sms = 152;
     unsigned long long launches = 0;
     std::string last_error;

@@ -16,125 +16,62 @@ void ht3d_weno5_advect_impl(ht3d_ctx* ctx, double* Tc_ex, const double* Vx, cons
                             double dt, double _dx, double _dy, double _dz, const int* bc_type6, const double* bc_val6,
                             int variant, int precision, int nx, int ny, int nz);
 
-namespace {
+#include "step_kernels.cuh"
 
-#define GIDX                                             \
-    const int i = blockIdx.x * blockDim.x + threadIdx.x; \
-    const int j = blockIdx.y * blockDim.y + threadIdx.y; \
-    const int k = blockIdx.z * blockDim.z + threadIdx.z
-
-__device__ __forceinline__ void faces_from_vertices(double* kx, double* ky, double* kz, const double* __restrict__ kv,
-                                                    int i, int j, int k, int nx, int ny, int nz) {
-    const int v1 = nx + 1, v2 = ny + 1;
-    if (i < nx + 1 && j < ny && k < nz)
-        kx[ix3(i, j, k, nx + 1, ny)] = (kv[ix3(i, j, k, v1, v2)] + kv[ix3(i, j + 1, k, v1, v2)] +
-                                        kv[ix3(i, j, k + 1, v1, v2)] + kv[ix3(i, j + 1, k + 1, v1, v2)]) * 0.25;
-    if (i < nx && j < ny + 1 && k < nz)
-        ky[ix3(i, j, k, nx, ny + 1)] = (kv[ix3(i, j, k, v1, v2)] + kv[ix3(i + 1, j, k, v1, v2)] +
-                                        kv[ix3(i, j, k + 1, v1, v2)] + kv[ix3(i + 1, j, k + 1, v1, v2)]) * 0.25;
-    if (i < nx && j < ny && k < nz + 1)
-        kz[ix3(i, j, k, nx, ny)] = (kv[ix3(i, j, k, v1, v2)] + kv[ix3(i + 1, j, k, v1, v2)] +
-                                    kv[ix3(i, j + 1, k, v1, v2)] + kv[ix3(i + 1, j + 1, k, v1, v2)]) * 0.25;
-}
-
-// InitThermal! (Dimensionless/kernels_HT3D.jl:99-107)
-__global__ void k_step_init_thermal(double* Rt, double* kx, double* ky, double* kz, const double* __restrict__ T,
-                                    const double* __restrict__ kv, double _dt, int nx, int ny, int nz) {
-    GIDX;
-    if (i < nx && j < ny && k < nz) Rt[ix3(i, j, k, nx, ny)] = -_dt * T[ix3(i + 1, j + 1, k + 1, nx + 2, ny + 2)];
-    faces_from_vertices(kx, ky, kz, kv, i, j, k, nx, ny, nz);
-}
-
-// InitDarcy! + KillNorthSouthFluxes! (Alban_v6.jl:47-55, 153-159)
-__global__ void k_step_init_darcy(double* Ty, double* kx, double* ky, double* kz, const double* __restrict__ T,
-                                  const double* __restrict__ kv, int kill_ns, int nx, int ny, int nz) {
-    GIDX;
-    if (i < nx && j < ny + 1 && k < nz) {
-        double t = (T[ix3(i + 1, j, k + 1, nx + 2, ny + 2)] + T[ix3(i + 1, j + 1, k + 1, nx + 2, ny + 2)]) * 0.5;
-        if (kill_ns && (j == 0 || j == ny)) t = 0.0;
-        Ty[ix3(i, j, k, nx, ny + 1)] = t;
+int ht3d_step_hrl_impl(ht3d_ctx* ctx, double* Tc_ex, double* Pc_ex, const double* ktv, const double* kfv, double* Vx,
+                       double* Vy, double* Vz, ht3d_hrl_params* p, ht3d_dyrel_stats* st_thermal,
+                       ht3d_dyrel_stats* st_darcy, int precision, int nx, int ny, int nz) {
+    ht3d_check_dims(nx, ny, nz, 1);
+    HT3D_REQUIRE(Tc_ex && Pc_ex && ktv && kfv && Vx && Vy && Vz && p, "null argument");
+    HT3D_REQUIRE(precision == HT3D_FP64 || precision == HT3D_MIXED, "unknown precision");
+    HT3D_REQUIRE(p->dt > 0.0, "dt must be positive");
+    const long long n = (long long)nx * ny * nz;
+    const long long nfx = (long long)(nx + 1) * ny * nz, nfy = (long long)nx * (ny + 1) * nz,
+                    nfz = (long long)nx * ny * (nz + 1);
+    double* R = (double*)ht3d_scratch(ctx, SLOT_STEP_R, sizeof(double) * n);
+    double* F = (double*)ht3d_scratch(ctx, SLOT_STEP_F, sizeof(double) * n);
+    double* F0 = (double*)ht3d_scratch(ctx, SLOT_STEP_F0, sizeof(double) * n);
+    double* Ty = (double*)ht3d_scratch(ctx, SLOT_STEP_TY, sizeof(double) * nfy);
+    double* kx = (double*)ht3d_scratch(ctx, SLOT_STEP_KX, sizeof(double) * nfx);
+    double* ky = (double*)ht3d_scratch(ctx, SLOT_STEP_KY, sizeof(double) * nfy);
+    double* kz = (double*)ht3d_scratch(ctx, SLOT_STEP_KZ, sizeof(double) * nfz);
+    const double _dx = 1.0 / p->dx, _dy = 1.0 / p->dy, _dz = 1.0 / p->dz, _dt = 1.0 / p->dt;
+    const dim3 gv = grid3(nx + 1, ny + 1, nz + 1, kBlock3), gc = grid3(nx, ny, nz, kBlock3);
+    auto solve = precision == HT3D_FP64 ? ht3d_dyrel_solve_fp64 : ht3d_dyrel_solve_mixed;
+    // thermal
+    HT3D_LAUNCH(ctx, k_step_init_thermal, gv, kBlock3, 0, R, kx, ky, kz, Tc_ex, ktv, _dt, nx, ny, nz);
+    int s = solve(ctx, Tc_ex, R, kx, ky, kz, _dt, p->dx, p->dy, p->dz, p->thermal_bc, p->thermal_val, &p->thermal,
+                  0, F, F0, st_thermal, nx, ny, nz);
+    if (s) return s;
+    // Darcy
+    HT3D_LAUNCH(ctx, k_step_init_darcy, gv, kBlock3, 0, Ty, kx, ky, kz, Tc_ex, kfv, p->kill_ns, nx, ny, nz);
+    HT3D_LAUNCH(ctx, k_step_rp, gc, kBlock3, 0, R, ky, Ty, p->Ra, _dy, nx, ny, nz);
+    s = solve(ctx, Pc_ex, R, kx, ky, kz, 0.0, p->dx, p->dy, p->dz, p->darcy_bc, p->darcy_val, &p->darcy, 0, F, F0,
+              st_darcy, nx, ny, nz);
+    if (s) return s;
+    // velocity and advection
+    HT3D_LAUNCH(ctx, k_step_vel, gv, kBlock3, 0, Vx, Vy, Vz, kx, ky, kz, Pc_ex, Ty, p->Ra, _dx, _dy, _dz, nx, ny, nz);
+    if (p->advection)
+        ht3d_weno5_advect_impl(ctx, Tc_ex, Vx, Vy, Vz, p->dt, _dx, _dy, _dz, p->weno_bc, p->weno_val,
+                               p->weno_variant, precision, nx, ny, nz);
+    if (p->dt_adapt) {
+        double* dres = (double*)ht3d_scratch(ctx, SLOT_RESULT, sizeof(double) * 64);
+        ht3d_reduce_device(ctx, Vx, nfx, RED_MAX_ABS, dres + 8);
+        ht3d_reduce_device(ctx, Vy, nfy, RED_MAX_ABS, dres + 9);
+        ht3d_reduce_device(ctx, Vz, nfz, RED_MAX_ABS, dres + 10);
+        ht3d_fetch_results(ctx, dres + 8, 3);
+        const double vmax = std::max(std::max(ctx->h_result[0], ctx->h_result[1]), ctx->h_result[2]);
+        p->dt = p->dt_fact * 1.0 / 6.1 * std::min(std::min(p->dx, p->dy), p->dz) / vmax;
+        if (p->dt_max > 0.0 && p->dt > p->dt_max) p->dt = p->dt_max;
     }
-    faces_from_vertices(kx, ky, kz, kv, i, j, k, nx, ny, nz);
+    return HT3D_OK;
 }
-
-// Compute_Rp! (Dimensionless/kernels_HT3D.jl:92-97)
-__global__ void k_step_rp(double* Rp, const double* __restrict__ ky, const double* __restrict__ Ty, double Ra, double _dy,
-                          int nx, int ny, int nz) {
-    GIDX;
-    if (i >= nx || j >= ny || k >= nz) return;
-    const int a = ix3(i, j, k, nx, ny + 1), b = ix3(i, j + 1, k, nx, ny + 1);
-    Rp[ix3(i, j, k, nx, ny)] = Ra * _dy * ((ky[b] * Ty[b]) - (ky[a] * Ty[a]));
-}
-
-// Init_vel! (Dimensionless/kernels_HT3D.jl:73-80)
-__global__ void k_step_vel(double* Vx, double* Vy, double* Vz, const double* __restrict__ kx,
-                           const double* __restrict__ ky, const double* __restrict__ kz, const double* __restrict__ P,
-                           const double* __restrict__ Ty, double Ra, double _dx, double _dy, double _dz, int nx, int ny,
-                           int nz) {
-    GIDX;
-    const int e1 = nx + 2, e2 = ny + 2;
-    if (i < nx + 1 && j < ny && k < nz) {
-        const int f = ix3(i, j, k, nx + 1, ny);
-        Vx[f] = -kx[f] * _dx * (P[ix3(i + 1, j + 1, k + 1, e1, e2)] - P[ix3(i, j + 1, k + 1, e1, e2)]);
-    }
-    if (i < nx && j < ny + 1 && k < nz) {
-        const int f = ix3(i, j, k, nx, ny + 1);
-        Vy[f] = -ky[f] * (_dy * (P[ix3(i + 1, j + 1, k + 1, e1, e2)] - P[ix3(i + 1, j, k + 1, e1, e2)]) - Ra * Ty[f]);
-    }
-    if (i < nx && j < ny && k < nz + 1) {
-        const int f = ix3(i, j, k, nx, ny);
-        Vz[f] = -kz[f] * _dz * (P[ix3(i + 1, j + 1, k + 1, e1, e2)] - P[ix3(i + 1, j + 1, k, e1, e2)]);
-    }
-}
-
-}  // namespace
 
 extern "C" int ht3d_step_hrl(ht3d_ctx* ctx, double* Tc_ex, double* Pc_ex, const double* ktv, const double* kfv,
                              double* Vx, double* Vy, double* Vz, ht3d_hrl_params* p, ht3d_dyrel_stats* st_thermal,
                              ht3d_dyrel_stats* st_darcy, int precision, int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
-        ht3d_check_dims(nx, ny, nz, 1);
-        HT3D_REQUIRE(Tc_ex && Pc_ex && ktv && kfv && Vx && Vy && Vz && p, "null argument");
-        HT3D_REQUIRE(precision == HT3D_FP64 || precision == HT3D_MIXED, "unknown precision");
-        HT3D_REQUIRE(p->dt > 0.0, "dt must be positive");
-        const long long n = (long long)nx * ny * nz;
-        const long long nfx = (long long)(nx + 1) * ny * nz, nfy = (long long)nx * (ny + 1) * nz,
-                        nfz = (long long)nx * ny * (nz + 1);
-        double* R = (double*)ht3d_scratch(ctx, SLOT_STEP_R, sizeof(double) * n);
-        double* F = (double*)ht3d_scratch(ctx, SLOT_STEP_F, sizeof(double) * n);
-        double* F0 = (double*)ht3d_scratch(ctx, SLOT_STEP_F0, sizeof(double) * n);
-        double* Ty = (double*)ht3d_scratch(ctx, SLOT_STEP_TY, sizeof(double) * nfy);
-        double* kx = (double*)ht3d_scratch(ctx, SLOT_STEP_KX, sizeof(double) * nfx);
-        double* ky = (double*)ht3d_scratch(ctx, SLOT_STEP_KY, sizeof(double) * nfy);
-        double* kz = (double*)ht3d_scratch(ctx, SLOT_STEP_KZ, sizeof(double) * nfz);
-        const double _dx = 1.0 / p->dx, _dy = 1.0 / p->dy, _dz = 1.0 / p->dz, _dt = 1.0 / p->dt;
-        const dim3 gv = grid3(nx + 1, ny + 1, nz + 1, kBlock3), gc = grid3(nx, ny, nz, kBlock3);
-        auto solve = precision == HT3D_FP64 ? ht3d_dyrel_solve_fp64 : ht3d_dyrel_solve_mixed;
-        // thermal
-        HT3D_LAUNCH(ctx, k_step_init_thermal, gv, kBlock3, 0, R, kx, ky, kz, Tc_ex, ktv, _dt, nx, ny, nz);
-        int s = solve(ctx, Tc_ex, R, kx, ky, kz, _dt, p->dx, p->dy, p->dz, p->thermal_bc, p->thermal_val, &p->thermal,
-                      0, F, F0, st_thermal, nx, ny, nz);
-        if (s) return s;
-        // Darcy
-        HT3D_LAUNCH(ctx, k_step_init_darcy, gv, kBlock3, 0, Ty, kx, ky, kz, Tc_ex, kfv, p->kill_ns, nx, ny, nz);
-        HT3D_LAUNCH(ctx, k_step_rp, gc, kBlock3, 0, R, ky, Ty, p->Ra, _dy, nx, ny, nz);
-        s = solve(ctx, Pc_ex, R, kx, ky, kz, 0.0, p->dx, p->dy, p->dz, p->darcy_bc, p->darcy_val, &p->darcy, 0, F, F0,
-                  st_darcy, nx, ny, nz);
-        if (s) return s;
-        // velocity and advection
-        HT3D_LAUNCH(ctx, k_step_vel, gv, kBlock3, 0, Vx, Vy, Vz, kx, ky, kz, Pc_ex, Ty, p->Ra, _dx, _dy, _dz, nx, ny, nz);
-        if (p->advection)
-            ht3d_weno5_advect_impl(ctx, Tc_ex, Vx, Vy, Vz, p->dt, _dx, _dy, _dz, p->weno_bc, p->weno_val,
-                                   p->weno_variant, precision, nx, ny, nz);
-        if (p->dt_adapt) {
-            double* dres = (double*)ht3d_scratch(ctx, SLOT_RESULT, sizeof(double) * 64);
-            ht3d_reduce_device(ctx, Vx, nfx, RED_MAX_ABS, dres + 8);
-            ht3d_reduce_device(ctx, Vy, nfy, RED_MAX_ABS, dres + 9);
-            ht3d_reduce_device(ctx, Vz, nfz, RED_MAX_ABS, dres + 10);
-            ht3d_fetch_results(ctx, dres + 8, 3);
-            const double vmax = std::max(std::max(ctx->h_result[0], ctx->h_result[1]), ctx->h_result[2]);
-            p->dt = p->dt_fact * 1.0 / 6.1 * std::min(std::min(p->dx, p->dy), p->dz) / vmax;
-        }
-        return HT3D_OK;
+        return ht3d_step_hrl_impl(ctx, Tc_ex, Pc_ex, ktv, kfv, Vx, Vy, Vz, p, st_thermal, st_darcy, precision, nx, ny,
+                                  nz);
     });
 }

@@ -44,7 +44,7 @@ def initial_fields(nx, ny, nz, seed=1, amp=1e-3, Tbot=1.0, Ttop=0.0, L=(1.0, 1.0
 
 
 def params(nx, ny, nz, Ra=1000.0, tol=1e-8, nitmax=10000, nitout=1000, dt_fact=1.0, weno_variant=abi.WENO_V1,
-           L=(1.0, 1.0, 1.0), Tbot=1.0, Ttop=0.0, advection=True, dt_adapt=True):
+           L=(1.0, 1.0, 1.0), Tbot=1.0, Ttop=0.0, advection=True, dt_adapt=True, dt_max=0.0):
     Lx, Ly, Lz = L
     dx, dy, dz = Lx / nx, Ly / ny, Lz / nz
     p = abi.HrlParams()
@@ -62,9 +62,39 @@ def params(nx, ny, nz, Ra=1000.0, tol=1e-8, nitmax=10000, nitout=1000, dt_fact=1
     p.dt_adapt = 1 if dt_adapt else 0
     p.advection = 1 if advection else 0
     p.dt_fact = dt_fact
+    p.dt_max = dt_max
     p.thermal = abi.DyrelParams.reference(tol=tol, nitmax=nitmax, nitout=nitout)
     p.darcy = abi.DyrelParams.reference(tol=tol, nitmax=nitmax, nitout=nitout)
     return p
+
+
+def ensemble(n_members=64, seed=4, nmin=31, nmax=95, ra=(100.0, 5000.0), log10k_sigma=0.25, corr_cells=4.0,
+             dt_max=1e-3, **kw):
+    """Members of the ensemble workload: per member, cells per axis drawn
+    from U{nmin..nmax}, Ra log-uniform on [ra[0], ra[1]], an independent
+    log-normal permeability kfv (log10 k ~ N(0, log10k_sigma) with a Gaussian
+    correlation of corr_cells cells) and the HRL initial condition; ktv = 1.
+    Returns a list of (Tc_ex, Pc_ex, ktv, kfv, HrlParams) with numpy fields.
+    Extra keyword arguments go to params().
+
+    The adapted dt is capped at dt_max: near the critical Rayleigh number the
+    velocity stays small for many steps, the reference's rule lets dt grow
+    without bound (to ~10^2 diffusion times), and convection then sets in
+    within one step at a CFL number above 10, which WENO5/SSP-RK2 does not
+    survive (a Ra = 118 member reached NaN at step 12 in FP64 as well)."""
+    from .v18 import lognormal_field
+    rng = np.random.default_rng(seed)
+    out = []
+    for m in range(n_members):
+        nx, ny, nz = (int(v) for v in rng.integers(nmin, nmax + 1, size=3))
+        Ra = float(np.exp(rng.uniform(np.log(ra[0]), np.log(ra[1]))))
+        T, P, ktv, _ = initial_fields(nx, ny, nz, seed=int(rng.integers(1 << 30)))
+        h = 1.0 / max(nx, ny, nz)
+        g = lognormal_field((nx + 1, ny + 1, nz + 1), (1.0 / nx, 1.0 / ny, 1.0 / nz), mean=0.0, sigma=log10k_sigma,
+                            corr=corr_cells * h, seed=int(rng.integers(1 << 30)))
+        kfv = np.asfortranarray(10.0 ** g)
+        out.append((T, P, ktv, kfv, params(nx, ny, nz, Ra=Ra, dt_max=dt_max, **kw)))
+    return out
 
 
 def bytes_per_iteration(nx, ny, nz, s):

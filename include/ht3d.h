@@ -68,6 +68,10 @@ extern "C" {
 #define HT3D_TUNE_TIME_INNER 3      /* 1: the mixed solver brackets every run of consecutive
                                        FP32 inner-iteration launches with CUDA events on the
                                        ctx stream (read back by ht3d_ctx_inner_timing)    */
+#define HT3D_TUNE_ENS_BLOCK 4       /* threads per block of the batched ensemble iteration:
+                                       0 = autotune on first use (64/128/256), or fixed   */
+#define HT3D_TUNE_ENS_GRAPH 5       /* 1 (default): replay windows of 16 batched inner
+                                       iterations as CUDA graphs; 0: launch one by one    */
 
 typedef struct ht3d_ctx ht3d_ctx;
 
@@ -106,6 +110,8 @@ typedef struct ht3d_hrl_params {
     int advection;
     double dt_fact;
     ht3d_dyrel_params thermal, darcy;
+    double dt_max;             /* > 0: upper bound of the adapted dt; 0 = the reference's
+                                  rule, which has none */
 } ht3d_hrl_params;
 
 /* Dimensional time step (see ht3d_step_v18); values in the reference's scaled
@@ -149,6 +155,7 @@ const char* ht3d_ctx_last_error(const ht3d_ctx* ctx);
 int ht3d_sizeof_dyrel_params(void);
 int ht3d_sizeof_dyrel_stats(void);
 int ht3d_sizeof_hrl_params(void);
+int ht3d_sizeof_instance(void);
 int ht3d_sizeof_v18_params(void);
 
 /* ------------------------------------------------------------------ */
@@ -406,6 +413,35 @@ int ht3d_dyrel_iterate_noalloc(double* X_ex, const double* R, const double* kx, 
 int ht3d_step_hrl(ht3d_ctx* ctx, double* Tc_ex, double* Pc_ex, const double* ktv, const double* kfv, double* Vx,
                   double* Vy, double* Vz, ht3d_hrl_params* p, ht3d_dyrel_stats* st_thermal,
                   ht3d_dyrel_stats* st_darcy, int precision, int nx, int ny, int nz);
+
+/* One member of an ensemble of independent HRL runs (the arguments of one
+   ht3d_step_hrl call).  No reference counterpart: the reference runs one
+   model per process. */
+typedef struct ht3d_instance {
+    double* Tc_ex;             /* (nx+2)(ny+2)(nz+2) */
+    double* Pc_ex;             /* (nx+2)(ny+2)(nz+2) */
+    const double* ktv;         /* vertices (nx+1)(ny+1)(nz+1) */
+    const double* kfv;         /* vertices */
+    double* Vx;                /* x-faces (nx+1) ny nz */
+    double* Vy;                /* y-faces nx (ny+1) nz */
+    double* Vz;                /* z-faces nx ny (nz+1) */
+    ht3d_hrl_params* params;   /* host; dt updated in place when dt_adapt */
+    ht3d_dyrel_stats* st_thermal;  /* host, may be NULL */
+    ht3d_dyrel_stats* st_darcy;    /* host, may be NULL */
+    int nx, ny, nz;
+    int status;                /* out: HT3D_* of this member's step */
+} ht3d_instance;
+
+/* One time step of every member: the same result, bit for bit, as calling
+   ht3d_step_hrl on each member in turn.  HT3D_MIXED batches the members: the
+   thermal solves of all members iterate in lockstep with one launch per
+   pseudo-iteration over every member still iterating (windows of them
+   replayed as CUDA graphs), then the Darcy solves; each member keeps its own
+   DYREL parameters, checks and stop test (members must share nitout and
+   nitmax).  HT3D_FP64 steps the members one after another.  A member that
+   fails (NaN, divergence) stops with its status; the others go on.  Returns
+   the first failing member's status, or HT3D_OK. */
+int ht3d_ensemble_step(ht3d_ctx* ctx, ht3d_instance* members, int n_members, int precision);
 
 /* One time step of the dimensional model, Dimensional/HydroThermal3D_v18.jl:404-572:
    pluton insertion at it == 1, thermal DYREL solve (conductivity, smoothing,

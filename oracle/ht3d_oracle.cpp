@@ -944,6 +944,7 @@ struct orc_hrl_params {
     int advection;
     double dt_fact;
     orc_dyrel_params thermal, darcy;
+    double dt_max;                   // > 0: upper bound of the adapted dt (not in the reference)
 };
 
 int orc_step_hrl(double* Tc_ex, double* Pc_ex, const double* ktv, const double* kfv, double* Vx, double* Vy,
@@ -979,6 +980,7 @@ int orc_step_hrl(double* Tc_ex, double* Pc_ex, const double* ktv, const double* 
         const double vmax = std::max(std::max(orc_max_abs(Vx, (nx + 1) * ny * nz), orc_max_abs(Vy, nx * (ny + 1) * nz)),
                                      orc_max_abs(Vz, nx * ny * (nz + 1)));
         p->dt = p->dt_fact * 1.0 / 6.1 * std::min(std::min(p->dx, p->dy), p->dz) / vmax;
+        if (p->dt_max > 0.0 && p->dt > p->dt_max) p->dt = p->dt_max;
     }
     return ORC_OK;
 }

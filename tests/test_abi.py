@@ -36,6 +36,7 @@ def test_struct_layouts_match(lib):
     assert lib.ht3d_sizeof_dyrel_params() == ctypes.sizeof(abi.DyrelParams)
     assert lib.ht3d_sizeof_dyrel_stats() == ctypes.sizeof(abi.DyrelStats)
     assert lib.ht3d_sizeof_hrl_params() == ctypes.sizeof(abi.HrlParams)
+    assert lib.ht3d_sizeof_instance() == ctypes.sizeof(abi.Instance)
 
 
 def test_status_strings(lib):

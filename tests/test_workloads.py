@@ -1,0 +1,39 @@
+"""Host-side set-up of the benchmark workloads (no GPU)."""
+import numpy as np
+
+from hydrothermal3d_gb300 import hrl
+
+
+def test_ensemble_workload_generator():
+    mem = hrl.ensemble(n_members=6, seed=4)
+    assert len(mem) == 6
+    sizes = set()
+    for T, P, ktv, kfv, p in mem:
+        nx, ny, nz = (s - 2 for s in T.shape)
+        sizes.add((nx, ny, nz))
+        assert all(31 <= v <= 95 for v in (nx, ny, nz))
+        assert 100.0 <= p.Ra <= 5000.0
+        assert kfv.shape == (nx + 1, ny + 1, nz + 1) and kfv.min() > 0 and np.isfinite(kfv).all()
+        assert abs(np.log10(kfv).std() - 0.25) < 0.05
+        assert p.thermal.nitout == mem[0][4].thermal.nitout
+    assert len(sizes) == 6
+    # seeded: the same members again
+    again = hrl.ensemble(n_members=6, seed=4)
+    for a, b in zip(mem, again):
+        np.testing.assert_array_equal(a[3], b[3])
+        assert a[4].Ra == b[4].Ra
+
+
+def test_dt_max_caps_the_adapted_dt(orc):
+    """dt_max bounds the adapted dt (0 keeps the reference's unbounded rule)."""
+    n = 8
+    T, P, ktv, kfv = hrl.initial_fields(n, n, n, seed=3)
+    dts = []
+    for cap in (0.0, 1e-5):
+        p = hrl.params(n, n, n, Ra=100.0, nitout=100, dt_max=cap)
+        V = [np.zeros((n + 1, n, n), order="F"), np.zeros((n, n + 1, n), order="F"), np.zeros((n, n, n + 1), order="F")]
+        Tc, Pc = T.copy(order="F"), P.copy(order="F")
+        s, _, _ = orc.step_hrl(Tc, Pc, ktv, kfv, *V, p)
+        assert s == 0
+        dts.append(p.dt)
+    assert dts[0] > 1e-5 and dts[1] == 1e-5
