@@ -47,6 +47,9 @@ def parse():
     ap.add_argument("--ens-members", type=int, default=64)
     ap.add_argument("--ens-steps", type=int, default=20)
     ap.add_argument("--skip-ensemble", action="store_true")
+    ap.add_argument("--sweep-n", type=int, default=511, help="cells per axis of the standalone WENO5 sweep (0 = skip)")
+    ap.add_argument("--fault-steps", type=int, default=0,
+                    help="time steps of the 511^3 fault-slab HRL case (mixed form; 0 = skip)")
     return ap.parse_args()
 
 
@@ -287,6 +290,11 @@ def run_ours(a):
     # --- secondary metric: batched ensemble vs the same members one by one
     if not a.skip_ensemble:
         out["ensemble"] = ensemble_bench(ctx, stream, a)
+    # --- standalone WENO5 sweep on the large grid
+    if a.sweep_n:
+        out["weno_sweep"] = sweep_bench(ctx, stream, a.sweep_n)
+    if a.fault_steps:
+        out["fault_slab_511"] = fault_bench(ctx, stream, a)
 
     if rank == 0:
         v, cores, desc, _ = cpu_sample(n, a.cpu_seconds, threads=os.cpu_count())
@@ -470,6 +478,76 @@ def ensemble_bench(ctx, stream, a):
     res["same_work"] = arms["batched"]["upd"] == arms["sequential"]["upd"]
     res["block_size"] = "autotuned (HT3D_TUNE_ENS_BLOCK = 0)"
     return res
+
+
+def sweep_bench(ctx, stream, n, reps=3):
+    """One SSP-RK2 WENO5 sweep over the three axes of an n^3 grid (blob in a
+    divergence-free curl velocity, CFL 0.5), FP32, mixed and FP64; inputs
+    resident in HBM (each field > L2); CUDA events on the ctx stream."""
+    import torch
+    import hydrothermal3d_gb300 as ht
+    from hydrothermal3d_gb300 import api, abi, sweep
+    V = sweep.curl_velocity(n, n, n, seed=6)
+    T0 = sweep.blob(n, n, n)
+    dt = sweep.cfl_dt(n, n, n, cfl=0.5)
+    h = (float(n),) * 3
+    bc, bv = [0, 0, 1, 1, 0, 0], [0, 0, 1.0, 0.0, 0, 0]
+    res = {"n": n, "velocity": "discrete curl of seeded sine modes (seed 6), max|V| = 1", "cfl": 0.5,
+           "unit": "GB/s (21 N s per sweep)"}
+    peak = measured_peak()[0]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        for name, prec, s in (("fp32", None, 4), ("mixed", abi.MIXED, 8), ("fp64", abi.FP64, 8)):
+            if prec is None:
+                T = T0.float().permute(2, 1, 0).contiguous().permute(2, 1, 0)
+                Vs = [v.float().permute(2, 1, 0).contiguous().permute(2, 1, 0) for v in V]
+                fn = lambda: api.weno5_advect_f32(ctx, T, *Vs, dt, *h, bc, bv, abi.WENO_V1)
+            else:
+                T = T0.clone()
+                fn = lambda: api.weno5_advect(ctx, T, *V, dt, *h, bc, bv, abi.WENO_V1, prec)
+            fn()
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(reps):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t = e0.elapsed_time(e1) / 1e3 / reps
+            gbs = sweep.bytes_per_sweep(n, n, n, s) / t / 1e9
+            res[name] = {"ms_per_sweep": t * 1e3, "T_eff_GBs": gbs, "frac_of_measured_hbm": gbs / peak,
+                         "storage_bytes": s}
+            del T
+    return res
+
+
+def fault_bench(ctx, stream, a):
+    """511^3 mixed-form HRL steps with a log-normal permeability and a x10
+    fault slab (seed 5)."""
+    import torch
+    import hydrothermal3d_gb300 as ht
+    from hydrothermal3d_gb300 import api, abi, hrl
+    n = 511
+    T, P, ktv, kfv, p = hrl.fault_slab_case(n=n, seed=5)
+    V = [ht.zeros(n + 1, n, n), ht.zeros(n, n + 1, n), ht.zeros(n, n, n + 1)]
+    iters, nbytes = [], 0
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(a.fault_steps):
+            gt, gd = api.step_hrl(ctx, T, P, ktv, kfv, *V, p, abi.MIXED)
+            iters.append((gt.iters, gd.iters))
+            nbytes += (gt.iters + gd.iters) * hrl.bytes_per_iteration(n, n, n, 4) + hrl.bytes_per_advection(n, n, n, 4)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3
+    inner = T[1:-1, 1:-1, 1:-1]
+    return {"n": n, "steps": a.fault_steps, "seconds": t, "time_steps_per_s": a.fault_steps / t,
+            "T_eff_GBs": nbytes / t / 1e9, "pseudo_iterations_per_step": [list(x) for x in iters],
+            "T_range": [float(inner.min()), float(inner.max())], "dt_last": p.dt,
+            "case": "HRL Ra 1000, log-normal kf (log10 sigma 0.25, 4-cell correlation) with a x10 slab 3 cells "
+                    "wide at mid-x, seed 5, dt_max 1e-3, mixed form, no warm-up (first steps from the initial "
+                    "condition)"}
 
 
 def measured_peak():

@@ -106,11 +106,11 @@ def to_numpy(t):
     return np.asfortranarray(t.detach().permute(2, 1, 0).contiguous().cpu().numpy().transpose(2, 1, 0))
 
 
-def _ptr(t, shape=None, name="array"):
+def _ptr(t, shape=None, name="array", dtype=torch.float64):
     if not isinstance(t, torch.Tensor):
         raise ValueError(f"{name}: expected a torch tensor")
-    if t.dtype != torch.float64 or not t.is_cuda:
-        raise ValueError(f"{name}: expected a CUDA float64 tensor, got {t.dtype} on {t.device}")
+    if t.dtype != dtype or not t.is_cuda:
+        raise ValueError(f"{name}: expected a CUDA {dtype} tensor, got {t.dtype} on {t.device}")
     if t.dim() == 2:
         n1, n2 = t.shape
         ok = t.stride() == (1, n1)
@@ -375,6 +375,15 @@ def weno5_advect(ctx, Tc_ex, Vx, Vy, Vz, dt, _dx, _dy, _dz, bc_type6, bc_val6, v
     nx, ny, nz = _cells_ex(Tc_ex, "Tc_ex"); S = _shapes(nx, ny, nz)
     ctx.call("ht3d_weno5_advect", _ptr(Tc_ex, S["ex"]), _ptr(Vx, S["fx"]), _ptr(Vy, S["fy"]), _ptr(Vz, S["fz"]), dt,
              _dx, _dy, _dz, abi.int6(*bc_type6), abi.dbl6(*bc_val6), variant, precision, nx, ny, nz)
+
+
+def weno5_advect_f32(ctx, Tc_ex, Vx, Vy, Vz, dt, _dx, _dy, _dz, bc_type6, bc_val6, variant=abi.WENO_V1):
+    """FP32 fused sweep (float32 fields of the same shapes)."""
+    nx, ny, nz = _cells_ex(Tc_ex, "Tc_ex"); S = _shapes(nx, ny, nz)
+    f = torch.float32
+    ctx.call("ht3d_weno5_advect_f32", _ptr(Tc_ex, S["ex"], "Tc_ex", f), _ptr(Vx, S["fx"], "Vx", f),
+             _ptr(Vy, S["fy"], "Vy", f), _ptr(Vz, S["fz"], "Vz", f), dt, _dx, _dy, _dz, abi.int6(*bc_type6),
+             abi.dbl6(*bc_val6), variant, nx, ny, nz)
 
 
 # ------------------------------------------------------ fused solver / step

@@ -97,6 +97,54 @@ def ensemble(n_members=64, seed=4, nmin=31, nmax=95, ra=(100.0, 5000.0), log10k_
     return out
 
 
+def lognormal_torch(shape, sigma=0.25, corr_cells=4.0, seed=5, device="cuda"):
+    """10**g with g ~ N(0, sigma) correlated by a Gaussian of corr_cells cells:
+    white noise filtered in Fourier space (torch, FP64, on `device`) and
+    normalised to zero mean and unit variance before scaling."""
+    import torch
+    gen = torch.Generator(device=device)
+    gen.manual_seed(seed)
+    w = torch.randn(shape, generator=gen, dtype=torch.float64, device=device)
+    k2 = 0.0
+    for ax, n in enumerate(shape):
+        f = torch.fft.fftfreq(n, dtype=torch.float64, device=device) * 2 * np.pi  # per cell
+        sh = [1] * len(shape)
+        sh[ax] = n
+        k2 = k2 + f.reshape(sh) ** 2
+    g = torch.fft.ifftn(torch.fft.fftn(w) * torch.exp(-k2 * corr_cells ** 2 / 4.0)).real
+    del w
+    g = (g - g.mean()) / g.std()
+    return torch.pow(10.0, sigma * g)
+
+
+def fault_slab_case(n=511, seed=5, Ra=1000.0, slab_factor=10.0, slab_cells=3, log10k_sigma=0.25, corr_cells=4.0,
+                    dt_max=1e-3, device="cuda", **kw):
+    """Large-grid HRL case: n^3 cells, log-normal background permeability
+    (log10 k ~ N(0, log10k_sigma), Gaussian correlation of corr_cells cells),
+    a vertical slab slab_cells cells wide at mid-x whose permeability is
+    multiplied by slab_factor, and the HRL initial condition (perturbation
+    amplitude 1e-3).  Built on `device`; returns column-major tensors
+    (Tc_ex, Pc_ex, ktv, kfv) and the HrlParams."""
+    import torch
+    from . import api
+    nx = ny = nz = n
+    kw_t = dict(dtype=torch.float64, device=device)
+    dy = 1.0 / ny
+    yce = torch.arange(ny + 2, **kw_t) * dy - 0.5 * dy
+    T = api.zeros(nx + 2, ny + 2, nz + 2, device=device)
+    T.copy_((1.0 - yce)[None, :, None].expand(nx + 2, ny + 2, nz + 2))
+    gen = torch.Generator(device=device)
+    gen.manual_seed(seed + 1)
+    T[1:-1, 1:-1, 1:-1] += (torch.rand((nx, ny, nz), generator=gen, **kw_t) * 2.0 - 1.0) * 1e-3
+    P = api.zeros(nx + 2, ny + 2, nz + 2, device=device)
+    ktv = api.ones(nx + 1, ny + 1, nz + 1, device=device)
+    kfv = api.zeros(nx + 1, ny + 1, nz + 1, device=device)
+    kfv.copy_(lognormal_torch((nx + 1, ny + 1, nz + 1), log10k_sigma, corr_cells, seed, device))
+    c0 = nx // 2 - slab_cells // 2  # first slab cell; its vertices c0 .. c0 + slab_cells
+    kfv[c0:c0 + slab_cells + 1] *= slab_factor
+    return T, P, ktv, kfv, params(nx, ny, nz, Ra=Ra, dt_max=dt_max, **kw)
+
+
 def bytes_per_iteration(nx, ny, nz, s):
     """Algorithmic bytes of one dimensionless DYREL pseudo-iteration:
     update {X, F0} (read+write) and read {kx, ky, kz, R, PC}: 9*N*s."""

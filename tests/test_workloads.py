@@ -37,3 +37,30 @@ def test_dt_max_caps_the_adapted_dt(orc):
         assert s == 0
         dts.append(p.dt)
     assert dts[0] > 1e-5 and dts[1] == 1e-5
+
+
+def test_curl_velocity_is_discretely_divergence_free():
+    import torch
+    from hydrothermal3d_gb300 import sweep
+    for n in ((12, 9, 7), (16, 16, 16)):
+        V = sweep.curl_velocity(*n, seed=6, device="cpu")
+        assert V[0].shape == (n[0] + 1, n[1], n[2]) and V[0].stride() == (1, n[0] + 1, (n[0] + 1) * n[1])
+        assert float(sweep.divergence(*V).abs().max()) < 1e-12 * max(n)
+        assert abs(max(float(v.abs().max()) for v in V) - 1.0) < 1e-14
+        # no flow through the walls
+        assert float(V[0][0].abs().max()) < 1e-14 and float(V[0][-1].abs().max()) < 1e-13
+        assert float(V[1][:, 0].abs().max()) < 1e-14 and float(V[2][:, :, -1].abs().max()) < 1e-13
+    a = sweep.curl_velocity(8, 8, 8, seed=6, device="cpu")[1]
+    b = sweep.curl_velocity(8, 8, 8, seed=6, device="cpu")[1]
+    assert torch.equal(a, b)
+
+
+def test_fault_slab_case():
+    import torch
+    T, P, ktv, kfv, p = hrl.fault_slab_case(n=21, device="cpu")
+    assert T.shape == (23, 23, 23) and kfv.shape == (22, 22, 22) and p.dt_max == 1e-3
+    ratio = float(kfv[9:13].mean() / torch.cat([kfv[:8], kfv[14:]]).mean())
+    assert 5.0 < ratio < 20.0  # the x10 slab over a log-normal background
+    assert abs(float(torch.log10(kfv[:8]).std()) - 0.25) < 0.08
+    inner = T[1:-1, 1:-1, 1:-1]
+    assert float(inner.max()) <= 1.0 + 1e-3 and float(inner.min()) >= -1e-3
