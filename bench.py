@@ -346,18 +346,20 @@ def roofline(ctx, stream, n, inner, step_ms, iters=20):
     import torch
     import hydrothermal3d_gb300 as ht
     from hydrothermal3d_gb300 import abi, hrl
-    inner_ms, inner_launches = inner
-    t = inner_ms / 1e3 / max(1, inner_launches)
+    inner_ms, inner_iters = inner
+    t = inner_ms / 1e3 / max(1, inner_iters)  # per pseudo-iteration
     alg = hrl.bytes_per_iteration(n, n, n, 4)
     peak = measured_peak()
     achieved = alg / t / 1e9
-    res = {"kernel": "k_mixed_inner (FP32 pseudo-iteration of the mixed form)", "bound": "hbm",
+    res = {"kernel": "k_mixed_inner (FP32 pseudo-iteration of the mixed form, padded float4 layout)", "bound": "hbm",
            "achieved": achieved, "peak": peak[0], "unit": "GB/s", "frac": achieved / peak[0], "peak_source": peak[1],
-           "traffic": profile_traffic("mixed_inner_f32"), "us_per_launch": t * 1e6,
-           "alg_bytes_per_launch": alg, "launches_timed": inner_launches,
+           "traffic": profile_traffic("mixed_inner_f32"), "traffic_unit": "DRAM bytes per pseudo-iteration",
+           "us_per_iteration": t * 1e6, "alg_bytes_per_iteration": alg, "iterations_timed": inner_iters,
            "share_of_timed_region": inner_ms / step_ms if step_ms else None,
            "timing": "CUDA events on the ctx stream around every run of consecutive inner launches inside the "
-                     "timed steps (HT3D_TUNE_TIME_INNER)"}
+                     "timed steps (HT3D_TUNE_TIME_INNER)",
+           "note": "the kernel streams 8 of the 9 algorithmic fields (the Jacobi diagonal is recomputed), so "
+                   "achieved can exceed the DRAM rate by up to 9/8; traffic is the measured DRAM bytes"}
     X64c = ht.zeros(n + 2, n + 2, n + 2).uniform_(0, 1)
     R64c = ht.zeros(n, n, n).uniform_(-1, 1)
     k64c = [ht.ones(n + 1, n, n), ht.ones(n, n + 1, n), ht.ones(n, n, n + 1)]
@@ -560,12 +562,13 @@ def measured_peak():
 
 
 def profile_traffic(name):
-    """DRAM bytes per launch from the committed ncu summary, if one exists."""
+    """DRAM bytes per pseudo-iteration at 255^3 from the committed ncu summary
+    (a line 'traffic_bytes_per_iteration_at_255: B'), if one exists."""
     p = os.path.join(ROOT, "profiles", f"{name}.md")
     try:
         with open(p) as f:
             for line in f:
-                if line.startswith("traffic_bytes_per_launch_at_255:"):
+                if line.startswith("traffic_bytes_per_iteration_at_255:"):
                     return float(line.split(":", 1)[1].split()[0])
     except Exception:
         pass

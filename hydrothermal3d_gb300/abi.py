@@ -12,6 +12,7 @@ TUNE_MIXED_REFRESH = 2
 TUNE_TIME_INNER = 3
 TUNE_ENS_BLOCK = 4
 TUNE_ENS_GRAPH = 5
+TUNE_TEMPORAL = 6
 DYREL_ZMARCH, DYREL_CELL = 1, 2
 
 

@@ -211,6 +211,33 @@ __global__ void k_dyrel_setup(const double* __restrict__ kx, const double* __res
         partials[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = v[0];
 }
 
+// The same bound for the mixed form, with reciprocal multiplications instead
+// of the reference's thirteen divisions (GB300's FP64 divide is slow; the mixed
+// form does not reproduce the FP64 form's rounding): diag = sum k/dx^2 + cdiag,
+// invPC = 1/diag and the per-block max of G/diag.
+__global__ void k_dyrel_setup_fast(const double* __restrict__ kx, const double* __restrict__ ky,
+                                   const double* __restrict__ kz, double cdiag, double _dx2, double _dy2, double _dz2,
+                                   int nx, int ny, int nz, double* __restrict__ invPC, double* __restrict__ partials) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    double v[1] = {-INFINITY};
+    if (i < nx && j < ny && k < nz) {
+        const double kW = kx[ix3(i, j, k, nx + 1, ny)], kE = kx[ix3(i + 1, j, k, nx + 1, ny)];
+        const double kS = ky[ix3(i, j, k, nx, ny + 1)], kN = ky[ix3(i, j + 1, k, nx, ny + 1)];
+        const double kB = kz[ix3(i, j, k, nx, ny)], kF = kz[ix3(i, j, k + 1, nx, ny)];
+        const double diag = (kB + kF) * _dz2 + (kN + kS) * _dy2 + (kE + kW) * _dx2 + cdiag;
+        const double g = (fabs(kE) + fabs(kW)) * _dx2 + (fabs(kN) + fabs(kS)) * _dy2 + (fabs(kB) + fabs(kF)) * _dz2 +
+                         fabs(diag);
+        const double inv = 1.0 / diag;
+        invPC[ix3(i, j, k, nx, ny)] = inv;
+        v[0] = g * inv;
+    }
+    block_reduce<RED_MAX, 1>(v);
+    if (threadIdx.x == 0 && threadIdx.y == 0)
+        partials[blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z)] = v[0];
+}
+
 // copy inner cells + face ghosts (not edges/corners) of a ghosted field
 template <typename T>
 __global__ void k_copy_ex_faces(T* __restrict__ dst, const T* __restrict__ src, int nx, int ny, int nz) {

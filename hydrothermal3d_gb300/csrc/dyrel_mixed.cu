@@ -67,6 +67,37 @@ __device__ __forceinline__ float c4(const float4& v, int m) {
     return m == 0 ? v.x : (m == 1 ? v.y : (m == 2 ? v.z : v.w));
 }
 
+// One cell of the FP32 inner iteration (the single place its arithmetic is
+// written, so every kernel that updates a cell rounds alike):
+//     F = (R + cX x + div q(x)) / diag,  F0' = h1 F0 + h2 F,  x' = x - dtau F0'
+// with q = -k dx on the six faces and diag = sum of k/dx^2 over them + cX.
+// Every operation is an explicit round-to-nearest intrinsic: the compiler may
+// neither contract nor reassociate them, so the value of a cell does not depend
+// on the kernel it is inlined into (k_mixed_inner shares fluxes between the
+// four cells of a quad, k_mixed_inner2 does not).
+__device__ __forceinline__ void mixed_cell(float xc, float xw, float xe, float xs, float xn, float xb, float xf,
+                                           float kW, float kE, float kS, float kN, float kB, float kF, float r,
+                                           float f0old, float h1, float h2, float dtau, float cX, float _dx, float _dy,
+                                           float _dz, float _dx2, float _dy2, float _dz2, float& f, float& f0,
+                                           float& xnew) {
+    const float qW = -__fmul_rn(kW, __fmul_rn(_dx, __fsub_rn(xc, xw)));
+    const float qE = -__fmul_rn(kE, __fmul_rn(_dx, __fsub_rn(xe, xc)));
+    const float qS = -__fmul_rn(kS, __fmul_rn(_dy, __fsub_rn(xc, xs)));
+    const float qN = -__fmul_rn(kN, __fmul_rn(_dy, __fsub_rn(xn, xc)));
+    const float qB = -__fmul_rn(kB, __fmul_rn(_dz, __fsub_rn(xc, xb)));
+    const float qF = -__fmul_rn(kF, __fmul_rn(_dz, __fsub_rn(xf, xc)));
+    float fu = __fmaf_rn(cX, xc, r);
+    fu = __fmaf_rn(_dx, __fsub_rn(qE, qW), fu);
+    fu = __fmaf_rn(_dy, __fsub_rn(qN, qS), fu);
+    fu = __fmaf_rn(_dz, __fsub_rn(qF, qB), fu);
+    float diag = __fmaf_rn(__fadd_rn(kW, kE), _dx2, cX);
+    diag = __fmaf_rn(__fadd_rn(kS, kN), _dy2, diag);
+    diag = __fmaf_rn(__fadd_rn(kB, kF), _dz2, diag);
+    f = __fdividef(fu, diag);
+    f0 = __fmaf_rn(h1, f0old, __fmul_rn(h2, f));
+    xnew = __fmaf_rn(-dtau, f0, xc);
+}
+
 // FP32 inner iteration of the mixed solver on the padded layout, for the
 // quad of cells 4q..4q+3 of row j, plane k (t = q + nq*j is the thread's
 // position in the plane).  Every field moves with 16-byte loads; the
@@ -114,7 +145,7 @@ __device__ __forceinline__ void mixed_quad(const float* __restrict__ Din, float*
     if (i0 + 4 < p.nx) dE = lane < 31 ? dE_sh : Din[base + 4];
     if (i0 + 3 < p.nx) kE3 = (lane < 31 && q < p.nq - 1) ? kE_sh : kx[base + 4];
     const float h1 = s.h1, h2 = s.h2, dtau = s.dtau, cX = s.cX, _dx = s._dx, _dy = s._dy, _dz = s._dz;
-    const float _dx2 = _dx * _dx, _dy2 = _dy * _dy, _dz2 = _dz * _dz;
+    const float _dx2 = __fmul_rn(_dx, _dx), _dy2 = __fmul_rn(_dy, _dy), _dz2 = __fmul_rn(_dz, _dz);
     float outD[4], outF0[4], outF[4];
 #pragma unroll
     for (int m = 0; m < 4; ++m) {
@@ -128,19 +159,12 @@ __device__ __forceinline__ void mixed_quad(const float* __restrict__ Din, float*
         const float xf = front ? c4(dF, m) : ghost(bc, 5, xc);
         const float kW = c4(kx4, m), kE = m == 3 ? kE3 : c4(kx4, m + 1);
         const float kS = c4(kyS, m), kN = c4(kyN, m), kB = c4(kzB, m), kF = c4(kzF, m);
-        const float qW = -kW * (_dx * (xc - xw));
-        const float qE = -kE * (_dx * (xe - xc));
-        const float qS = -kS * (_dy * (xc - xs));
-        const float qN = -kN * (_dy * (xn - xc));
-        const float qB = -kB * (_dz * (xc - xb));
-        const float qF = -kF * (_dz * (xf - xc));
-        const float fu = c4(r4, m) + cX * xc + _dx * (qE - qW) + _dy * (qN - qS) + _dz * (qF - qB);
-        const float diag = (kW + kE) * _dx2 + (kS + kN) * _dy2 + (kB + kF) * _dz2 + cX;
-        const float f = __fdividef(fu, diag);
-        const float f0 = h1 * c4(f04, m) + h2 * f;
+        float f, f0, xn1;
+        mixed_cell(xc, xw, xe, xs, xn, xb, xf, kW, kE, kS, kN, kB, kF, c4(r4, m), c4(f04, m), h1, h2, dtau, cX, _dx, _dy,
+                   _dz, _dx2, _dy2, _dz2, f, f0, xn1);
         const bool valid = i < p.nx;
         outF0[m] = valid ? f0 : 0.f;
-        outD[m] = valid ? xc - dtau * f0 : 0.f;
+        outD[m] = valid ? xn1 : 0.f;
         outF[m] = valid ? f : 0.f;
     }
     if (!act) return;
@@ -159,6 +183,169 @@ __global__ void __launch_bounds__(256, 4) k_mixed_inner(const float* __restrict_
     mixed_quad<STOREF>(Din, Dout, Rin, kx, ky, kz, F0, F, s, bc, p, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y,
                        threadIdx.x & 31);
 }
+
+// ---------------------------------------------------------------------------
+// Two inner iterations per pass (temporal blocking).  A CTA owns a column tile
+// of TB_X x TB_Y cells (its "halo tile") whose inner (TB_X-2) x (TB_Y-2) cells
+// it updates twice, marching through a chunk of zchunk planes:
+//   A: iteration n on every cell of the halo tile, plane p;
+//   B: iteration n+1 on the inner cells of plane p-1 from D' planes p-2
+//      (register), p-1 (shared), p (register).
+// Halo cells (one ring in x and y, one plane before and after the chunk) are
+// computed by both neighbouring CTAs.  Every field is read once per pass and
+// D, F0 are written once: half the traffic of two single iterations.  F0 is
+// ping-ponged (the halo reads neighbouring cells' F0).  Both iterations use
+// mixed_cell, so the result is bit-identical to two k_mixed_inner launches.
+//
+// The inputs of plane p (D over the tile plus one ring, kx, ky, kz, Rin, F0)
+// are staged in shared memory by cp.async two planes ahead (a ring of
+// TB_STAGES planes), so the loads of later planes are in flight while plane p
+// is computed.  Elements outside the grid are zero-filled by the copy.
+// ---------------------------------------------------------------------------
+constexpr int TB_X = 32, TB_Y = 16, TB_STAGES = 3;
+constexpr int TB_DX = TB_X + 2, TB_DY = TB_Y + 2;  // D tile with its ring
+
+struct TbStage {
+    float D[TB_DY][TB_DX];
+    float kx[TB_Y][TB_X + 1];  // west faces of the tile's columns + the last east face
+    float ky[TB_Y + 1][TB_X];  // south faces of the tile's rows + the last north face
+    float kz[TB_Y][TB_X];      // bottom faces of plane p
+    float R[TB_Y][TB_X];
+    float F0[TB_Y][TB_X];
+};
+
+__device__ __forceinline__ void cp_async4(float* smem, const float* gmem, bool valid) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem), "r"(valid ? 4 : 0));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::); }
+
+template <bool STOREF>
+__global__ void __launch_bounds__(TB_X* TB_Y, 2) k_mixed_inner2(const float* __restrict__ Din, float* __restrict__ Dout,
+                                                                const float* __restrict__ Rin,
+                                                                const float* __restrict__ kx,
+                                                                const float* __restrict__ ky,
+                                                                const float* __restrict__ kz,
+                                                                const float* __restrict__ F0in,
+                                                                float* __restrict__ F0out, float* __restrict__ F,
+                                                                DyrelScalT<float> s, BC6<float> bc, Pad p, int zchunk) {
+    extern __shared__ __align__(16) unsigned char tb_smem[];
+    TbStage* st = reinterpret_cast<TbStage*>(tb_smem);
+    float(*Dp)[TB_Y][TB_X] = reinterpret_cast<float(*)[TB_Y][TB_X]>(tb_smem + sizeof(TbStage) * TB_STAGES);
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + TB_X * ty;
+    constexpr int NT = TB_X * TB_Y;
+    const int x0 = blockIdx.x * (TB_X - 2) - 1, y0 = blockIdx.y * (TB_Y - 2) - 1;  // halo tile origin
+    const int gi = x0 + tx, gj = y0 + ty;
+    const bool in = gi >= 0 && gi < p.nx && gj >= 0 && gj < p.ny;
+    const bool inner = in && tx >= 1 && tx <= TB_X - 2 && ty >= 1 && ty <= TB_Y - 2;
+    const int k0 = blockIdx.z * zchunk, k1 = min(p.nz, k0 + zchunk);
+    const int pa0 = max(k0 - 1, 0);
+    const int plast = min(k1 + 1, p.nz);  // last staged plane (plane nz: its bottom z-faces only)
+    const float h1 = s.h1, h2 = s.h2, dtau = s.dtau, cX = s.cX, _dx = s._dx, _dy = s._dy, _dz = s._dz;
+    const float _dx2 = __fmul_rn(_dx, _dx), _dy2 = __fmul_rn(_dy, _dy), _dz2 = __fmul_rn(_dz, _dz);
+    // this thread's copy assignments (in-plane offsets and validity; fixed over planes)
+    int dOff[2], kxOff[2], kyOff[2];
+    bool dOk[2], kxOk[2], kyOk[2];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int e = tid + r * NT;
+        {
+            const int c = e % TB_DX, rr = e / TB_DX, xi = x0 - 1 + c, yj = y0 - 1 + rr;
+            dOk[r] = e < TB_DX * TB_DY && xi >= 0 && xi < p.nx && yj >= 0 && yj < p.ny;
+            dOff[r] = dOk[r] ? xi + p.PX * yj : 0;
+        }
+        {
+            const int c = e % (TB_X + 1), rr = e / (TB_X + 1), xi = x0 + c, yj = y0 + rr;
+            kxOk[r] = e < (TB_X + 1) * TB_Y && xi >= 0 && xi <= p.nx && yj >= 0 && yj < p.ny;
+            kxOff[r] = kxOk[r] ? xi + p.PX * yj : 0;
+        }
+        {
+            const int c = e % TB_X, rr = e / TB_X, xi = x0 + c, yj = y0 + rr;
+            kyOk[r] = e < TB_X * (TB_Y + 1) && xi >= 0 && xi < p.nx && yj >= 0 && yj <= p.ny;
+            kyOff[r] = kyOk[r] ? xi + p.PX * yj : 0;
+        }
+    }
+    const int cOff = in ? gi + p.PX * gj : 0;
+    // stage the inputs of plane k into ring slot k % TB_STAGES
+    auto stage = [&](int k) {
+        TbStage& S = st[k % TB_STAGES];
+        const long long pb = p.plane * k;
+        const bool full = k < p.nz;  // plane nz: z-faces only
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            const int e = tid + r * NT;
+            if (e < TB_DX * TB_DY) cp_async4(&S.D[0][0] + e, Din + pb + dOff[r], full && dOk[r]);
+            if (e < (TB_X + 1) * TB_Y) cp_async4(&S.kx[0][0] + e, kx + pb + kxOff[r], full && kxOk[r]);
+            if (e < TB_X * (TB_Y + 1)) cp_async4(&S.ky[0][0] + e, ky + pb + kyOff[r], full && kyOk[r]);
+        }
+        cp_async4(&S.kz[ty][tx], kz + pb + cOff, in);
+        cp_async4(&S.R[ty][tx], Rin + pb + cOff, full && in);
+        cp_async4(&S.F0[ty][tx], F0in + pb + cOff, full && in);
+    };
+    stage(pa0);
+    cp_async_commit();
+    if (pa0 + 1 <= plast) stage(pa0 + 1);
+    cp_async_commit();
+    float dm1 = (pa0 > 0 && in) ? Din[p.plane * (pa0 - 1) + cOff] : 0.f;  // D(p-1) of this column
+    // D' of planes q-1 and q for B, and the coefficients of plane q = p-1
+    float dpm = 0.f, dpc = 0.f;
+    float cW = 0.f, cE = 0.f, cS = 0.f, cN = 0.f, cB = 0.f, cF = 0.f, cr = 0.f, cf0 = 0.f;
+    for (int pl = pa0; pl <= k1; ++pl) {
+        if (pl + 2 <= plast) stage(pl + 2);
+        cp_async_commit();
+        cp_async_wait1();  // planes pl and pl + 1 have landed (this thread's copies)
+        __syncthreads();
+        float da = 0.f, aW = 0.f, aE = 0.f, aS = 0.f, aN = 0.f, aB = 0.f, aF = 0.f, ar = 0.f, af0 = 0.f;
+        if (pl < p.nz) {
+            const TbStage& S = st[pl % TB_STAGES];
+            const TbStage& S1 = st[(pl + 1) % TB_STAGES];
+            aW = S.kx[ty][tx];
+            aE = S.kx[ty][tx + 1];
+            aS = S.ky[ty][tx];
+            aN = S.ky[ty + 1][tx];
+            aB = S.kz[ty][tx];
+            aF = S1.kz[ty][tx];
+            ar = S.R[ty][tx];
+            const float f0o = S.F0[ty][tx];
+            const float xc = S.D[ty + 1][tx + 1];
+            const float xw = (gi == 0) ? ghost(bc, 0, xc) : S.D[ty + 1][tx];
+            const float xe = (gi == p.nx - 1) ? ghost(bc, 1, xc) : S.D[ty + 1][tx + 2];
+            const float xs = (gj == 0) ? ghost(bc, 2, xc) : S.D[ty][tx + 1];
+            const float xn = (gj == p.ny - 1) ? ghost(bc, 3, xc) : S.D[ty + 2][tx + 1];
+            const float xb = (pl == 0) ? ghost(bc, 4, xc) : dm1;
+            const float xf = (pl == p.nz - 1) ? ghost(bc, 5, xc) : S1.D[ty + 1][tx + 1];
+            float f;
+            mixed_cell(xc, xw, xe, xs, xn, xb, xf, aW, aE, aS, aN, aB, aF, ar, f0o, h1, h2, dtau, cX, _dx, _dy, _dz,
+                       _dx2, _dy2, _dz2, f, af0, da);
+            dm1 = xc;
+            Dp[pl & 1][ty][tx] = da;
+        }
+        __syncthreads();
+        const int q = pl - 1;
+        if (q >= k0 && inner) {
+            const float xc = dpc;
+            const float xw = (gi == 0) ? ghost(bc, 0, xc) : Dp[q & 1][ty][tx - 1];
+            const float xe = (gi == p.nx - 1) ? ghost(bc, 1, xc) : Dp[q & 1][ty][tx + 1];
+            const float xs = (gj == 0) ? ghost(bc, 2, xc) : Dp[q & 1][ty - 1][tx];
+            const float xn = (gj == p.ny - 1) ? ghost(bc, 3, xc) : Dp[q & 1][ty + 1][tx];
+            const float xb = (q == 0) ? ghost(bc, 4, xc) : dpm;
+            const float xf = (q == p.nz - 1) ? ghost(bc, 5, xc) : da;
+            float f, f0, xn1;
+            mixed_cell(xc, xw, xe, xs, xn, xb, xf, cW, cE, cS, cN, cB, cF, cr, cf0, h1, h2, dtau, cX, _dx, _dy, _dz,
+                       _dx2, _dy2, _dz2, f, f0, xn1);
+            const long long e = p.plane * q + cOff;
+            Dout[e] = xn1;
+            F0out[e] = f0;
+            if (STOREF) F[e] = f;
+        }
+        dpm = dpc;
+        dpc = da;
+        cW = aW; cE = aE; cS = aS; cN = aN; cB = aB; cF = aF; cr = ar; cf0 = af0;
+    }
+    asm volatile("cp.async.wait_group 0;\n" ::);
+}
+constexpr size_t kTbSmem = sizeof(TbStage) * TB_STAGES + sizeof(float) * 2 * TB_Y * TB_X;
 
 // ---------------------------------------------------------------------------
 // Batched inner iteration over an ensemble of independent instances.  One
@@ -336,7 +523,7 @@ struct InnerTimer {
         HT3D_CUDA(cudaEventRecord(ctx->events[2 * pairs], ctx->stream));
         open = true;
     }
-    void count() { if (on) ++launches; }
+    void count(int iterations = 1) { if (on) launches += iterations; }
     void end() {
         if (!on || !open) return;
         HT3D_CUDA(cudaEventRecord(ctx->events[2 * pairs + 1], ctx->stream));
@@ -373,7 +560,8 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
     double* X2 = (double*)ht3d_scratch(ctx, SLOT_X2, sizeof(double) * nex);
     float* Da = (float*)ht3d_scratch(ctx, SLOT_F32_X, pbytes);
     float* Db = (float*)ht3d_scratch(ctx, SLOT_F32_X2, pbytes);
-    float* F0s = (float*)ht3d_scratch(ctx, SLOT_F32_F0, pbytes);
+    float* F0a = (float*)ht3d_scratch(ctx, SLOT_F32_F0, pbytes);
+    float* F0b = (float*)ht3d_scratch(ctx, SLOT_F32_F0B, pbytes);
     float* Fs = (float*)ht3d_scratch(ctx, SLOT_F32_F, pbytes);
     float* Rin = (float*)ht3d_scratch(ctx, SLOT_F32_R, pbytes);
     float* kx32 = (float*)ht3d_scratch(ctx, SLOT_F32_KX, pbytes);
@@ -393,12 +581,11 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
         bch.val2[f] = 0.0f;
     }
     const dim3 b2(32, 8, 1), gc((nx + 31) / 32, (ny + 7) / 8, nz);
-    {
-        const double transient = cX != 0.0 ? 1.0 : 0.0, dt = cX != 0.0 ? 1.0 / cX : 1.0;
-        HT3D_LAUNCH(ctx, k_dyrel_setup<1>, gc, b2, 0, kx, ky, kz, 1.0, transient, dt, dx, dy, dz, nx, ny, nz, invPC, parts);
-        HT3D_LAUNCH(ctx, (k_reduce_partials<RED_MAX, 1>), 1, 1024, 0, parts, (int)(gc.x * gc.y * gc.z), dres);
-    }
-    for (float* a : {Da, Db, F0s, Fs, Rin, kx32, ky32, kz32}) HT3D_CUDA(cudaMemsetAsync(a, 0, pbytes, ctx->stream));
+    HT3D_LAUNCH(ctx, k_dyrel_setup_fast, gc, b2, 0, kx, ky, kz, cX, 1.0 / (dx * dx), 1.0 / (dy * dy), 1.0 / (dz * dz),
+                nx, ny, nz, invPC, parts);
+    HT3D_LAUNCH(ctx, (k_reduce_partials<RED_MAX, 1>), 1, 1024, 0, parts, (int)(gc.x * gc.y * gc.z), dres);
+    for (float* a : {Da, Db, F0a, F0b, Fs, Rin, kx32, ky32, kz32})
+        HT3D_CUDA(cudaMemsetAsync(a, 0, pbytes, ctx->stream));
     HT3D_LAUNCH(ctx, k_pack, dim3((nx + 1 + 31) / 32, (ny + 7) / 8, nz), b2, 0, kx32, kx, nx + 1, ny, nz, P);
     HT3D_LAUNCH(ctx, k_pack, dim3((nx + 31) / 32, (ny + 1 + 7) / 8, nz), b2, 0, ky32, ky, nx, ny + 1, nz, P);
     HT3D_LAUNCH(ctx, k_pack, dim3((nx + 31) / 32, (ny + 7) / 8, nz + 1), b2, 0, kz32, kz, nx, ny, nz + 1, P);
@@ -412,16 +599,32 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
     sc._dy = 1.0 / dy;
     sc._dz = 1.0 / dz;
     const dim3 ib(256), ig((unsigned)(((long long)P.nq * ny + 255) / 256), (unsigned)nz);
+    // two iterations per pass (k_mixed_inner2) inside runs of inner iterations
+    const bool pairs = ctx->mixed_temporal != 0;
+    int zc = ctx->mixed_temporal >= 2 ? ctx->mixed_temporal : 0;
+    const int tiles = ((nx + TB_X - 3) / (TB_X - 2)) * ((ny + TB_Y - 3) / (TB_Y - 2));
+    if (!zc) zc = (int)std::min<long long>(64, std::max<long long>(8, (long long)nz * tiles / (8LL * ctx->num_sms)));
+    const dim3 tb(TB_X, TB_Y), tg((nx + TB_X - 3) / (TB_X - 2), (ny + TB_Y - 3) / (TB_Y - 2), (nz + zc - 1) / zc);
+    if (pairs) {
+        static_assert(kTbSmem <= 227 * 1024, "staging ring exceeds the shared memory of a CTA");
+        HT3D_CUDA(cudaFuncSetAttribute(k_mixed_inner2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTbSmem));
+        HT3D_CUDA(cudaFuncSetAttribute(k_mixed_inner2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTbSmem));
+    }
     InnerTimer timer(ctx);
     double* xcur = X;
     double* xnxt = X2;
     float* dcur = Da;
     float* dnxt = Db;
+    float* f0cur = F0a;  // current FP32 momentum (k_mixed_inner2 writes the other buffer)
+    float* f0nxt = F0b;
     double nF_abs = 0., nF_rel = 0., nF_ini = 0.;
     int it_done = 0, converged = 0, status = HT3D_OK, checks = 0;
     bool last_fp64 = false;  // the last iteration ran the FP64 kernel (check or refresh)
     const int nmax = n_iter_fixed > 0 ? n_iter_fixed : prm->nitmax;
     const int refresh_every = ctx->mixed_refresh;
+    auto is_fp64 = [&](int it) {
+        return is_check(it, prm->nitout) || (refresh_every > 0 && it % refresh_every == 0);
+    };
     for (int iter = 1; iter <= nmax; ++iter) {
         const bool chk = is_check(iter, prm->nitout);
         // defect-correction refresh between the reference's checks: fold D into X
@@ -434,17 +637,39 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
         sc.dtau = S.dtau;
         if (chk || refresh) {
             timer.end();
-            HT3D_LAUNCH(ctx, k_mixed_check, LC.grid, LC.block, 0, xcur, xnxt, dcur, dnxt, R, kx, ky, kz, invPC, F0s, Fs,
-                        F, Rin, sc, bc, P, LC.zchunk, parts);
+            HT3D_LAUNCH(ctx, k_mixed_check, LC.grid, LC.block, 0, xcur, xnxt, dcur, dnxt, R, kx, ky, kz, invPC, f0cur,
+                        Fs, F, Rin, sc, bc, P, LC.zchunk, parts);
             std::swap(xcur, xnxt);
         } else {
             const DyrelScalT<float> s32(sc);
             timer.begin();
-            if (storef)
-                HT3D_LAUNCH(ctx, k_mixed_inner<true>, ig, ib, 0, dcur, dnxt, Rin, kx32, ky32, kz32, F0s, Fs, s32, bch, P);
-            else
-                HT3D_LAUNCH(ctx, k_mixed_inner<false>, ig, ib, 0, dcur, dnxt, Rin, kx32, ky32, kz32, F0s, Fs, s32, bch, P);
-            timer.count();
+            // this run of inner iterations ends at run_end; a run that ends the
+            // solve keeps its last iteration single (the final fold needs the
+            // correction before the last iteration)
+            int run_end = iter;
+            while (run_end < nmax && !is_fp64(run_end + 1)) ++run_end;
+            const int pair_end = run_end == nmax ? run_end - 1 : run_end;
+            const int left = pair_end - iter + 1;
+            if (pairs && left >= 2 && left % 2 == 0) {
+                const bool storef2 = iter + 1 == nmax || is_check(iter + 2, prm->nitout);
+                if (storef2)
+                    HT3D_LAUNCH(ctx, k_mixed_inner2<true>, tg, tb, kTbSmem, dcur, dnxt, Rin, kx32, ky32, kz32, f0cur,
+                                f0nxt, Fs, s32, bch, P, zc);
+                else
+                    HT3D_LAUNCH(ctx, k_mixed_inner2<false>, tg, tb, kTbSmem, dcur, dnxt, Rin, kx32, ky32, kz32, f0cur,
+                                f0nxt, Fs, s32, bch, P, zc);
+                std::swap(f0cur, f0nxt);
+                timer.count(2);
+                ++iter;  // the pass did iterations iter and iter + 1
+            } else {
+                if (storef)
+                    HT3D_LAUNCH(ctx, k_mixed_inner<true>, ig, ib, 0, dcur, dnxt, Rin, kx32, ky32, kz32, f0cur, Fs, s32,
+                                bch, P);
+                else
+                    HT3D_LAUNCH(ctx, k_mixed_inner<false>, ig, ib, 0, dcur, dnxt, Rin, kx32, ky32, kz32, f0cur, Fs, s32,
+                                bch, P);
+                timer.count();
+            }
         }
         std::swap(dcur, dnxt);
         it_done = iter;
@@ -475,7 +700,7 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
         dim3 g((nx + 2 + 31) / 32, (ny + 2 + 7) / 8, nz + 2);
         HT3D_LAUNCH(ctx, k_copy_ex_faces<double>, g, b2, 0, X, xcur, nx, ny, nz);
     }
-    HT3D_LAUNCH(ctx, k_unpack, gc, b2, 0, F0, F0s, P);
+    HT3D_LAUNCH(ctx, k_unpack, gc, b2, 0, F0, f0cur, P);
     if (!last_fp64) HT3D_LAUNCH(ctx, k_unpack, gc, b2, 0, F, Fs, P);
     timer.collect();
     if (st) {
@@ -661,9 +886,8 @@ void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
             h.bch.val2[f] = 0.0f;
         }
         const dim3 gc((nx + 31) / 32, (ny + 7) / 8, nz);
-        const double transient = I.cX != 0.0 ? 1.0 : 0.0, dt = I.cX != 0.0 ? 1.0 / I.cX : 1.0;
-        HT3D_LAUNCH(ctx, k_dyrel_setup<1>, gc, b2, 0, I.kx, I.ky, I.kz, 1.0, transient, dt, I.dx, I.dy, I.dz, nx, ny, nz,
-                    h.invPC, parts);
+        HT3D_LAUNCH(ctx, k_dyrel_setup_fast, gc, b2, 0, I.kx, I.ky, I.kz, I.cX, 1.0 / (I.dx * I.dx),
+                    1.0 / (I.dy * I.dy), 1.0 / (I.dz * I.dz), nx, ny, nz, h.invPC, parts);
         HT3D_LAUNCH(ctx, (k_reduce_partials<RED_MAX, 1>), 1, 1024, 0, parts, (int)(gc.x * gc.y * gc.z), dres + q);
         const size_t pbytes = sizeof(float) * (size_t)h.P.size;
         for (float* a : h.f32) HT3D_CUDA(cudaMemsetAsync(a, 0, pbytes, ctx->stream));

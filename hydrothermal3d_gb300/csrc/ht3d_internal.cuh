@@ -25,7 +25,7 @@ enum ScratchSlot {
     SLOT_G,             // Gershgorin ratios
     SLOT_SNAP,          // pre-launch snapshot for in-place boundary kernels
     SLOT_F32_X, SLOT_F32_X2, SLOT_F32_F0, SLOT_F32_R, SLOT_F32_PC, SLOT_F32_KX, SLOT_F32_KY, SLOT_F32_KZ,
-    SLOT_F32_F,
+    SLOT_F32_F, SLOT_F32_F0B,
     SLOT_STEP_R, SLOT_STEP_F, SLOT_STEP_F0, SLOT_STEP_TY, SLOT_STEP_KX, SLOT_STEP_KY, SLOT_STEP_KZ,
     SLOT_WENO_T0, SLOT_WENO_T1, SLOT_WENO_T2, SLOT_WENO_V,
     SLOT_AUX0, SLOT_AUX1, SLOT_AUX2, SLOT_AUX3,
@@ -42,10 +42,11 @@ struct ht3d_ctx {
     int sync_each_call = 1;
     int dyrel_variant = 0;                // thread layout of the fused DYREL iteration (0 = per precision)
     int mixed_refresh = 256;              // FP64 defect-correction cadence of the mixed solver
+    int mixed_temporal = 0;               // mixed form: two inner iterations per pass (>= 2: z-chunk)
     int time_inner = 0;                   // time the mixed solver's inner-iteration runs
     std::vector<cudaEvent_t> events;      // event pool of the inner-iteration timer
     double inner_ms = 0.0;                // accumulated device time of the timed runs
-    unsigned long long inner_launches = 0;  // inner-iteration launches inside them
+    unsigned long long inner_launches = 0;  // inner iterations inside them
     // batched ensemble solve
     int ens_block = 0;                    // threads per block of the batched kernel (0 = autotune)
     int ens_graphs = 1;                   // replay windows of inner iterations as CUDA graphs

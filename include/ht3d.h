@@ -72,6 +72,13 @@ extern "C" {
                                        0 = autotune on first use (64/128/256), or fixed   */
 #define HT3D_TUNE_ENS_GRAPH 5       /* 1 (default): replay windows of 16 batched inner
                                        iterations as CUDA graphs; 0: launch one by one    */
+#define HT3D_TUNE_TEMPORAL 6        /* mixed form: 0 (default) = one FP32 inner iteration per
+                                       launch; 1 = two per pass through memory (temporal
+                                       blocking, z-chunk chosen per grid), >= 2 = the same
+                                       with that many planes per chunk; bit-identical
+                                       results (on GB300 the two-iteration pass is still
+                                       instruction-issue bound and slower: 135 vs 91 us
+                                       per iteration at 255^3)                          */
 
 typedef struct ht3d_ctx ht3d_ctx;
 
@@ -147,8 +154,9 @@ int ht3d_ctx_synchronize(ht3d_ctx* ctx);
 int ht3d_ctx_set_tuning(ht3d_ctx* ctx, int key, int value);
 /* number of CUDA kernels this ctx has launched (monotonic) */
 unsigned long long ht3d_ctx_launch_count(const ht3d_ctx* ctx);
-/* device time (ms) and launch count of the mixed solver's timed inner-iteration
-   runs since the last reset (HT3D_TUNE_TIME_INNER); reset != 0 clears them */
+/* device time (ms) and inner-iteration count of the mixed solver's timed
+   inner-iteration runs since the last reset (HT3D_TUNE_TIME_INNER); reset != 0
+   clears them */
 int ht3d_ctx_inner_timing(ht3d_ctx* ctx, double* ms, unsigned long long* launches, int reset);
 const char* ht3d_ctx_last_error(const ht3d_ctx* ctx);
 /* sizes of the parameter structs, for binding checks */

@@ -231,5 +231,41 @@ def test_mixed_fixed_iterations_track_fp64(ctx, orc, n, bc, niter):
     du_ref, du = (Xo - X)[inner], (ht.to_numpy(Xd) - X)[inner]
     assert rel_err(du, du_ref) <= 1e-4
     assert rel_err(ht.to_numpy(Xd), Xo, m) <= 1e-6
-    assert rel_err(ht.to_numpy(F0d), F0o) <= 1e-4
-    assert rel_err(ht.to_numpy(Fd), Fo) <= 1e-3
+    # F and F0 shrink as the iteration converges (to ~1e-7 on one cell):
+    # compare against the larger of their final size and 1e-3 of the first
+    # iteration's scale R*dx^2
+    fscale = max(np.abs(Fo).max(), np.abs(F0o).max(), 1e-3 * np.abs(R).max() * min(d) ** 2)
+    assert np.max(np.abs(ht.to_numpy(F0d) - F0o)) <= 1e-4 * fscale
+    assert np.max(np.abs(ht.to_numpy(Fd) - Fo)) <= 1e-3 * fscale
+
+
+@pytest.mark.parametrize("n", [(1, 1, 1), (2, 3, 2), (5, 4, 3), (30, 14, 9), (31, 15, 40), (64, 29, 33), (95, 47, 70)])
+@pytest.mark.parametrize("niter,refresh", [(40, 8), (37, 8), (25, 256), (100, 16)])
+@pytest.mark.parametrize("zchunk", [1, 2, 7])
+def test_mixed_temporal_blocking_is_bit_identical(ctx, n, niter, refresh, zchunk):
+    """k_mixed_inner2 (two iterations per pass through memory, with halo
+    recomputation across tiles and z-chunks) gives bit for bit the result of
+    one k_mixed_inner launch per iteration: X, F, F0 and the check sums."""
+    nx, ny, nz = n
+    X, R, k = problem(n, seed=37)
+    types, vals = BCS["mixedbc"]
+    prm = abi.DyrelParams.reference(nitout=10)
+    d = (1.0 / nx, 0.9 / ny, 1.2 / nz)
+    out = []
+    ctx.set_tuning(abi.TUNE_MIXED_REFRESH, refresh)
+    try:
+        for temporal in (0, zchunk):
+            ctx.set_tuning(abi.TUNE_TEMPORAL, temporal)
+            Xd, Fd, F0d = ht.from_numpy(X), ht.zeros(nx, ny, nz), ht.zeros(nx, ny, nz)
+            st = api.dyrel_solve_dimless(ctx, Xd, ht.from_numpy(R), *[ht.from_numpy(a) for a in k], 30.0, *d, types,
+                                         vals, prm, Fd, F0d, abi.MIXED, n_iter_fixed=niter)
+            out.append((ht.to_numpy(Xd), ht.to_numpy(Fd), ht.to_numpy(F0d), st.nF_abs, st.lambda_min, st.iters))
+    finally:
+        ctx.set_tuning(abi.TUNE_TEMPORAL, 0)
+        ctx.set_tuning(abi.TUNE_MIXED_REFRESH, 256)
+    a, b = out
+    m = no_edges_mask(X.shape)
+    np.testing.assert_array_equal(a[0][m], b[0][m])
+    np.testing.assert_array_equal(a[1], b[1])
+    np.testing.assert_array_equal(a[2], b[2])
+    assert a[3:] == b[3:]
