@@ -27,11 +27,16 @@ def main():
     ap.add_argument("--iters", type=int, default=5)
     ap.add_argument("--variant", type=int, default=0,
                     help="DYREL thread layout: 0 per precision, 1 z-march tiles, 2 one thread per cell")
+    ap.add_argument("--tune", action="append", default=[],
+                    help="KEY=VALUE context tuning (HT3D_TUNE_* number), repeatable")
     a = ap.parse_args()
     n = a.n
     stream = torch.cuda.Stream()
     ctx = ht.Context(device=0, stream=stream.cuda_stream)
     ctx.check(ctx.lib.ht3d_ctx_set_tuning(ctx.ptr, abi.TUNE_DYREL_VARIANT, a.variant))
+    for kv in a.tune:
+        key, val = (int(x) for x in kv.split("="))
+        ctx.set_tuning(key, val)
     d = 1.0 / n
     bt, bv = abi.int6(0, 0, 1, 1, 0, 0), abi.dbl6(0, 0, 1, 0, 0, 0)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -72,8 +77,8 @@ def main():
         ms, nl = ctx.inner_timing(reset=True)
         t = ms / 1e3 / max(1, nl)
         alg = hrl.bytes_per_iteration(n, n, n, 4)
-        print(json.dumps({"kernel": "k_mixed_inner", "n": n, "inner_launches": nl, "us_per_launch": t * 1e6,
-                          "alg_GBs": alg / t / 1e9}))
+        print(json.dumps({"kernel": "k_mixed_inner", "n": n, "tune": a.tune, "inner_iterations": nl,
+                          "us_per_iteration": t * 1e6, "alg_GBs": alg / t / 1e9}))
     else:
         prec = abi.FP64 if a.kernel == "weno_f64" else abi.MIXED
         T = ht.zeros(n + 2, n + 2, n + 2).uniform_(0, 1)
