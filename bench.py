@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--ens-steps", type=int, default=20)
     ap.add_argument("--skip-ensemble", action="store_true")
     ap.add_argument("--sweep-n", type=int, default=511, help="cells per axis of the standalone WENO5 sweep (0 = skip)")
+    ap.add_argument("--v18-steps", type=int, default=2,
+                    help="time steps of the 127^3 dimensional (v18) box, plain FP64 (0 = skip)")
     ap.add_argument("--fault-steps", type=int, default=0,
                     help="time steps of the 511^3 fault-slab HRL case (mixed form; 0 = skip)")
     return ap.parse_args()
@@ -295,6 +297,8 @@ def run_ours(a):
         out["weno_sweep"] = sweep_bench(ctx, stream, a.sweep_n)
     if a.fault_steps:
         out["fault_slab_511"] = fault_bench(ctx, stream, a)
+    if a.v18_steps:
+        out["dimensional_127"] = v18_bench(ctx, stream, a.v18_steps)
 
     if rank == 0:
         v, cores, desc, _ = cpu_sample(n, a.cpu_seconds, threads=os.cpu_count())
@@ -520,6 +524,40 @@ def sweep_bench(ctx, stream, n, reps=3):
                          "storage_bytes": s}
             del T
     return res
+
+
+def v18_bench(ctx, stream, steps, n=127):
+    """Dimensional model (ht3d_step_v18, plain FP64) on the 10 x 10 x 5 km box
+    at n^3: the steady initialisation step (it = 0) and the following steps
+    with pluton insertion and WENO5-v2 sub-stepping.  T_eff counts 10N*8+N
+    bytes per thermal and 11N*8+N per Darcy pseudo-iteration plus 21N*8 per
+    advection sub-step."""
+    import torch
+    import hydrothermal3d_gb300 as ht
+    from hydrothermal3d_gb300 import api, v18
+    b = v18.box(n, n, n, seed=2)
+    p = b["params"]
+    T, P = ht.from_numpy(b["T"]), ht.from_numpy(b["P"])
+    args = (ht.from_numpy(b["phc"]), ht.from_numpy(b["phv"]), ht.from_numpy(b["wN"]), ht.from_numpy(b["kmul"]))
+    V = [ht.zeros(n + 1, n, n), ht.zeros(n, n + 1, n), ht.zeros(n, n, n + 1)]
+    bt, bd = v18.bytes_per_iteration(n, n, n)
+    rows, nbytes = [], 0
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for it in range(steps):
+            p.it = it
+            gt, gd = api.step_v18(ctx, T, P, *args, *V, p)
+            rows.append({"it": it, "iters": [gt.iters, gd.iters], "advection_substeps": p.n_adv})
+            nbytes += gt.iters * bt + gd.iters * bd + p.n_adv * 21 * n ** 3 * 8
+        e1.record(stream)
+        torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / 1e3
+    return {"n": n, "steps": steps, "seconds": t, "time_steps_per_s": steps / t, "T_eff_GBs": nbytes / t / 1e9,
+            "per_step": rows, "dtype": "f64",
+            "case": "10x10x5 km box, T 600->20 C, log10 k ~ N(-15, 0.5) with 500 m correlation (seed 2), "
+                    "DYREL tol 1e-10 relative, nitmax 1e4, WENO5 v2 with the reference's stencil, CFL 0.5"}
 
 
 def fault_bench(ctx, stream, a):

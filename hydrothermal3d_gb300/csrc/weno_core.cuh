@@ -45,9 +45,10 @@ __device__ __forceinline__ float weno5_f32(float v1, float v2, float v3, float v
     const float s1 = (13.0f / 12.0f) * (a1 * a1) + 0.25f * (b1 * b1) + e;
     const float s2 = (13.0f / 12.0f) * (a2 * a2) + 0.25f * (b2 * b2) + e;
     const float s3 = (13.0f / 12.0f) * (a3 * a3) + 0.25f * (b3 * b3) + e;
-    const float w1 = 0.1f / (s1 * s1), w2 = 0.6f / (s2 * s2), w3 = 0.3f / (s3 * s3);
-    const float iw = 1.0f / (w1 + w2 + w3);
-    return (w1 * p1 + w2 * p2 + w3 * p3) * iw;
+    // approximate-reciprocal divisions (__fdividef, a few ulp): s >= 1e-18 keeps
+    // every divisor and the weight sum (<= ~1e36) inside its accurate range
+    const float w1 = __fdividef(0.1f, s1 * s1), w2 = __fdividef(0.6f, s2 * s2), w3 = __fdividef(0.3f, s3 * s3);
+    return __fdividef(w1 * p1 + w2 * p2 + w3 * p3, w1 + w2 + w3);
 }
 
 struct WenoBC {

@@ -63,7 +63,7 @@ extern "C" {
 #define HT3D_DYREL_ZMARCH 1         /*   32x8 column tiles marching in z              */
 #define HT3D_DYREL_CELL 2           /*   one thread per cell                          */
 #define HT3D_TUNE_MIXED_REFRESH 2   /* mixed form: FP64 defect-correction refresh every N
-                                       inner iterations between checks (default 256; 0 = only
+                                       inner iterations between checks (default 512; 0 = only
                                        at the reference's check iterations)             */
 #define HT3D_TUNE_TIME_INNER 3      /* 1: the mixed solver brackets every run of consecutive
                                        FP32 inner-iteration launches with CUDA events on the

@@ -57,7 +57,7 @@ def assert_same(a, b):
 def tuned(ctx):
     ctx.set_tuning(abi.TUNE_MIXED_REFRESH, 64)
     yield ctx
-    ctx.set_tuning(abi.TUNE_MIXED_REFRESH, 256)
+    ctx.set_tuning(abi.TUNE_MIXED_REFRESH, 512)
     ctx.set_tuning(abi.TUNE_ENS_BLOCK, 0)
     ctx.set_tuning(abi.TUNE_ENS_GRAPH, 1)
 

@@ -220,7 +220,7 @@ def test_mixed_fixed_iterations_track_fp64(ctx, orc, n, bc, niter):
                                       vals, prm, Fd, F0d, abi.MIXED, n_iter_fixed=niter)
         ms, launches = ctx.inner_timing(reset=True)
     finally:
-        ctx.set_tuning(abi.TUNE_MIXED_REFRESH, 256)
+        ctx.set_tuning(abi.TUNE_MIXED_REFRESH, 512)
         ctx.set_tuning(abi.TUNE_TIME_INNER, 0)
     assert so == 0 and std.status == 0 and std.iters == niter and std.checks == sto.checks
     # checks at 1, 2 and every 10th iteration, FP64 refreshes at every other 8th
@@ -262,7 +262,7 @@ def test_mixed_temporal_blocking_is_bit_identical(ctx, n, niter, refresh, zchunk
             out.append((ht.to_numpy(Xd), ht.to_numpy(Fd), ht.to_numpy(F0d), st.nF_abs, st.lambda_min, st.iters))
     finally:
         ctx.set_tuning(abi.TUNE_TEMPORAL, 0)
-        ctx.set_tuning(abi.TUNE_MIXED_REFRESH, 256)
+        ctx.set_tuning(abi.TUNE_MIXED_REFRESH, 512)
     a, b = out
     m = no_edges_mask(X.shape)
     np.testing.assert_array_equal(a[0][m], b[0][m])
