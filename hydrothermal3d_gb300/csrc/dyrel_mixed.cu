@@ -1,4 +1,8 @@
 // Mixed-precision DYREL solver (FP32 inner iterations, FP64 defect correction).
+#include <cuda.h>
+#include <cstddef>
+#include <mutex>
+
 #include "dyrel_common.cuh"
 #include "ensemble_internal.cuh"
 
@@ -198,123 +202,161 @@ __global__ void __launch_bounds__(256, 4) k_mixed_inner(const float* __restrict_
 // mixed_cell, so the result is bit-identical to two k_mixed_inner launches.
 //
 // The inputs of plane p (D over the tile plus one ring, kx, ky, kz, Rin, F0)
-// are staged in shared memory by cp.async two planes ahead (a ring of
-// TB_STAGES planes), so the loads of later planes are in flight while plane p
-// is computed.  Elements outside the grid are zero-filled by the copy.
+// are brought into shared memory by TMA tensor copies (one thread issues six
+// 3-D box loads per plane, completing on the plane's mbarrier) two planes
+// ahead, in a ring of TB_STAGES planes.  Boxes are TB_BW floats wide and start
+// on a 4-float boundary below the tile (TMA wants 16-byte aligned x); elements
+// outside the arrays are zero-filled.  Every mbarrier wait is bounded: on
+// timeout the CTA records HT3D_ERR_TIMEOUT in *err, waits (bounded) for its
+// copies in flight and returns.
 // ---------------------------------------------------------------------------
-constexpr int TB_X = 32, TB_Y = 16, TB_STAGES = 3;
-constexpr int TB_DX = TB_X + 2, TB_DY = TB_Y + 2;  // D tile with its ring
+constexpr int TB_X = 32, TB_Y = 16, TB_STAGES = 3, TB_BW = 40;
+constexpr unsigned kTbWaitLimit = 1u << 22;
 
-struct TbStage {
-    float D[TB_DY][TB_DX];
-    float kx[TB_Y][TB_X + 1];  // west faces of the tile's columns + the last east face
-    float ky[TB_Y + 1][TB_X];  // south faces of the tile's rows + the last north face
-    float kz[TB_Y][TB_X];      // bottom faces of plane p
-    float R[TB_Y][TB_X];
-    float F0[TB_Y][TB_X];
+struct __align__(128) TbStage {
+    float D[TB_Y + 2][TB_BW];   // rows y0-1 .. y0+TB_Y, columns xD .. xD+TB_BW-1
+    float pad0[(128 - ((TB_Y + 2) * TB_BW * 4) % 128) % 128 / 4];
+    float kx[TB_Y][TB_BW];      // rows y0 .. y0+TB_Y-1, columns xK ..
+    float ky[TB_Y + 1][TB_BW];  // rows y0 .. y0+TB_Y
+    float pad1[(128 - ((TB_Y + 1) * TB_BW * 4) % 128) % 128 / 4];
+    float kz[TB_Y][TB_BW];
+    float R[TB_Y][TB_BW];
+    float F0[TB_Y][TB_BW];
+};
+constexpr unsigned kTbStageBytes = 4u * TB_BW * ((TB_Y + 2) + 5 * TB_Y + 1);  // bytes the six boxes deliver
+static_assert(offsetof(TbStage, kx) % 128 == 0 && offsetof(TbStage, ky) % 128 == 0 &&
+                  offsetof(TbStage, kz) % 128 == 0 && offsetof(TbStage, R) % 128 == 0 &&
+                  offsetof(TbStage, F0) % 128 == 0 && sizeof(TbStage) % 128 == 0,
+              "TMA destinations must be 128-byte aligned");
+
+struct TbMaps {  // tensor maps of one pass (by value, in the constant bank)
+    CUtensorMap D, kx, ky, kz, R, F0;
 };
 
-__device__ __forceinline__ void cp_async4(float* smem, const float* gmem, bool valid) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem), "r"(valid ? 4 : 0));
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
+    for (unsigned it = 0; it < kTbWaitLimit; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void tma_load3(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::
+            "r"(smem_u32(dst)), "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
 
 template <bool STOREF>
-__global__ void __launch_bounds__(TB_X* TB_Y, 2) k_mixed_inner2(const float* __restrict__ Din, float* __restrict__ Dout,
-                                                                const float* __restrict__ Rin,
-                                                                const float* __restrict__ kx,
-                                                                const float* __restrict__ ky,
-                                                                const float* __restrict__ kz,
-                                                                const float* __restrict__ F0in,
+__global__ void __launch_bounds__(TB_X* TB_Y, 2) k_mixed_inner2(const __grid_constant__ TbMaps maps,
+                                                                const float* __restrict__ Din, float* __restrict__ Dout,
                                                                 float* __restrict__ F0out, float* __restrict__ F,
-                                                                DyrelScalT<float> s, BC6<float> bc, Pad p, int zchunk) {
-    extern __shared__ __align__(16) unsigned char tb_smem[];
-    TbStage* st = reinterpret_cast<TbStage*>(tb_smem);
-    float(*Dp)[TB_Y][TB_X] = reinterpret_cast<float(*)[TB_Y][TB_X]>(tb_smem + sizeof(TbStage) * TB_STAGES);
+                                                                DyrelScalT<float> s, BC6<float> bc, Pad p, int zchunk,
+                                                                int* __restrict__ err) {
+    extern __shared__ unsigned char tb_raw[];
+    unsigned char* base = tb_raw + ((128 - (smem_u32(tb_raw) & 127)) & 127);
+    TbStage* st = reinterpret_cast<TbStage*>(base);
+    float(*Dp)[TB_Y][TB_X] = reinterpret_cast<float(*)[TB_Y][TB_X]>(base + sizeof(TbStage) * TB_STAGES);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(base + sizeof(TbStage) * TB_STAGES + sizeof(float) * 2 * TB_Y * TB_X);
+    __shared__ int abort_flag;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + TB_X * ty;
-    constexpr int NT = TB_X * TB_Y;
     const int x0 = blockIdx.x * (TB_X - 2) - 1, y0 = blockIdx.y * (TB_Y - 2) - 1;  // halo tile origin
+    const int xD = (x0 - 1) & ~3, xK = x0 & ~3;  // 16-byte aligned box origins (floor)
+    const int oD = x0 - xD, oK = x0 - xK;        // column of this tile's x0 in the boxes
     const int gi = x0 + tx, gj = y0 + ty;
     const bool in = gi >= 0 && gi < p.nx && gj >= 0 && gj < p.ny;
     const bool inner = in && tx >= 1 && tx <= TB_X - 2 && ty >= 1 && ty <= TB_Y - 2;
     const int k0 = blockIdx.z * zchunk, k1 = min(p.nz, k0 + zchunk);
     const int pa0 = max(k0 - 1, 0);
-    const int plast = min(k1 + 1, p.nz);  // last staged plane (plane nz: its bottom z-faces only)
+    const int plast = min(k1 + 1, p.nz);  // last staged plane (plane nz: its bottom z-faces)
     const float h1 = s.h1, h2 = s.h2, dtau = s.dtau, cX = s.cX, _dx = s._dx, _dy = s._dy, _dz = s._dz;
     const float _dx2 = __fmul_rn(_dx, _dx), _dy2 = __fmul_rn(_dy, _dy), _dz2 = __fmul_rn(_dz, _dz);
-    // this thread's copy assignments (in-plane offsets and validity; fixed over planes)
-    int dOff[2], kxOff[2], kyOff[2];
-    bool dOk[2], kxOk[2], kyOk[2];
-#pragma unroll
-    for (int r = 0; r < 2; ++r) {
-        const int e = tid + r * NT;
-        {
-            const int c = e % TB_DX, rr = e / TB_DX, xi = x0 - 1 + c, yj = y0 - 1 + rr;
-            dOk[r] = e < TB_DX * TB_DY && xi >= 0 && xi < p.nx && yj >= 0 && yj < p.ny;
-            dOff[r] = dOk[r] ? xi + p.PX * yj : 0;
-        }
-        {
-            const int c = e % (TB_X + 1), rr = e / (TB_X + 1), xi = x0 + c, yj = y0 + rr;
-            kxOk[r] = e < (TB_X + 1) * TB_Y && xi >= 0 && xi <= p.nx && yj >= 0 && yj < p.ny;
-            kxOff[r] = kxOk[r] ? xi + p.PX * yj : 0;
-        }
-        {
-            const int c = e % TB_X, rr = e / TB_X, xi = x0 + c, yj = y0 + rr;
-            kyOk[r] = e < TB_X * (TB_Y + 1) && xi >= 0 && xi < p.nx && yj >= 0 && yj <= p.ny;
-            kyOff[r] = kyOk[r] ? xi + p.PX * yj : 0;
-        }
-    }
-    const int cOff = in ? gi + p.PX * gj : 0;
-    // stage the inputs of plane k into ring slot k % TB_STAGES
-    auto stage = [&](int k) {
+    auto issue = [&](int k) {  // thread 0: the six boxes of plane k into slot k % TB_STAGES
         TbStage& S = st[k % TB_STAGES];
-        const long long pb = p.plane * k;
-        const bool full = k < p.nz;  // plane nz: z-faces only
-#pragma unroll
-        for (int r = 0; r < 2; ++r) {
-            const int e = tid + r * NT;
-            if (e < TB_DX * TB_DY) cp_async4(&S.D[0][0] + e, Din + pb + dOff[r], full && dOk[r]);
-            if (e < (TB_X + 1) * TB_Y) cp_async4(&S.kx[0][0] + e, kx + pb + kxOff[r], full && kxOk[r]);
-            if (e < TB_X * (TB_Y + 1)) cp_async4(&S.ky[0][0] + e, ky + pb + kyOff[r], full && kyOk[r]);
-        }
-        cp_async4(&S.kz[ty][tx], kz + pb + cOff, in);
-        cp_async4(&S.R[ty][tx], Rin + pb + cOff, full && in);
-        cp_async4(&S.F0[ty][tx], F0in + pb + cOff, full && in);
+        uint64_t* b = &bar[k % TB_STAGES];
+        mbar_expect_tx(b, kTbStageBytes);
+        tma_load3(&S.D[0][0], &maps.D, xD, y0 - 1, k, b);
+        tma_load3(&S.kx[0][0], &maps.kx, xK, y0, k, b);
+        tma_load3(&S.ky[0][0], &maps.ky, xK, y0, k, b);
+        tma_load3(&S.kz[0][0], &maps.kz, xK, y0, k, b);
+        tma_load3(&S.R[0][0], &maps.R, xK, y0, k, b);
+        tma_load3(&S.F0[0][0], &maps.F0, xK, y0, k, b);
     };
-    stage(pa0);
-    cp_async_commit();
-    if (pa0 + 1 <= plast) stage(pa0 + 1);
-    cp_async_commit();
-    float dm1 = (pa0 > 0 && in) ? Din[p.plane * (pa0 - 1) + cOff] : 0.f;  // D(p-1) of this column
-    // D' of planes q-1 and q for B, and the coefficients of plane q = p-1
+    if (tid == 0) {
+        abort_flag = 0;
+        for (int q = 0; q < TB_STAGES; ++q) mbar_init(&bar[q], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (tid == 0) {
+        issue(pa0);
+        if (pa0 + 1 <= plast) issue(pa0 + 1);
+    }
+    int issued = min(pa0 + 1, plast);  // last plane whose copies are in flight or done
+    float dm1 = (pa0 > 0 && in) ? Din[p.plane * (pa0 - 1) + gi + (long long)p.PX * gj] : 0.f;  // D(p-1)
     float dpm = 0.f, dpc = 0.f;
     float cW = 0.f, cE = 0.f, cS = 0.f, cN = 0.f, cB = 0.f, cF = 0.f, cr = 0.f, cf0 = 0.f;
     for (int pl = pa0; pl <= k1; ++pl) {
-        if (pl + 2 <= plast) stage(pl + 2);
-        cp_async_commit();
-        cp_async_wait1();  // planes pl and pl + 1 have landed (this thread's copies)
+        if (pl + 2 <= plast) {
+            if (tid == 0) {
+                // order the earlier generic reads of this slot before the async-proxy writes
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue(pl + 2);
+            }
+            issued = pl + 2;
+        }
+        // planes pl and pl + 1 have landed (phase = number of earlier uses of the
+        // slot); thread 0 polls the barriers, the CTA barrier then releases (and
+        // orders the copied data for) every other thread
+        if (tid == 0) {
+            bool ok = mbar_wait_bounded(&bar[pl % TB_STAGES], ((pl - pa0) / TB_STAGES) & 1);
+            if (pl + 1 <= plast)
+                ok = ok && mbar_wait_bounded(&bar[(pl + 1) % TB_STAGES], ((pl + 1 - pa0) / TB_STAGES) & 1);
+            if (!ok) abort_flag = 1;
+        }
         __syncthreads();
+        if (abort_flag) {
+            if (tid == 0) {
+                atomicExch(err, HT3D_ERR_TIMEOUT);
+                for (int q = pl; q <= issued; ++q) mbar_wait_bounded(&bar[q % TB_STAGES], ((q - pa0) / TB_STAGES) & 1);
+            }
+            __syncthreads();
+            return;
+        }
         float da = 0.f, aW = 0.f, aE = 0.f, aS = 0.f, aN = 0.f, aB = 0.f, aF = 0.f, ar = 0.f, af0 = 0.f;
         if (pl < p.nz) {
             const TbStage& S = st[pl % TB_STAGES];
             const TbStage& S1 = st[(pl + 1) % TB_STAGES];
-            aW = S.kx[ty][tx];
-            aE = S.kx[ty][tx + 1];
-            aS = S.ky[ty][tx];
-            aN = S.ky[ty + 1][tx];
-            aB = S.kz[ty][tx];
-            aF = S1.kz[ty][tx];
-            ar = S.R[ty][tx];
-            const float f0o = S.F0[ty][tx];
-            const float xc = S.D[ty + 1][tx + 1];
-            const float xw = (gi == 0) ? ghost(bc, 0, xc) : S.D[ty + 1][tx];
-            const float xe = (gi == p.nx - 1) ? ghost(bc, 1, xc) : S.D[ty + 1][tx + 2];
-            const float xs = (gj == 0) ? ghost(bc, 2, xc) : S.D[ty][tx + 1];
-            const float xn = (gj == p.ny - 1) ? ghost(bc, 3, xc) : S.D[ty + 2][tx + 1];
+            const int cd = tx + oD, ck = tx + oK;
+            aW = S.kx[ty][ck];
+            aE = S.kx[ty][ck + 1];
+            aS = S.ky[ty][ck];
+            aN = S.ky[ty + 1][ck];
+            aB = S.kz[ty][ck];
+            aF = S1.kz[ty][ck];
+            ar = S.R[ty][ck];
+            const float f0o = S.F0[ty][ck];
+            const float xc = S.D[ty + 1][cd];
+            const float xw = (gi == 0) ? ghost(bc, 0, xc) : S.D[ty + 1][cd - 1];
+            const float xe = (gi == p.nx - 1) ? ghost(bc, 1, xc) : S.D[ty + 1][cd + 1];
+            const float xs = (gj == 0) ? ghost(bc, 2, xc) : S.D[ty][cd];
+            const float xn = (gj == p.ny - 1) ? ghost(bc, 3, xc) : S.D[ty + 2][cd];
             const float xb = (pl == 0) ? ghost(bc, 4, xc) : dm1;
-            const float xf = (pl == p.nz - 1) ? ghost(bc, 5, xc) : S1.D[ty + 1][tx + 1];
+            const float xf = (pl == p.nz - 1) ? ghost(bc, 5, xc) : S1.D[ty + 1][cd];
             float f;
             mixed_cell(xc, xw, xe, xs, xn, xb, xf, aW, aE, aS, aN, aB, aF, ar, f0o, h1, h2, dtau, cX, _dx, _dy, _dz,
                        _dx2, _dy2, _dz2, f, af0, da);
@@ -334,7 +376,7 @@ __global__ void __launch_bounds__(TB_X* TB_Y, 2) k_mixed_inner2(const float* __r
             float f, f0, xn1;
             mixed_cell(xc, xw, xe, xs, xn, xb, xf, cW, cE, cS, cN, cB, cF, cr, cf0, h1, h2, dtau, cX, _dx, _dy, _dz,
                        _dx2, _dy2, _dz2, f, f0, xn1);
-            const long long e = p.plane * q + cOff;
+            const long long e = p.plane * q + gi + (long long)p.PX * gj;
             Dout[e] = xn1;
             F0out[e] = f0;
             if (STOREF) F[e] = f;
@@ -343,9 +385,40 @@ __global__ void __launch_bounds__(TB_X* TB_Y, 2) k_mixed_inner2(const float* __r
         dpc = da;
         cW = aW; cE = aE; cS = aS; cN = aN; cB = aB; cF = aF; cr = ar; cf0 = af0;
     }
-    asm volatile("cp.async.wait_group 0;\n" ::);
 }
-constexpr size_t kTbSmem = sizeof(TbStage) * TB_STAGES + sizeof(float) * 2 * TB_Y * TB_X;
+constexpr size_t kTbSmem = 128 + sizeof(TbStage) * TB_STAGES + sizeof(float) * 2 * TB_Y * TB_X + 8 * TB_STAGES;
+
+// cuTensorMapEncodeTiled, fetched from the driver at run time (no libcuda link)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)f;
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+// map of a padded FP32 field: (PX, PY, nz+1) elements, boxes TB_BW x rows x 1
+bool tb_map(CUtensorMap* m, const float* field, const Pad& P, unsigned rows) {
+    EncodeTiledFn fn = encode_tiled();
+    if (!fn) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)P.PX, (cuuint64_t)P.PY, (cuuint64_t)P.nz + 1};
+    const cuuint64_t strides[2] = {(cuuint64_t)P.PX * 4, (cuuint64_t)P.plane * 4};
+    const cuuint32_t box[3] = {(cuuint32_t)TB_BW, rows, 1};
+    const cuuint32_t es[3] = {1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)field, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
 
 // ---------------------------------------------------------------------------
 // Batched inner iteration over an ensemble of independent instances.  One
@@ -600,15 +673,29 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
     sc._dz = 1.0 / dz;
     const dim3 ib(256), ig((unsigned)(((long long)P.nq * ny + 255) / 256), (unsigned)nz);
     // two iterations per pass (k_mixed_inner2) inside runs of inner iterations
-    const bool pairs = ctx->mixed_temporal != 0;
+    bool pairs = ctx->mixed_temporal != 0;
     int zc = ctx->mixed_temporal >= 2 ? ctx->mixed_temporal : 0;
     const int tiles = ((nx + TB_X - 3) / (TB_X - 2)) * ((ny + TB_Y - 3) / (TB_Y - 2));
     if (!zc) zc = (int)std::min<long long>(64, std::max<long long>(8, (long long)nz * tiles / (8LL * ctx->num_sms)));
     const dim3 tb(TB_X, TB_Y), tg((nx + TB_X - 3) / (TB_X - 2), (ny + TB_Y - 3) / (TB_Y - 2), (nz + zc - 1) / zc);
+    TbMaps mapsA, mapsB;  // passes reading (Da, F0a) and (Db, F0b)
+    int* derr = nullptr;
+    if (pairs) {
+        pairs = tb_map(&mapsA.D, Da, P, TB_Y + 2) && tb_map(&mapsB.D, Db, P, TB_Y + 2) &&
+                tb_map(&mapsA.F0, F0a, P, TB_Y) && tb_map(&mapsB.F0, F0b, P, TB_Y) &&
+                tb_map(&mapsA.kx, kx32, P, TB_Y) && tb_map(&mapsA.ky, ky32, P, TB_Y + 1) &&
+                tb_map(&mapsA.kz, kz32, P, TB_Y) && tb_map(&mapsA.R, Rin, P, TB_Y);
+        mapsB.kx = mapsA.kx;
+        mapsB.ky = mapsA.ky;
+        mapsB.kz = mapsA.kz;
+        mapsB.R = mapsA.R;
+    }
     if (pairs) {
         static_assert(kTbSmem <= 227 * 1024, "staging ring exceeds the shared memory of a CTA");
         HT3D_CUDA(cudaFuncSetAttribute(k_mixed_inner2<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTbSmem));
         HT3D_CUDA(cudaFuncSetAttribute(k_mixed_inner2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTbSmem));
+        derr = (int*)ht3d_scratch(ctx, SLOT_AUX0, sizeof(int) * 16);
+        HT3D_CUDA(cudaMemsetAsync(derr, 0, sizeof(int), ctx->stream));
     }
     InnerTimer timer(ctx);
     double* xcur = X;
@@ -652,12 +739,16 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
             const int left = pair_end - iter + 1;
             if (pairs && left >= 2 && left % 2 == 0) {
                 const bool storef2 = iter + 1 == nmax || is_check(iter + 2, prm->nitout);
+                // D alternates every iteration, F0 only on passes: pick their maps separately
+                TbMaps mp = mapsA;
+                mp.D = dcur == Da ? mapsA.D : mapsB.D;
+                mp.F0 = f0cur == F0a ? mapsA.F0 : mapsB.F0;
                 if (storef2)
-                    HT3D_LAUNCH(ctx, k_mixed_inner2<true>, tg, tb, kTbSmem, dcur, dnxt, Rin, kx32, ky32, kz32, f0cur,
-                                f0nxt, Fs, s32, bch, P, zc);
+                    HT3D_LAUNCH(ctx, k_mixed_inner2<true>, tg, tb, kTbSmem, mp, dcur, dnxt, f0nxt, Fs, s32, bch, P, zc,
+                                derr);
                 else
-                    HT3D_LAUNCH(ctx, k_mixed_inner2<false>, tg, tb, kTbSmem, dcur, dnxt, Rin, kx32, ky32, kz32, f0cur,
-                                f0nxt, Fs, s32, bch, P, zc);
+                    HT3D_LAUNCH(ctx, k_mixed_inner2<false>, tg, tb, kTbSmem, mp, dcur, dnxt, f0nxt, Fs, s32, bch, P, zc,
+                                derr);
                 std::swap(f0cur, f0nxt);
                 timer.count(2);
                 ++iter;  // the pass did iterations iter and iter + 1
@@ -702,6 +793,12 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
     }
     HT3D_LAUNCH(ctx, k_unpack, gc, b2, 0, F0, f0cur, P);
     if (!last_fp64) HT3D_LAUNCH(ctx, k_unpack, gc, b2, 0, F, Fs, P);
+    if (derr) {  // a bounded wait of k_mixed_inner2 gave up
+        int herr = 0;
+        HT3D_CUDA(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        HT3D_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (herr && status == HT3D_OK) status = herr;
+    }
     timer.collect();
     if (st) {
         st->iters = it_done; st->converged = converged; st->status = status; st->checks = checks;

@@ -4,7 +4,8 @@
   ncu --set full --clock-control none -k regex:k_dyrel_iter -s 2 -c 1 -o out \\
       python -m hydrothermal3d_gb300.profile_kernels --kernel dyrel_f32 --n 255 --iters 5
 
-Kernels: dyrel_f32 (FP32 pseudo-iteration on the reference layout),
+Kernels: weno_f32 (one FP32 WENO5 sweep in a curl velocity),
+dyrel_f32 (FP32 pseudo-iteration on the reference layout),
 dyrel_f64 (plain FP64 pseudo-iteration), mixed_solve (a mixed-form DYREL
 solve of --iters pseudo-iterations: two FP64 checks, then the padded FP32
 inner kernel k_mixed_inner), weno_f64 / weno_mixed (one fused WENO5
@@ -22,7 +23,8 @@ from hydrothermal3d_gb300 import abi, hrl
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--kernel", default="dyrel_f32", choices=["dyrel_f32", "dyrel_f64", "mixed_solve", "weno_f64", "weno_mixed"])
+    ap.add_argument("--kernel", default="dyrel_f32",
+                    choices=["dyrel_f32", "dyrel_f64", "mixed_solve", "weno_f64", "weno_mixed", "weno_f32"])
     ap.add_argument("--n", type=int, default=255)
     ap.add_argument("--iters", type=int, default=5)
     ap.add_argument("--variant", type=int, default=0,
@@ -79,6 +81,23 @@ def main():
         alg = hrl.bytes_per_iteration(n, n, n, 4)
         print(json.dumps({"kernel": "k_mixed_inner", "n": n, "tune": a.tune, "inner_iterations": nl,
                           "us_per_iteration": t * 1e6, "alg_GBs": alg / t / 1e9}))
+    elif a.kernel == "weno_f32":
+        from hydrothermal3d_gb300 import api, sweep
+        V = [v.float().permute(2, 1, 0).contiguous().permute(2, 1, 0) for v in sweep.curl_velocity(n, n, n, seed=6)]
+        T = sweep.blob(n, n, n).float().permute(2, 1, 0).contiguous().permute(2, 1, 0)
+        dtc = sweep.cfl_dt(n, n, n)
+        run = lambda: api.weno5_advect_f32(ctx, T, *V, dtc, float(n), float(n), float(n), [0, 0, 1, 1, 0, 0],
+                                           [0, 0, 1.0, 0.0, 0, 0], abi.WENO_V1)
+        run()
+        ctx.synchronize()
+        e0.record(stream)
+        for _ in range(a.iters):
+            run()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1e3 / a.iters
+        print(json.dumps({"kernel": "weno_f32 sweep", "n": n, "us_per_sweep": t * 1e6,
+                          "alg_GBs": sweep.bytes_per_sweep(n, n, n, 4) / t / 1e9}))
     else:
         prec = abi.FP64 if a.kernel == "weno_f64" else abi.MIXED
         T = ht.zeros(n + 2, n + 2, n + 2).uniform_(0, 1)

@@ -76,9 +76,9 @@ extern "C" {
                                        launch; 1 = two per pass through memory (temporal
                                        blocking, z-chunk chosen per grid), >= 2 = the same
                                        with that many planes per chunk; bit-identical
-                                       results (on GB300 the two-iteration pass is still
-                                       instruction-issue bound and slower: 135 vs 91 us
-                                       per iteration at 255^3)                          */
+                                       results (on GB300 the two-iteration pass, TMA-staged,
+                                       is still instruction-issue bound and slower: 98.5
+                                       vs 86 us per iteration at 255^3)                  */
 
 typedef struct ht3d_ctx ht3d_ctx;
 
