@@ -48,6 +48,9 @@ def parse():
     ap.add_argument("--ens-steps", type=int, default=20)
     ap.add_argument("--skip-ensemble", action="store_true")
     ap.add_argument("--sweep-n", type=int, default=511, help="cells per axis of the standalone WENO5 sweep (0 = skip)")
+    ap.add_argument("--c63-steps", type=int, default=10,
+                    help="time steps of the 63^3 HRL case (config 1): oracle on the host cores and GPU forms "
+                         "(0 = skip)")
     ap.add_argument("--v18-steps", type=int, default=2,
                     help="time steps of the 127^3 dimensional (v18) box, plain FP64 (0 = skip)")
     ap.add_argument("--fault-steps", type=int, default=0,
@@ -183,6 +186,71 @@ def cpu_sample(n, seconds, threads=None):
     return nbytes / t_tot / 1e9, cores, desc, t_tot
 
 
+def oracle_c63(steps, threads=None):
+    """Config 1: the oracle (C++ FP64, OpenMP) runs `steps` full HRL time steps
+    at 63^3 from the seeded initial condition on the host cores.  Returns the
+    timing summary and the final (T, P) for the GPU parity check."""
+    import oracle
+    from hydrothermal3d_gb300 import hrl
+    if threads:
+        oracle.set_threads(threads)
+    n = 63
+    T, P, ktv, kfv = hrl.initial_fields(n, n, n, seed=1)
+    p = hrl.params(n, n, n)
+    V = [np.zeros(s, order="F") for s in ((n + 1, n, n), (n, n + 1, n), (n, n, n + 1))]
+    iters, nbytes = [], 0
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        st, a_, b_ = oracle.step_hrl(T, P, ktv, kfv, *V, p)
+        iters.append([a_.iters, b_.iters])
+        nbytes += (a_.iters + b_.iters) * hrl.bytes_per_iteration(n, n, n, 8) + hrl.bytes_per_advection(n, n, n, 8)
+    t = time.perf_counter() - t0
+    res = {"n": n, "steps": steps, "seconds": t, "time_steps_per_s": steps / t, "T_eff_GBs": nbytes / t / 1e9,
+           "cores": oracle.num_threads(), "pseudo_iterations_per_step": iters,
+           "impl": "oracle (C++ FP64, unfused kernels, OpenMP)"}
+    return res, T, P
+
+
+def c63_bench(ctx, stream, steps):
+    """Config 1 on the GPU (FP64 and mixed forms, same 63^3 workload and steps
+    as the oracle run beside it); the FP64 form's final fields are compared
+    with the oracle's."""
+    import torch
+    import hydrothermal3d_gb300 as ht
+    from hydrothermal3d_gb300 import api, abi, hrl
+    cpu, To, Po = oracle_c63(steps, threads=os.cpu_count())
+    n = 63
+    T0, P0, ktv, kfv = hrl.initial_fields(n, n, n, seed=1)
+    ktd, kfd = ht.from_numpy(ktv), ht.from_numpy(kfv)
+    V = [ht.zeros(n + 1, n, n), ht.zeros(n, n + 1, n), ht.zeros(n, n, n + 1)]
+    res = {"cpu_oracle": cpu}
+    inner = (slice(1, -1),) * 3
+    for name, prec, s in (("gpu_fp64", abi.FP64, 8), ("gpu_mixed", abi.MIXED, 4)):
+        Td, Pd = ht.from_numpy(T0), ht.from_numpy(P0)
+        p = hrl.params(n, n, n)
+        nbytes = 0
+        with torch.cuda.stream(stream):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(steps):
+                gt, gd = api.step_hrl(ctx, Td, Pd, ktd, kfd, *V, p, prec)
+                nbytes += (gt.iters + gd.iters) * hrl.bytes_per_iteration(n, n, n, s) + \
+                    hrl.bytes_per_advection(n, n, n, s)
+            torch.cuda.synchronize()
+            t = time.perf_counter() - t0
+        Tg = ht.to_numpy(Td)
+        Pg = ht.to_numpy(Pd)
+        Pg_, Po_ = Pg[inner] - Pg[inner].mean(), Po[inner] - Po[inner].mean()
+        res[name] = {"time_steps_per_s": steps / t, "T_eff_GBs": nbytes / t / 1e9, "seconds": t,
+                     "T_rel_err_vs_oracle": float(np.abs(Tg[inner] - To[inner]).max() / np.abs(To[inner]).max()),
+                     "P_rel_err_vs_oracle_mean_removed": float(np.abs(Pg_ - Po_).max() / np.abs(Po_).max()),
+                     "T_bitwise_equal_to_oracle": bool(np.array_equal(Tg[inner], To[inner]))}
+    res["note"] = ("63^3 fields fit in L2 (each FP64 field ~2 MB), so GPU T_eff here is not an HBM figure; "
+                   "the accumulated mixed error includes the growth of perturbations through the convective "
+                   "instability over the steps")
+    return res
+
+
 def run_reference(a):
     ws, rank, _ = dist_setup()
     if rank != 0:
@@ -200,6 +268,8 @@ def run_reference(a):
             "config": workload_config(a, {"reference_impl": "CPU oracle port (reference is Julia; not runnable here)"}),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if a.c63_steps:
+        line["config_63"] = oracle_c63(a.c63_steps, threads=os.cpu_count())[0]
     print(json.dumps(line))
 
 
@@ -299,6 +369,8 @@ def run_ours(a):
         out["fault_slab_511"] = fault_bench(ctx, stream, a)
     if a.v18_steps:
         out["dimensional_127"] = v18_bench(ctx, stream, a.v18_steps)
+    if a.c63_steps and rank == 0:
+        out["config_63"] = c63_bench(ctx, stream, a.c63_steps)
 
     if rank == 0:
         v, cores, desc, _ = cpu_sample(n, a.cpu_seconds, threads=os.cpu_count())

@@ -24,7 +24,9 @@ from hydrothermal3d_gb300 import abi, hrl
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--kernel", default="dyrel_f32",
-                    choices=["dyrel_f32", "dyrel_f64", "mixed_solve", "weno_f64", "weno_mixed", "weno_f32"])
+                    choices=["dyrel_f32", "dyrel_f64", "mixed_solve", "weno_f64", "weno_mixed", "weno_f32",
+                             "ensemble"])
+    ap.add_argument("--members", type=int, default=16, help="ensemble members (--kernel ensemble)")
     ap.add_argument("--n", type=int, default=255)
     ap.add_argument("--iters", type=int, default=5)
     ap.add_argument("--variant", type=int, default=0,
@@ -81,6 +83,22 @@ def main():
         alg = hrl.bytes_per_iteration(n, n, n, 4)
         print(json.dumps({"kernel": "k_mixed_inner", "n": n, "tune": a.tune, "inner_iterations": nl,
                           "us_per_iteration": t * 1e6, "alg_GBs": alg / t / 1e9}))
+    elif a.kernel == "ensemble":
+        from hydrothermal3d_gb300 import api
+        mem = []
+        for T, P, ktv, kfv, p in hrl.ensemble(a.members, seed=4):
+            nx, ny, nz = (q - 2 for q in T.shape)
+            mem.append(api.Member(ht.from_numpy(T), ht.from_numpy(P), ht.from_numpy(ktv), ht.from_numpy(kfv),
+                                  ht.zeros(nx + 1, ny, nz), ht.zeros(nx, ny + 1, nz), ht.zeros(nx, ny, nz + 1), p))
+        ctx.set_tuning(abi.TUNE_TIME_INNER, 1)
+        with torch.cuda.stream(stream):
+            for _ in range(a.iters):
+                api.ensemble_step(ctx, mem, abi.MIXED)
+        torch.cuda.synchronize()
+        ms, nl = ctx.inner_timing(reset=True)
+        cells = sum(int(m.Tc_ex.shape[0] - 2) * int(m.Tc_ex.shape[1] - 2) * int(m.Tc_ex.shape[2] - 2) for m in mem)
+        print(json.dumps({"kernel": "k_ens_inner", "members": len(mem), "cells": cells, "inner_iterations": nl,
+                          "us_per_iteration": 1e3 * ms / max(1, nl)}))
     elif a.kernel == "weno_f32":
         from hydrothermal3d_gb300 import api, sweep
         V = [v.float().permute(2, 1, 0).contiguous().permute(2, 1, 0) for v in sweep.curl_velocity(n, n, n, seed=6)]
