@@ -61,9 +61,21 @@ __global__ void __launch_bounds__(256) k_weno_stage_f32(const float* __restrict_
 }
 
 // Both stages of one axis fused, x-axis: a warp owns a row; the row of T0 and
-// of the stage-1 result T1 live in shared memory (ghosts by the BC rules).
-// Reads T0 and Vx once and writes T once.
+// of the stage-1 result T1 live in shared memory with three ghost cells on
+// each side (filled by the BC rules after each stage), so the stencils are
+// plain shared loads.  Reads T0 and Vx once and writes T once.
 constexpr int kRowWarps = 8;
+
+// ghost cells r[-3..-1] and r[n..n+2] of a shared row r (r points at element 0)
+__device__ __forceinline__ void fill_row_ghosts(float* r, int n, const WenoBC& bc, int lane) {
+    if (lane < 3) {  // left: position -1-q mirrors q (periodic: n-1-q)
+        const int q = lane;
+        r[-1 - q] = bc.typeL == HT3D_BC_PERIODIC ? r[n - 1 - q] : weno_ghost(r[q], true, bc);
+    } else if (lane < 6) {  // right: position n+q mirrors n-1-q (periodic: q)
+        const int q = lane - 3;
+        r[n + q] = bc.typeR == HT3D_BC_PERIODIC ? r[q] : weno_ghost(r[n - 1 - q], false, bc);
+    }
+}
 
 template <int QUIRK>
 __global__ void __launch_bounds__(32 * kRowWarps) k_weno_rows_f32(float* __restrict__ T, const float* __restrict__ Vx,
@@ -74,23 +86,23 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_weno_rows_f32(float* __restr
     const long long row = (long long)blockIdx.x * kRowWarps + warp;  // over (j, k)
     if (row >= (long long)ny * nz) return;                           // whole warps only
     const int j = (int)(row % ny), k = (int)(row / ny);
-    float* s0 = rows_sm + (size_t)warp * 2 * nx;
-    float* s1 = s0 + nx;
+    float* s0 = rows_sm + (size_t)warp * 2 * (nx + 6) + 3;  // T0[-3 .. nx+2]
+    float* s1 = s0 + nx + 6;                                 // T1[-3 .. nx+2]
     float* line = T + 1 + (long long)(nx + 2) * ((j + 1) + (long long)(ny + 2) * (k + 1));
     const float* vrow = Vx + (long long)(nx + 1) * (j + (long long)ny * k);
     for (int m = lane; m < nx; m += 32) s0[m] = line[m];
     __syncwarp();
+    fill_row_ghosts(s0, nx, bc, lane);
+    __syncwarp();
     for (int m = lane; m < nx; m += 32) {
-        float x[7];
-#pragma unroll
-        for (int o = 0; o < 7; ++o) x[o] = line_at<float>(s0, 1, m + o - 3, nx, bc);
+        const float* x = s0 + m - 3;
         s1[m] = weno_point_f32<QUIRK>(x[0], x[1], x[2], x[3], x[4], x[5], x[6], vrow[m], vrow[m + 1], dt, h);
     }
     __syncwarp();
+    fill_row_ghosts(s1, nx, bc, lane);
+    __syncwarp();
     for (int m = lane; m < nx; m += 32) {
-        float x[7];
-#pragma unroll
-        for (int o = 0; o < 7; ++o) x[o] = line_at<float>(s1, 1, m + o - 3, nx, bc);
+        const float* x = s1 + m - 3;
         const float t = weno_point_f32<QUIRK>(x[0], x[1], x[2], x[3], x[4], x[5], x[6], vrow[m], vrow[m + 1], dt, h);
         line[m] = 0.5f * t + 0.5f * s0[m];
     }
@@ -159,7 +171,7 @@ __global__ void __launch_bounds__(128) k_weno_march_f32(const float* __restrict_
     }
 #pragma unroll
     for (int q = 0; q < 5; ++q) v[q] = c0 + q <= n ? vline[(long long)(c0 + q) * vs] : 0.f;
-#pragma unroll 4
+#pragma unroll 2
     for (int c = c0; c < c1; ++c) {
         const int p = c + 3;  // T1 position entering the window
         float head;
@@ -205,7 +217,7 @@ float* axis_f32(ht3d_ctx* ctx, float* cur, float* other, float* tmp, const float
                 int nx, int ny, int nz) {
     const bool periodic = bc.typeL == HT3D_BC_PERIODIC || bc.typeR == HT3D_BC_PERIODIC;
     if (AXIS == 0) {
-        const size_t smem = sizeof(float) * 2 * (size_t)nx * kRowWarps;
+        const size_t smem = sizeof(float) * 2 * (size_t)(nx + 6) * kRowWarps;
         if (smem <= 96 * 1024) {
             if (smem > 48 * 1024)
                 HT3D_CUDA(cudaFuncSetAttribute(k_weno_rows_f32<QUIRK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
