@@ -51,6 +51,9 @@ def parse():
     ap.add_argument("--c63-steps", type=int, default=10,
                     help="time steps of the 63^3 HRL case (config 1): oracle on the host cores and GPU forms "
                          "(0 = skip)")
+    ap.add_argument("--growth-steps", type=int, default=6,
+                    help="steps of the 127^3 error-growth comparison (mixed and a 1e-8-perturbed FP64 run "
+                         "against FP64; 0 = skip)")
     ap.add_argument("--v18-steps", type=int, default=2,
                     help="time steps of the 127^3 dimensional (v18) box, plain FP64 (0 = skip)")
     ap.add_argument("--fault-steps", type=int, default=0,
@@ -369,6 +372,8 @@ def run_ours(a):
         out["fault_slab_511"] = fault_bench(ctx, stream, a)
     if a.v18_steps:
         out["dimensional_127"] = v18_bench(ctx, stream, a.v18_steps)
+    if a.growth_steps:
+        out["error_growth_127"] = growth_bench(ctx, stream, a.growth_steps)
     if a.c63_steps and rank == 0:
         out["config_63"] = c63_bench(ctx, stream, a.c63_steps)
 
@@ -596,6 +601,42 @@ def sweep_bench(ctx, stream, n, reps=3):
                          "storage_bytes": s}
             del T
     return res
+
+
+def growth_bench(ctx, stream, steps, n=127, eps=1e-8):
+    """How the HRL workload amplifies small differences: per time step, the
+    max-norm relative T difference against the FP64 run of (a) the mixed form
+    and (b) the FP64 form started from the initial condition perturbed by
+    eps * U(-1, 1) (relative, seed 9).  Both use the FP64 run's dt sequence."""
+    import torch
+    import hydrothermal3d_gb300 as ht
+    from hydrothermal3d_gb300 import api, abi, hrl
+    T0, P0, ktv, kfv = hrl.initial_fields(n, n, n, seed=1)
+    Tp = T0.copy(order="F")
+    Tp[1:-1, 1:-1, 1:-1] *= 1.0 + eps * np.random.default_rng(9).uniform(-1, 1, (n, n, n))
+    ktd, kfd = ht.from_numpy(ktv), ht.from_numpy(kfv)
+    V = [ht.zeros(n + 1, n, n), ht.zeros(n, n + 1, n), ht.zeros(n, n, n + 1)]
+    runs = {"fp64": (T0, abi.FP64), "mixed": (T0, abi.MIXED), "fp64_perturbed": (Tp, abi.FP64)}
+    fields = {k: (ht.from_numpy(t), ht.from_numpy(P0)) for k, (t, _) in runs.items()}
+    inner = (slice(1, -1),) * 3
+    out = {"n": n, "perturbation": eps, "mixed_vs_fp64": [], "fp64_perturbed_vs_fp64": []}
+    p = hrl.params(n, n, n)
+    with torch.cuda.stream(stream):
+        for _ in range(steps):
+            dt = p.dt
+            api.step_hrl(ctx, *fields["fp64"], ktd, kfd, *V, p, abi.FP64)
+            for k in ("mixed", "fp64_perturbed"):
+                q = hrl.params(n, n, n)
+                q.dt = dt
+                api.step_hrl(ctx, *fields[k], ktd, kfd, *V, q, runs[k][1])
+            torch.cuda.synchronize()
+            ref = fields["fp64"][0][inner]
+            scale = float(ref.abs().max())
+            out["mixed_vs_fp64"].append(float((fields["mixed"][0][inner] - ref).abs().max()) / scale)
+            out["fp64_perturbed_vs_fp64"].append(float((fields["fp64_perturbed"][0][inner] - ref).abs().max()) / scale)
+    out["note"] = ("a 1e-8 perturbation of the FP64 run grows like the mixed form's difference: the accumulated "
+                   "difference measures the convective instability of the workload, the per-step error the form")
+    return out
 
 
 def v18_bench(ctx, stream, steps, n=127):

@@ -112,3 +112,19 @@ def test_ensemble_requires_shared_schedule(ctx):
     with pytest.raises(ht.Ht3dError):
         api.ensemble_step(ctx, to_device(base), abi.MIXED)
 
+
+
+def test_ensemble_more_members_than_one_launch_group(ctx):
+    """130 members exceed one batched launch's parameter block (120 member
+    records): the lockstep iteration is split into several launches per
+    pseudo-iteration and stays bit-identical to per-member steps."""
+    rng = np.random.default_rng(57)
+    sizes = [tuple(int(v) for v in rng.integers(3, 9, size=3)) for _ in range(130)]
+    base = members_np(sizes, seed=58, nitout=50)
+    for *_, p in base:
+        p.thermal.nitmax = p.darcy.nitmax = 500
+        p.thermal.tol_rel = p.darcy.tol_rel = p.thermal.tol_abs = p.darcy.tol_abs = 1e-6
+    seq, ens = to_device(base), to_device(base)
+    step_sequential(ctx, seq, abi.MIXED)
+    assert api.ensemble_step(ctx, ens, abi.MIXED) == [abi.OK] * len(ens)
+    assert_same(ens, seq)
