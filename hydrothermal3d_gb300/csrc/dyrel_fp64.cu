@@ -130,3 +130,20 @@ extern "C" int ht3d_dyrel_iterate(ht3d_ctx* ctx, double* X_ex, const double* R, 
     });
 }
 
+
+extern "C" int ht3d_dyrel_thermal_iterate(ht3d_ctx* ctx, int n_iter, double* T_ex, const double* Rt, const double* kx,
+                                          const double* ky, const double* kz, const double* PC, double* F0,
+                                          double _dt, double dx, double dy, double dz, const int* bc_type6,
+                                          const double* bc_val6, double h1, double h2, double dtau, int nx, int ny,
+                                          int nz) {
+    return ht3d_dyrel_iterate(ctx, T_ex, Rt, kx, ky, kz, PC, F0, _dt, dx, dy, dz, bc_type6, bc_val6, h1, h2, dtau,
+                              n_iter, nx, ny, nz);
+}
+
+extern "C" int ht3d_dyrel_darcy_iterate(ht3d_ctx* ctx, int n_iter, double* P_ex, const double* Rp, const double* kx,
+                                        const double* ky, const double* kz, const double* PC, double* F0, double dx,
+                                        double dy, double dz, const int* bc_type6, const double* bc_val6, double h1,
+                                        double h2, double dtau, int nx, int ny, int nz) {
+    return ht3d_dyrel_iterate(ctx, P_ex, Rp, kx, ky, kz, PC, F0, 0.0, dx, dy, dz, bc_type6, bc_val6, h1, h2, dtau,
+                              n_iter, nx, ny, nz);
+}

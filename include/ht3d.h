@@ -380,12 +380,24 @@ int ht3d_dyrel_solve_dimless(ht3d_ctx* ctx, double* X_ex, const double* R, const
 /* n_iter plain pseudo-iterations of the fused DYREL kernel with fixed
    (h1, h2, dtau) and no checks -- the inner loop of ht3d_dyrel_solve_dimless
    (Dimensional/HydroThermal3D_v18.jl:451-455 without the check block), for
-   callers that run their own schedule.  invPC is 1/PC (n^3).  The _f32
-   variant takes FP32 fields (the mixed form's inner iteration). */
+   callers that run their own schedule.  The FP64 form takes PC (n^3) and
+   divides by it like the reference (F /= PC); the _f32 variant takes FP32
+   fields and invPC = 1/PC, which it multiplies. */
 int ht3d_dyrel_iterate(ht3d_ctx* ctx, double* X_ex, const double* R, const double* kx, const double* ky,
-                       const double* kz, const double* invPC, double* F0, double cX, double dx, double dy, double dz,
+                       const double* kz, const double* PC, double* F0, double cX, double dx, double dy, double dz,
                        const int* bc_type6, const double* bc_val6, double h1, double h2, double dtau, int n_iter,
                        int nx, int ny, int nz);
+/* The same iteration for the two dimensionless problems by name: the thermal
+   one (ResidualDiffusionTransient!, cX = _dt, Dimensionless/HydroThermal3D_Alban_v6.jl:84-90)
+   and the Darcy one (ResidualDiffusion!, cX = 0, Dimensionless/kernels_HT3D.jl:128-134). */
+int ht3d_dyrel_thermal_iterate(ht3d_ctx* ctx, int n_iter, double* T_ex, const double* Rt, const double* kx,
+                               const double* ky, const double* kz, const double* PC, double* F0, double _dt,
+                               double dx, double dy, double dz, const int* bc_type6, const double* bc_val6, double h1,
+                               double h2, double dtau, int nx, int ny, int nz);
+int ht3d_dyrel_darcy_iterate(ht3d_ctx* ctx, int n_iter, double* P_ex, const double* Rp, const double* kx,
+                             const double* ky, const double* kz, const double* PC, double* F0, double dx, double dy,
+                             double dz, const int* bc_type6, const double* bc_val6, double h1, double h2, double dtau,
+                             int nx, int ny, int nz);
 int ht3d_dyrel_iterate_f32(ht3d_ctx* ctx, float* X_ex, const float* R, const float* kx, const float* ky,
                            const float* kz, const float* invPC, float* F0, double cX, double dx, double dy, double dz,
                            const int* bc_type6, const double* bc_val6, double h1, double h2, double dtau, int n_iter,
