@@ -335,6 +335,52 @@ inline void dyrel_init_params(const ht3d_dyrel_params* prm, double lmax, DyrelSt
 
 inline bool is_check(int iter, int nitout) { return (iter % nitout == 0) || iter <= 2; }
 
+// Host bookkeeping of a DYREL solve's check iterations
+// (Dimensional/HydroThermal3D_v18.jl:457-476): the residual norm
+// mean|F|/sqrt(N), the NaN and divergence errors, the Rayleigh-quotient
+// update of lambda_min and the damping parameters, and the stop test.  One
+// copy for every solver so they all round alike.
+struct DyrelCheck {
+    double nF_abs = 0.0, nF_rel = 0.0, nF_ini = 0.0;
+    int checks = 0, converged = 0, status = HT3D_OK;
+
+    // s_abs = sum |F*PC|, s_num / s_den the Rayleigh-quotient sums; returns
+    // true when the solve stops at this check (error or converged).
+    bool update(DyrelState& S, const ht3d_dyrel_params* prm, double s_abs, double s_num, double s_den, double ncells,
+                int iter, bool stop_test) {
+        ++checks;
+        nF_abs = s_abs / ncells / sqrt(ncells) * prm->norm_scale;
+        if (iter == 1) nF_ini = nF_abs;
+        nF_rel = nF_abs / nF_ini;
+        if (std::isnan(nF_abs)) {
+            status = HT3D_ERR_NAN;
+            return true;
+        }
+        if (nF_rel > 100) {
+            status = HT3D_ERR_DIVERGED;
+            return true;
+        }
+        if (iter > 1) {
+            S.lmin = fabs(s_num) / fabs(s_den);
+            S.c = 2.0 * sqrt(S.lmin) * prm->cfact;
+            S.h1 = (2 - S.c * S.dtau) / (2 + S.c * S.dtau);
+            S.h2 = 2 * S.dtau / (2 + S.c * S.dtau);
+        }
+        if (stop_test && (nF_abs < prm->tol_abs || nF_rel < prm->tol_rel)) {
+            converged = 1;
+            return true;
+        }
+        return false;
+    }
+
+    void fill(ht3d_dyrel_stats* st, const DyrelState& S, int iters) const {
+        if (!st) return;
+        st->iters = iters; st->converged = converged; st->status = status; st->checks = checks;
+        st->nF_abs = nF_abs; st->nF_rel = nF_rel; st->nF_ini = nF_ini; st->lambda_min = S.lmin;
+        st->lambda_max = S.lmax; st->h1 = S.h1; st->h2 = S.h2; st->dtau = S.dtau;
+    }
+};
+
 
 // ---------------------------------------------------------------------------
 // n_iter plain pseudo-iterations with fixed (h1, h2, dtau): the solver's inner

@@ -45,8 +45,8 @@ int ht3d_dyrel_solve_fp64(ht3d_ctx* ctx, double* X, const double* R, const doubl
     sc._dz = 1.0 / dz;
     double* cur = X;
     double* nxt = X2;
-    double nF_abs = 0., nF_rel = 0., nF_ini = 0.;
-    int it_done = 0, converged = 0, status = HT3D_OK, checks = 0;
+    DyrelCheck C;
+    int it_done = 0;
     const int nmax = n_iter_fixed > 0 ? n_iter_fixed : prm->nitmax;
     HT3D_REQUIRE(prm->nitout >= 1, "nitout must be >= 1");
     for (int iter = 1; iter <= nmax; ++iter) {
@@ -64,33 +64,18 @@ int ht3d_dyrel_solve_fp64(ht3d_ctx* ctx, double* X, const double* R, const doubl
         std::swap(cur, nxt);
         it_done = iter;
         if (chk) {
-            ++checks;
             tree_sum3(ctx, parts, n, parts + 3 * n);
-            const double s_abs = ctx->h_result[0], s_num = ctx->h_result[1], s_den = ctx->h_result[2];
-            nF_abs = s_abs / (double)n / sqrt((double)n) * prm->norm_scale;
-            if (iter == 1) nF_ini = nF_abs;
-            nF_rel = nF_abs / nF_ini;
-            if (std::isnan(nF_abs)) { status = HT3D_ERR_NAN; break; }
-            if (nF_rel > 100) { status = HT3D_ERR_DIVERGED; break; }
-            if (iter > 1) {
-                S.lmin = fabs(s_num) / fabs(s_den);
-                S.c = 2.0 * sqrt(S.lmin) * prm->cfact;
-                S.h1 = (2 - S.c * S.dtau) / (2 + S.c * S.dtau);
-                S.h2 = 2 * S.dtau / (2 + S.c * S.dtau);
-            }
-            if (n_iter_fixed <= 0 && (nF_abs < prm->tol_abs || nF_rel < prm->tol_rel)) { converged = 1; break; }
+            if (C.update(S, prm, ctx->h_result[0], ctx->h_result[1], ctx->h_result[2], (double)n, iter,
+                         n_iter_fixed <= 0))
+                break;
         }
     }
     if (cur != X) {
         dim3 b(32, 8, 1), g((nx + 2 + 31) / 32, (ny + 2 + 7) / 8, nz + 2);
         HT3D_LAUNCH(ctx, k_copy_ex_faces<double>, g, b, 0, X, cur, nx, ny, nz);
     }
-    if (st) {
-        st->iters = it_done; st->converged = converged; st->status = status; st->checks = checks;
-        st->nF_abs = nF_abs; st->nF_rel = nF_rel; st->nF_ini = nF_ini; st->lambda_min = S.lmin;
-        st->lambda_max = S.lmax; st->h1 = S.h1; st->h2 = S.h2; st->dtau = S.dtau;
-    }
-    return status;
+    C.fill(st, S, it_done);
+    return C.status;
 }
 
 

@@ -704,8 +704,8 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
     float* dnxt = Db;
     float* f0cur = F0a;  // current FP32 momentum (k_mixed_inner2 writes the other buffer)
     float* f0nxt = F0b;
-    double nF_abs = 0., nF_rel = 0., nF_ini = 0.;
-    int it_done = 0, converged = 0, status = HT3D_OK, checks = 0;
+    DyrelCheck C;
+    int it_done = 0;
     bool last_fp64 = false;  // the last iteration ran the FP64 kernel (check or refresh)
     const int nmax = n_iter_fixed > 0 ? n_iter_fixed : prm->nitmax;
     const int refresh_every = ctx->mixed_refresh;
@@ -766,22 +766,11 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
         it_done = iter;
         last_fp64 = chk || refresh;
         if (chk) {
-            ++checks;
             HT3D_LAUNCH(ctx, (k_reduce_partials<RED_SUM, 3>), 1, 1024, 0, parts, (int)LC.nblocks, dres);
             ht3d_fetch_results(ctx, dres, 3);
-            const double s_abs = ctx->h_result[0], s_num = ctx->h_result[1], s_den = ctx->h_result[2];
-            nF_abs = s_abs / (double)n / sqrt((double)n) * prm->norm_scale;
-            if (iter == 1) nF_ini = nF_abs;
-            nF_rel = nF_abs / nF_ini;
-            if (std::isnan(nF_abs)) { status = HT3D_ERR_NAN; break; }
-            if (nF_rel > 100) { status = HT3D_ERR_DIVERGED; break; }
-            if (iter > 1) {
-                S.lmin = fabs(s_num) / fabs(s_den);
-                S.c = 2.0 * sqrt(S.lmin) * prm->cfact;
-                S.h1 = (2 - S.c * S.dtau) / (2 + S.c * S.dtau);
-                S.h2 = 2 * S.dtau / (2 + S.c * S.dtau);
-            }
-            if (n_iter_fixed <= 0 && (nF_abs < prm->tol_abs || nF_rel < prm->tol_rel)) { converged = 1; break; }
+            if (C.update(S, prm, ctx->h_result[0], ctx->h_result[1], ctx->h_result[2], (double)n, iter,
+                         n_iter_fixed <= 0))
+                break;
         }
     }
     timer.end();
@@ -797,15 +786,11 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
         int herr = 0;
         HT3D_CUDA(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
         HT3D_CUDA(cudaStreamSynchronize(ctx->stream));
-        if (herr && status == HT3D_OK) status = herr;
+        if (herr && C.status == HT3D_OK) C.status = herr;
     }
     timer.collect();
-    if (st) {
-        st->iters = it_done; st->converged = converged; st->status = status; st->checks = checks;
-        st->nF_abs = nF_abs; st->nF_rel = nF_rel; st->nF_ini = nF_ini; st->lambda_min = S.lmin;
-        st->lambda_max = S.lmax; st->h1 = S.h1; st->h2 = S.h2; st->dtau = S.dtau;
-    }
-    return status;
+    C.fill(st, S, it_done);
+    return C.status;
 }
 
 
@@ -861,8 +846,8 @@ struct EnsHost {
     BC6<double> bc;
     BC6<float> bch;
     bool used, active, last_fp64;
-    int it_done, checks, converged, status;
-    double nF_abs, nF_rel, nF_ini;
+    int it_done;
+    DyrelCheck C;
 };
 
 unsigned long long mix_sig(unsigned long long h, unsigned long long v) {
@@ -1011,10 +996,7 @@ void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
         h.active = true;
         h.last_fp64 = false;
         h.it_done = 0;
-        h.checks = 0;
-        h.converged = 0;
-        h.status = HT3D_OK;
-        h.nF_abs = h.nF_rel = h.nF_ini = 0.0;
+        h.C = DyrelCheck();
     }
 
     // ---- launch groups of the members still iterating, for each block size;
@@ -1175,32 +1157,9 @@ void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
             for (int q = 0; q < n; ++q) {
                 EnsHost& h = H[q];
                 if (!h.active) continue;
-                const ht3d_dyrel_params* prm = in[q].prm;
                 const double nc = (double)in[q].nx * in[q].ny * in[q].nz;
-                ++h.checks;
-                const double s_abs = hres[3 * q], s_num = hres[3 * q + 1], s_den = hres[3 * q + 2];
-                h.nF_abs = s_abs / nc / sqrt(nc) * prm->norm_scale;
-                if (iter == 1) h.nF_ini = h.nF_abs;
-                h.nF_rel = h.nF_abs / h.nF_ini;
-                bool stop = false;
-                if (std::isnan(h.nF_abs)) {
-                    h.status = HT3D_ERR_NAN;
-                    stop = true;
-                } else if (h.nF_rel > 100) {
-                    h.status = HT3D_ERR_DIVERGED;
-                    stop = true;
-                } else {
-                    if (iter > 1) {
-                        h.S.lmin = fabs(s_num) / fabs(s_den);
-                        h.S.c = 2.0 * sqrt(h.S.lmin) * prm->cfact;
-                        h.S.h1 = (2 - h.S.c * h.S.dtau) / (2 + h.S.c * h.S.dtau);
-                        h.S.h2 = 2 * h.S.dtau / (2 + h.S.c * h.S.dtau);
-                    }
-                    if (h.nF_abs < prm->tol_abs || h.nF_rel < prm->tol_rel) {
-                        h.converged = 1;
-                        stop = true;
-                    }
-                }
+                const bool stop =
+                    h.C.update(h.S, in[q].prm, hres[3 * q], hres[3 * q + 1], hres[3 * q + 2], nc, iter, true);
                 if (stop) {
                     h.active = false;
                     --nactive;
@@ -1228,13 +1187,8 @@ void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
         }
         HT3D_LAUNCH(ctx, k_unpack, gc, b2, 0, I.F0, h.f32[2], h.P);
         if (!h.last_fp64) HT3D_LAUNCH(ctx, k_unpack, gc, b2, 0, I.F, h.f32[3], h.P);
-        if (I.st) {
-            ht3d_dyrel_stats* st = I.st;
-            st->iters = h.it_done; st->converged = h.converged; st->status = h.status; st->checks = h.checks;
-            st->nF_abs = h.nF_abs; st->nF_rel = h.nF_rel; st->nF_ini = h.nF_ini; st->lambda_min = h.S.lmin;
-            st->lambda_max = h.S.lmax; st->h1 = h.S.h1; st->h2 = h.S.h2; st->dtau = h.S.dtau;
-        }
-        in[q].status = h.status;
+        h.C.fill(I.st, h.S, h.it_done);
+        in[q].status = h.C.status;
     }
     timer.collect();
 }

@@ -670,8 +670,8 @@ int dim_dyrel(ht3d_ctx* ctx, double* X, DimWork& W, const double* wN, DimScal s,
     A.terms = W.terms; A.T0 = W.T0; A.rC = W.rC; A.Tex = W.Tex; A.prf0 = W.prf0; A.rfy = W.rfy;
     double* cur = X;
     double* nxt = W.X2;
-    double nF_abs = 0., nF_rel = 0., nF_ini = 0.;
-    int it_done = 0, converged = 0, status = HT3D_OK, checks = 0;
+    DyrelCheck C;
+    int it_done = 0;
     for (int iter = 1; iter <= prm->nitmax; ++iter) {
         const bool chk = is_check(iter, prm->nitout);
         const bool storef = !chk && (iter == prm->nitmax || is_check(iter + 1, prm->nitout));
@@ -684,30 +684,13 @@ int dim_dyrel(ht3d_ctx* ctx, double* X, DimWork& W, const double* wN, DimScal s,
         std::swap(cur, nxt);
         it_done = iter;
         if (chk) {
-            ++checks;
             tree_sum3(ctx, W.terms, n, W.terms + 3 * n);
-            const double s_abs = ctx->h_result[0], s_num = ctx->h_result[1], s_den = ctx->h_result[2];
-            nF_abs = s_abs / (double)n / sqrt((double)n) * prm->norm_scale;
-            if (iter == 1) nF_ini = nF_abs;
-            nF_rel = nF_abs / nF_ini;
-            if (std::isnan(nF_abs)) { status = HT3D_ERR_NAN; break; }
-            if (nF_rel > 100) { status = HT3D_ERR_DIVERGED; break; }
-            if (iter > 1) {
-                S.lmin = fabs(s_num) / fabs(s_den);
-                S.c = 2.0 * sqrt(S.lmin) * prm->cfact;
-                S.h1 = (2 - S.c * S.dtau) / (2 + S.c * S.dtau);
-                S.h2 = 2 * S.dtau / (2 + S.c * S.dtau);
-            }
-            if (nF_abs < prm->tol_abs || nF_rel < prm->tol_rel) { converged = 1; break; }
+            if (C.update(S, prm, ctx->h_result[0], ctx->h_result[1], ctx->h_result[2], (double)n, iter, true)) break;
         }
     }
     if (cur != X) HT3D_CUDA(cudaMemcpyAsync(X, cur, sizeof(double) * nex, cudaMemcpyDeviceToDevice, ctx->stream));
-    if (st) {
-        st->iters = it_done; st->converged = converged; st->status = status; st->checks = checks;
-        st->nF_abs = nF_abs; st->nF_rel = nF_rel; st->nF_ini = nF_ini; st->lambda_min = S.lmin;
-        st->lambda_max = S.lmax; st->h1 = S.h1; st->h2 = S.h2; st->dtau = S.dtau;
-    }
-    return status;
+    C.fill(st, S, it_done);
+    return C.status;
 }
 
 }  // namespace
