@@ -471,20 +471,27 @@ __global__ void __launch_bounds__(BS) k_ens_inner(const __grid_constant__ EnsLau
                        threadIdx.x & 31, live);
 }
 
-// FP64 check iteration of the mixed solver (see above).  FP64 fields in the
-// reference layout, FP32 fields in the padded layout.
+// FP64 check / refresh iteration of the mixed solver (see above).  FP64
+// fields in the reference layout, FP32 fields in the padded layout.  The fold
+// X + D and the residual are FP64; the quantities stored in FP32 (F, F0, the
+// next correction D) are formed in FP32 with the inner iteration's rounding
+// rules, and the Rayleigh-quotient terms are summed per thread in FP32 (they
+// only estimate lambda_min).  CHECK = false (a refresh between the
+// reference's checks) skips the check sums and the FP64 F.
+template <bool CHECK>
 __global__ void __launch_bounds__(TX* TY) k_mixed_check(
     const double* __restrict__ Xin, double* __restrict__ Xout, const float* __restrict__ Din, float* __restrict__ Dout,
     const double* __restrict__ R, const double* __restrict__ kx, const double* __restrict__ ky,
     const double* __restrict__ kz, const double* __restrict__ invPC, float* __restrict__ F0,
-    float* __restrict__ F32, double* __restrict__ F64, float* __restrict__ Rin, DyrelScal s, BC6<double> bc,
-    Pad p, int zchunk, double* __restrict__ partials) {
+    float* __restrict__ F32, double* __restrict__ F64, float* __restrict__ Rin, DyrelScal s, DyrelScalT<float> s32,
+    BC6<double> bc, Pad p, int zchunk, double* __restrict__ partials) {
     const int nx = p.nx, ny = p.ny, nz = p.nz;
     const int i = blockIdx.x * TX + threadIdx.x;
     const int j = blockIdx.y * TY + threadIdx.y;
     const int k0 = blockIdx.z * zchunk;
     const int k1 = min(nz, k0 + zchunk);
     double acc[3] = {0.0, 0.0, 0.0};
+    float rq_num = 0.f, rq_den = 0.f;
     if (i < nx && j < ny && k0 < k1) {
         const int n1 = nx + 2, n2 = ny + 2;
         const long long pl = (long long)n1 * n2, cpl = (long long)nx * ny, pp = p.plane;
@@ -517,17 +524,19 @@ __global__ void __launch_bounds__(TX* TY) k_mixed_check(
             const double qN = -kycol[fyo + nx] * (s._dy * (xn - xc));
             const double fu = R[c] + s.cX * xc + s._dx * (qE - qW) + s._dy * (qN - qS) + s._dz * (qF - qB);
             const double f = fu * invPC[c];
-            const double f0 = s.h1 * (double)F0[pc] + s.h2 * f;
-            const double fit = (double)F32[pc];
-            const double d = s.dtau * f0;
-            acc[0] += fabs(fu);
-            acc[1] += -d * (f - fit);
-            acc[2] += d * d;
-            F0[pc] = (float)f0;
-            F32[pc] = (float)f;
-            F64[c] = f;
+            const float f32 = (float)f;
+            const float f0 = __fmaf_rn(s32.h1, F0[pc], __fmul_rn(s32.h2, f32));
+            const float d = __fmul_rn(s32.dtau, f0);
+            if (CHECK) {
+                acc[0] += fabs(fu);
+                rq_num = __fmaf_rn(-d, __fsub_rn(f32, F32[pc]), rq_num);
+                rq_den = __fmaf_rn(d, d, rq_den);
+                F64[c] = f;
+            }
+            F0[pc] = f0;
+            F32[pc] = f32;
             Rin[pc] = (float)fu;
-            Dout[pc] = (float)(-d);
+            Dout[pc] = -d;
             ocol[e] = xc;
             if (i == 0) ocol[e - 1] = xw;
             if (i == nx - 1) ocol[e + 1] = xe;
@@ -540,6 +549,9 @@ __global__ void __launch_bounds__(TX* TY) k_mixed_check(
             qB = qF;
         }
     }
+    if (!CHECK) return;
+    acc[1] = (double)rq_num;
+    acc[2] = (double)rq_den;
     block_reduce<RED_SUM, 3>(acc);
     if (threadIdx.x == 0 && threadIdx.y == 0) {
         const long long b = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
@@ -707,6 +719,7 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
     DyrelCheck C;
     int it_done = 0;
     bool last_fp64 = false;  // the last iteration ran the FP64 kernel (check or refresh)
+    bool last_chk = false;   // ... and was a check (which writes the FP64 F)
     const int nmax = n_iter_fixed > 0 ? n_iter_fixed : prm->nitmax;
     const int refresh_every = ctx->mixed_refresh;
     auto is_fp64 = [&](int it) {
@@ -724,8 +737,13 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
         sc.dtau = S.dtau;
         if (chk || refresh) {
             timer.end();
-            HT3D_LAUNCH(ctx, k_mixed_check, LC.grid, LC.block, 0, xcur, xnxt, dcur, dnxt, R, kx, ky, kz, invPC, f0cur,
-                        Fs, F, Rin, sc, bc, P, LC.zchunk, parts);
+            const DyrelScalT<float> s32(sc);
+            if (chk)
+                HT3D_LAUNCH(ctx, k_mixed_check<true>, LC.grid, LC.block, 0, xcur, xnxt, dcur, dnxt, R, kx, ky, kz, invPC,
+                            f0cur, Fs, F, Rin, sc, s32, bc, P, LC.zchunk, parts);
+            else
+                HT3D_LAUNCH(ctx, k_mixed_check<false>, LC.grid, LC.block, 0, xcur, xnxt, dcur, dnxt, R, kx, ky, kz,
+                            invPC, f0cur, Fs, F, Rin, sc, s32, bc, P, LC.zchunk, parts);
             std::swap(xcur, xnxt);
         } else {
             const DyrelScalT<float> s32(sc);
@@ -765,6 +783,7 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
         std::swap(dcur, dnxt);
         it_done = iter;
         last_fp64 = chk || refresh;
+        last_chk = chk;
         if (chk) {
             HT3D_LAUNCH(ctx, (k_reduce_partials<RED_SUM, 3>), 1, 1024, 0, parts, (int)LC.nblocks, dres);
             ht3d_fetch_results(ctx, dres, 3);
@@ -781,7 +800,7 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
         HT3D_LAUNCH(ctx, k_copy_ex_faces<double>, g, b2, 0, X, xcur, nx, ny, nz);
     }
     HT3D_LAUNCH(ctx, k_unpack, gc, b2, 0, F0, f0cur, P);
-    if (!last_fp64) HT3D_LAUNCH(ctx, k_unpack, gc, b2, 0, F, Fs, P);
+    if (!last_chk) HT3D_LAUNCH(ctx, k_unpack, gc, b2, 0, F, Fs, P);
     if (derr) {  // a bounded wait of k_mixed_inner2 gave up
         int herr = 0;
         HT3D_CUDA(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -845,7 +864,7 @@ struct EnsHost {
     DyrelScal sc;
     BC6<double> bc;
     BC6<float> bch;
-    bool used, active, last_fp64;
+    bool used, active, last_fp64, last_chk;
     int it_done;
     DyrelCheck C;
 };
@@ -995,6 +1014,7 @@ void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
         h.xnxt = h.X2;
         h.active = true;
         h.last_fp64 = false;
+        h.last_chk = false;
         h.it_done = 0;
         h.C = DyrelCheck();
     }
@@ -1079,12 +1099,19 @@ void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
                 h.sc.h2 = h.S.h2;
                 h.sc.dtau = h.S.dtau;
                 const EnsSolveInst& I = in[q];
-                HT3D_LAUNCH(ctx, k_mixed_check, h.LC.grid, h.LC.block, 0, h.xcur, h.xnxt, h.f32[parity],
-                            h.f32[parity ^ 1], I.R, I.kx, I.ky, I.kz, h.invPC, h.f32[2], h.f32[3], I.F, h.f32[4], h.sc,
-                            h.bc, h.P, h.LC.zchunk, parts);
+                const DyrelScalT<float> s32(h.sc);
+                if (chk)
+                    HT3D_LAUNCH(ctx, k_mixed_check<true>, h.LC.grid, h.LC.block, 0, h.xcur, h.xnxt, h.f32[parity],
+                                h.f32[parity ^ 1], I.R, I.kx, I.ky, I.kz, h.invPC, h.f32[2], h.f32[3], I.F, h.f32[4],
+                                h.sc, s32, h.bc, h.P, h.LC.zchunk, parts);
+                else
+                    HT3D_LAUNCH(ctx, k_mixed_check<false>, h.LC.grid, h.LC.block, 0, h.xcur, h.xnxt, h.f32[parity],
+                                h.f32[parity ^ 1], I.R, I.kx, I.ky, I.kz, h.invPC, h.f32[2], h.f32[3], I.F, h.f32[4],
+                                h.sc, s32, h.bc, h.P, h.LC.zchunk, parts);
                 std::swap(h.xcur, h.xnxt);
                 h.it_done = iter;
                 h.last_fp64 = true;
+                h.last_chk = chk;
                 if (chk)
                     HT3D_LAUNCH(ctx, (k_reduce_partials<RED_SUM, 3>), 1, 1024, 0, parts, (int)h.LC.nblocks,
                                 dres + 3 * q);
@@ -1148,6 +1175,7 @@ void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
                 if (H[q].active) {
                     H[q].it_done = iter + window - 1;
                     H[q].last_fp64 = false;
+                    H[q].last_chk = false;
                 }
             iter += window - 1;
         }
@@ -1186,7 +1214,7 @@ void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
             HT3D_LAUNCH(ctx, k_copy_ex_faces<double>, g, b2, 0, I.X, h.xcur, nx, ny, nz);
         }
         HT3D_LAUNCH(ctx, k_unpack, gc, b2, 0, I.F0, h.f32[2], h.P);
-        if (!h.last_fp64) HT3D_LAUNCH(ctx, k_unpack, gc, b2, 0, I.F, h.f32[3], h.P);
+        if (!h.last_chk) HT3D_LAUNCH(ctx, k_unpack, gc, b2, 0, I.F, h.f32[3], h.P);
         h.C.fill(I.st, h.S, h.it_done);
         in[q].status = h.C.status;
     }
