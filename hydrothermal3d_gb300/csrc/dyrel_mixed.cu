@@ -270,21 +270,25 @@ __global__ void __launch_bounds__(TB_X* TB_Y, 2) k_mixed_inner2(const __grid_con
     extern __shared__ unsigned char tb_raw[];
     unsigned char* base = tb_raw + ((128 - (smem_u32(tb_raw) & 127)) & 127);
     TbStage* st = reinterpret_cast<TbStage*>(base);
-    float(*Dp)[TB_Y][TB_X] = reinterpret_cast<float(*)[TB_Y][TB_X]>(base + sizeof(TbStage) * TB_STAGES);
+    float* dpbuf = reinterpret_cast<float*>(base + sizeof(TbStage) * TB_STAGES);  // two D' planes
     uint64_t* bar = reinterpret_cast<uint64_t*>(base + sizeof(TbStage) * TB_STAGES + sizeof(float) * 2 * TB_Y * TB_X);
     __shared__ int abort_flag;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + TB_X * ty;
     const int x0 = blockIdx.x * (TB_X - 2) - 1, y0 = blockIdx.y * (TB_Y - 2) - 1;  // halo tile origin
     const int xD = (x0 - 1) & ~3, xK = x0 & ~3;  // 16-byte aligned box origins (floor)
-    const int oD = x0 - xD, oK = x0 - xK;        // column of this tile's x0 in the boxes
     const int gi = x0 + tx, gj = y0 + ty;
     const bool in = gi >= 0 && gi < p.nx && gj >= 0 && gj < p.ny;
     const bool inner = in && tx >= 1 && tx <= TB_X - 2 && ty >= 1 && ty <= TB_Y - 2;
+    const bool gW = gi == 0, gE = gi == p.nx - 1, gS = gj == 0, gN = gj == p.ny - 1;
     const int k0 = blockIdx.z * zchunk, k1 = min(p.nz, k0 + zchunk);
     const int pa0 = max(k0 - 1, 0);
     const int plast = min(k1 + 1, p.nz);  // last staged plane (plane nz: its bottom z-faces)
     const float h1 = s.h1, h2 = s.h2, dtau = s.dtau, cX = s.cX, _dx = s._dx, _dy = s._dy, _dz = s._dz;
     const float _dx2 = __fmul_rn(_dx, _dx), _dy2 = __fmul_rn(_dy, _dy), _dz2 = __fmul_rn(_dz, _dz);
+    // this thread's element offsets inside a stage's tiles (fixed over planes)
+    const int oD = (ty + 1) * TB_BW + tx + (x0 - xD);  // D centre
+    const int oK = ty * TB_BW + tx + (x0 - xK);        // faces / cell fields
+    const int oP = ty * TB_X + tx;                      // D' planes
     auto issue = [&](int k) {  // thread 0: the six boxes of plane k into slot k % TB_STAGES
         TbStage& S = st[k % TB_STAGES];
         uint64_t* b = &bar[k % TB_STAGES];
@@ -307,7 +311,18 @@ __global__ void __launch_bounds__(TB_X* TB_Y, 2) k_mixed_inner2(const __grid_con
         if (pa0 + 1 <= plast) issue(pa0 + 1);
     }
     int issued = min(pa0 + 1, plast);  // last plane whose copies are in flight or done
-    float dm1 = (pa0 > 0 && in) ? Din[p.plane * (pa0 - 1) + gi + (long long)p.PX * gj] : 0.f;  // D(p-1)
+    // rotating stage pointers (planes pl, pl + 1, pl + 2) and D' planes
+    const TbStage* S0 = &st[pa0 % TB_STAGES];
+    const TbStage* S1 = &st[(pa0 + 1) % TB_STAGES];
+    const TbStage* S2 = &st[(pa0 + 2) % TB_STAGES];
+    float* dpw = dpbuf + (pa0 & 1) * TB_Y * TB_X + oP;  // written by A at plane pl
+    float* dpr = dpbuf + ((pa0 + 1) & 1) * TB_Y * TB_X + oP;  // plane pl - 1, read by B
+    // running global addresses of this column for B's plane q = pl - 1
+    const long long colo = gi + (long long)p.PX * gj;
+    float* outD = Dout + colo + p.plane * (long long)(pa0 - 1);
+    float* outF0 = F0out + colo + p.plane * (long long)(pa0 - 1);
+    float* outF = F + colo + p.plane * (long long)(pa0 - 1);
+    float dm1 = (pa0 > 0 && in) ? Din[p.plane * (pa0 - 1) + colo] : 0.f;  // D(p-1)
     float dpm = 0.f, dpc = 0.f;
     float cW = 0.f, cE = 0.f, cS = 0.f, cN = 0.f, cB = 0.f, cF = 0.f, cr = 0.f, cf0 = 0.f;
     for (int pl = pa0; pl <= k1; ++pl) {
@@ -339,51 +354,60 @@ __global__ void __launch_bounds__(TB_X* TB_Y, 2) k_mixed_inner2(const __grid_con
         }
         float da = 0.f, aW = 0.f, aE = 0.f, aS = 0.f, aN = 0.f, aB = 0.f, aF = 0.f, ar = 0.f, af0 = 0.f;
         if (pl < p.nz) {
-            const TbStage& S = st[pl % TB_STAGES];
-            const TbStage& S1 = st[(pl + 1) % TB_STAGES];
-            const int cd = tx + oD, ck = tx + oK;
-            aW = S.kx[ty][ck];
-            aE = S.kx[ty][ck + 1];
-            aS = S.ky[ty][ck];
-            aN = S.ky[ty + 1][ck];
-            aB = S.kz[ty][ck];
-            aF = S1.kz[ty][ck];
-            ar = S.R[ty][ck];
-            const float f0o = S.F0[ty][ck];
-            const float xc = S.D[ty + 1][cd];
-            const float xw = (gi == 0) ? ghost(bc, 0, xc) : S.D[ty + 1][cd - 1];
-            const float xe = (gi == p.nx - 1) ? ghost(bc, 1, xc) : S.D[ty + 1][cd + 1];
-            const float xs = (gj == 0) ? ghost(bc, 2, xc) : S.D[ty][cd];
-            const float xn = (gj == p.ny - 1) ? ghost(bc, 3, xc) : S.D[ty + 2][cd];
+            const float* d0 = &S0->D[0][0] + oD;
+            const float* k0p = &S0->kx[0][0] + oK;
+            const float* y0p = &S0->ky[0][0] + oK;
+            aW = k0p[0];
+            aE = k0p[1];
+            aS = y0p[0];
+            aN = y0p[TB_BW];
+            aB = (&S0->kz[0][0])[oK];
+            aF = (&S1->kz[0][0])[oK];
+            ar = (&S0->R[0][0])[oK];
+            const float f0o = (&S0->F0[0][0])[oK];
+            const float xc = d0[0];
+            const float xw = gW ? ghost(bc, 0, xc) : d0[-1];
+            const float xe = gE ? ghost(bc, 1, xc) : d0[1];
+            const float xs = gS ? ghost(bc, 2, xc) : d0[-TB_BW];
+            const float xn = gN ? ghost(bc, 3, xc) : d0[TB_BW];
             const float xb = (pl == 0) ? ghost(bc, 4, xc) : dm1;
-            const float xf = (pl == p.nz - 1) ? ghost(bc, 5, xc) : S1.D[ty + 1][cd];
+            const float xf = (pl == p.nz - 1) ? ghost(bc, 5, xc) : (&S1->D[0][0])[oD];
             float f;
             mixed_cell(xc, xw, xe, xs, xn, xb, xf, aW, aE, aS, aN, aB, aF, ar, f0o, h1, h2, dtau, cX, _dx, _dy, _dz,
                        _dx2, _dy2, _dz2, f, af0, da);
             dm1 = xc;
-            Dp[pl & 1][ty][tx] = da;
+            *dpw = da;
         }
         __syncthreads();
-        const int q = pl - 1;
-        if (q >= k0 && inner) {
+        if (pl - 1 >= k0 && inner) {
+            const int q = pl - 1;
             const float xc = dpc;
-            const float xw = (gi == 0) ? ghost(bc, 0, xc) : Dp[q & 1][ty][tx - 1];
-            const float xe = (gi == p.nx - 1) ? ghost(bc, 1, xc) : Dp[q & 1][ty][tx + 1];
-            const float xs = (gj == 0) ? ghost(bc, 2, xc) : Dp[q & 1][ty - 1][tx];
-            const float xn = (gj == p.ny - 1) ? ghost(bc, 3, xc) : Dp[q & 1][ty + 1][tx];
+            const float xw = gW ? ghost(bc, 0, xc) : dpr[-1];
+            const float xe = gE ? ghost(bc, 1, xc) : dpr[1];
+            const float xs = gS ? ghost(bc, 2, xc) : dpr[-TB_X];
+            const float xn = gN ? ghost(bc, 3, xc) : dpr[TB_X];
             const float xb = (q == 0) ? ghost(bc, 4, xc) : dpm;
             const float xf = (q == p.nz - 1) ? ghost(bc, 5, xc) : da;
             float f, f0, xn1;
             mixed_cell(xc, xw, xe, xs, xn, xb, xf, cW, cE, cS, cN, cB, cF, cr, cf0, h1, h2, dtau, cX, _dx, _dy, _dz,
                        _dx2, _dy2, _dz2, f, f0, xn1);
-            const long long e = p.plane * q + gi + (long long)p.PX * gj;
-            Dout[e] = xn1;
-            F0out[e] = f0;
-            if (STOREF) F[e] = f;
+            *outD = xn1;
+            *outF0 = f0;
+            if (STOREF) *outF = f;
         }
+        outD += p.plane;
+        outF0 += p.plane;
+        outF += p.plane;
         dpm = dpc;
         dpc = da;
         cW = aW; cE = aE; cS = aS; cN = aN; cB = aB; cF = aF; cr = ar; cf0 = af0;
+        const TbStage* t = S0;
+        S0 = S1;
+        S1 = S2;
+        S2 = t;
+        float* u = dpw;
+        dpw = dpr;
+        dpr = u;
     }
 }
 constexpr size_t kTbSmem = 128 + sizeof(TbStage) * TB_STAGES + sizeof(float) * 2 * TB_Y * TB_X + 8 * TB_STAGES;

@@ -77,7 +77,7 @@ extern "C" {
                                        blocking, z-chunk chosen per grid), >= 2 = the same
                                        with that many planes per chunk; bit-identical
                                        results (on GB300 the two-iteration pass, TMA-staged,
-                                       is still instruction-issue bound and slower: 98.5
+                                       is still instruction-issue bound and slower: 95
                                        vs 86 us per iteration at 255^3)                  */
 
 typedef struct ht3d_ctx ht3d_ctx;
