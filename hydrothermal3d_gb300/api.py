@@ -27,7 +27,13 @@ class Ht3dError(RuntimeError):
 
 
 class Context:
-    """Owns one ht3d_ctx (one CUDA stream; scratch memory)."""
+    """Owns one ht3d_ctx (one CUDA stream; scratch memory).
+
+    stream: the cudaStream_t (int handle, e.g. torch.cuda.Stream().cuda_stream)
+    the library launches on; None gives the context a private non-blocking
+    stream.  Issue the torch work that produces a call's inputs on the same
+    stream (``with torch.cuda.stream(s)``), or synchronize it first: a private
+    stream is not ordered after torch's.  Calls are synchronous by default."""
 
     def __init__(self, device=0, stream=None, sync=True):
         self.lib = _lib.load()
@@ -37,6 +43,7 @@ class Context:
         if st != abi.OK:
             raise Ht3dError(st, self.lib.ht3d_status_string(st).decode())
         self.device = device
+        self.stream = s  # the stream handle the context was created on (0: a private stream)
         if not sync:
             self.lib.ht3d_ctx_set_sync(self.ptr, 0)
 

@@ -105,6 +105,12 @@ static inline int ht3d_guard(ht3d_ctx* ctx, Fn&& body, bool sync = true) {
 
 void* ht3d_scratch(ht3d_ctx* ctx, int slot, size_t bytes);
 
+// every pointer argument is set (entry points reject NULL before any launch)
+template <typename... P>
+static inline bool all_nonnull(P... p) {
+    return ((p != nullptr) && ...);
+}
+
 // ---------------------------------------------------------------------------
 // Launch helpers
 // ---------------------------------------------------------------------------

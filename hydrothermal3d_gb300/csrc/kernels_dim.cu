@@ -260,6 +260,7 @@ extern "C" {
 int ht3d_ComputeThermalConductivity(ht3d_ctx* ctx, double* ktv, const double* Tce, const double* phv, double phi0,
                                     double scale_kt, double scale_T, int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(ktv, Tce, phv), "null argument");
         DIMS;
         HT3D_LAUNCH(ctx, k_thermal_conductivity, G3(nx + 1, ny + 1, nz + 1), kBlock3, 0, ktv, Tce, phv, phi0, scale_kt,
                     scale_T, nx, ny, nz);
@@ -272,6 +273,7 @@ int ht3d_ComputeHydroConductivity(ht3d_ctx* ctx, double* kfv, const double* Tce,
                                   double scale_T, double scale_L, double scale_t, double scale_eta, int mode,
                                   const double* kmul_v, int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(kfv, Tce, Pce, phv), "null argument");
         DIMS;
         HT3D_REQUIRE(mode >= 1 && mode <= 3, "mode must be 1, 2 or 3");
         HT3D_LAUNCH(ctx, k_hydro_conductivity, G3(nx + 1, ny + 1, nz + 1), kBlock3, 0, kfv, Tce, Pce, phv, ymin, dy,
@@ -283,6 +285,7 @@ int ht3d_ComputeHydroConductivity(ht3d_ctx* ctx, double* kfv, const double* Tce,
 int ht3d_ComputeFluidDensity(ht3d_ctx* ctx, double* rhofv, const double* Tce, const double* Pce, const double* phv,
                              double scale_sigma, double scale_T, double scale_rho, int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(rhofv, Tce, Pce, phv), "null argument");
         DIMS;
         HT3D_LAUNCH(ctx, k_fluid_density, G3(nx + 1, ny + 1, nz + 1), kBlock3, 0, rhofv, Tce, Pce, phv, scale_sigma,
                     scale_T, scale_rho, nx, ny, nz);
@@ -292,6 +295,7 @@ int ht3d_ComputeFluidDensity(ht3d_ctx* ctx, double* rhofv, const double* Tce, co
 
 int ht3d_SmoothConductivityV2C(ht3d_ctx* ctx, double* ktc, const double* ktv, int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(ktc, ktv), "null argument");
         DIMS;
         HT3D_LAUNCH(ctx, k_smooth_v2c, G3(nx, ny, nz), kBlock3, 0, ktc, ktv, nx, ny, nz);
         return HT3D_OK;
@@ -300,6 +304,7 @@ int ht3d_SmoothConductivityV2C(ht3d_ctx* ctx, double* ktc, const double* ktv, in
 
 int ht3d_SmoothConductivityC2V(ht3d_ctx* ctx, double* ktv, const double* ktc, int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(ktv, ktc), "null argument");
         DIMS;
         if (nx > 1 && ny > 1 && nz > 1)
             HT3D_LAUNCH(ctx, k_smooth_c2v, G3(nx - 1, ny - 1, nz - 1), kBlock3, 0, ktv, ktc, nx, ny, nz);
@@ -309,6 +314,7 @@ int ht3d_SmoothConductivityC2V(ht3d_ctx* ctx, double* ktv, const double* ktc, in
 
 int ht3d_InitConductivity(ht3d_ctx* ctx, double* kx, double* ky, double* kz, const double* ktv, int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(kx, ky, kz, ktv), "null argument");
         DIMS;
         HT3D_LAUNCH(ctx, k_init_conductivity, G3(nx + 1, ny + 1, nz + 1), kBlock3, 0, kx, ky, kz, ktv, nx, ny, nz);
         return HT3D_OK;
@@ -319,6 +325,7 @@ int ht3d_ComputeRhoCeffective(ht3d_ctx* ctx, double* rhoC_eff, const double* Tc_
                               const double* phc_ex, double phi_i, double sca_T, double sca_sigma, double sca_C,
                               double sca_rho, int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(rhoC_eff, Tc_ex, Pc_ex, phc_ex), "null argument");
         DIMS;
         HT3D_LAUNCH(ctx, k_rhoC_eff, G3(nx, ny, nz), kBlock3, 0, rhoC_eff, Tc_ex, Pc_ex, phc_ex, phi_i, sca_T, sca_sigma,
                     sca_C, sca_rho, nx, ny, nz);
@@ -332,6 +339,7 @@ int ht3d_ResidualTemperatureLinearised(ht3d_ctx* ctx, double* F, const double* T
                                        double transient, double _dt, double _dx, double _dy, double _dz, int nx,
                                        int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(F, Tc_ex, Tc_old, rhoC_eff, phc_ex, PC, qx, qy, qz), "null argument");
         DIMS;
         HT3D_LAUNCH(ctx, k_res_temperature, G3(nx, ny, nz), kBlock3, 0, F, Tc_ex, Tc_old, rhoC_eff, phc_ex, PC, qx, qy,
                     qz, Qt, transient, _dt, _dx, _dy, _dz, nx, ny, nz);
@@ -374,6 +382,7 @@ int ht3d_SetPressureBCs_dim(ht3d_ctx* ctx, double* Pc_ex, const double* wN, cons
 int ht3d_PhiRhof(ht3d_ctx* ctx, double* phirhofc, const double* Tc_ex, const double* Pc_ex, const double* phc_ex,
                  double phi_i, double scale_rho, double scale_T, double scale_sigma, int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(phirhofc, Tc_ex, Pc_ex, phc_ex), "null argument");
         DIMS;
         HT3D_LAUNCH(ctx, k_phi_rhof, G3(nx, ny, nz), kBlock3, 0, phirhofc, Tc_ex, Pc_ex, phc_ex, phi_i, scale_rho,
                     scale_T, scale_sigma, 0, 0, nx, ny, nz);
@@ -384,6 +393,7 @@ int ht3d_PhiRhof(ht3d_ctx* ctx, double* phirhofc, const double* Tc_ex, const dou
 int ht3d_PhiRhofOld(ht3d_ctx* ctx, double* phirhofc, const double* Tc0, const double* Pc0, const double* phc_ex,
                     double phi_i, double scale_rho, double scale_T, double scale_sigma, int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(phirhofc, Tc0, Pc0, phc_ex), "null argument");
         DIMS;
         HT3D_LAUNCH(ctx, k_phi_rhof, G3(nx, ny, nz), kBlock3, 0, phirhofc, Tc0, Pc0, phc_ex, phi_i, scale_rho, scale_T,
                     scale_sigma, 1, 0, nx, ny, nz);
@@ -394,6 +404,7 @@ int ht3d_PhiRhofOld(ht3d_ctx* ctx, double* phirhofc, const double* Tc0, const do
 int ht3d_PhiDrhodP(ht3d_ctx* ctx, double* phidrhodP, const double* Tc_ex, const double* Pc_ex, const double* phc_ex,
                    double phi_i, double scale_rho, double scale_T, double scale_sigma, int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(phidrhodP, Tc_ex, Pc_ex, phc_ex), "null argument");
         DIMS;
         HT3D_LAUNCH(ctx, k_phi_rhof, G3(nx, ny, nz), kBlock3, 0, phidrhodP, Tc_ex, Pc_ex, phc_ex, phi_i, scale_rho,
                     scale_T, scale_sigma, 0, 1, nx, ny, nz);
@@ -405,6 +416,7 @@ int ht3d_ComputeDarcyFlux(ht3d_ctx* ctx, double* qx, double* qy, double* qz, con
                           const double* ky, const double* kz, const double* Pf, double g, double _dx, double _dy,
                           double _dz, int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(qx, qy, qz, rhofv, kx, ky, kz, Pf), "null argument");
         DIMS;
         HT3D_LAUNCH(ctx, k_darcy_flux, G3(nx + 1, ny + 1, nz + 1), kBlock3, 0, qx, qy, qz, rhofv, kx, ky, kz, Pf, g, _dx,
                     _dy, _dz, nx, ny, nz);
@@ -417,6 +429,7 @@ int ht3d_ResidualFluidPressure(ht3d_ctx* ctx, double* F, const double* phc_ex, c
                                const double* qz, double transient, double _dt, double _dx, double _dy, double _dz,
                                int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(F, phc_ex, phirhofc, phirhofc0, PC, qx, qy, qz), "null argument");
         DIMS;
         HT3D_LAUNCH(ctx, k_res_pressure, G3(nx, ny, nz), kBlock3, 0, F, phc_ex, phirhofc, phirhofc0, PC, qx, qy, qz,
                     transient, _dt, _dx, _dy, _dz, nx, ny, nz);
@@ -427,6 +440,7 @@ int ht3d_ResidualFluidPressure(ht3d_ctx* ctx, double* F, const double* phc_ex, c
 int ht3d_Init_vel_dim(ht3d_ctx* ctx, double* Vx, double* Vy, double* Vz, const double* qx, const double* qy,
                       const double* qz, const double* rhofv, int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(Vx, Vy, Vz, qx, qy, qz, rhofv), "null argument");
         DIMS;
         HT3D_LAUNCH(ctx, k_init_vel_dim, G3(nx + 1, ny + 1, nz + 1), kBlock3, 0, Vx, Vy, Vz, qx, qy, qz, rhofv, nx, ny,
                     nz);
@@ -436,6 +450,7 @@ int ht3d_Init_vel_dim(ht3d_ctx* ctx, double* Vx, double* Vy, double* Vz, const d
 
 int ht3d_material_law(ht3d_ctx* ctx, int which, const double* a, const double* b, double* out, long long n) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(a, out), "null argument");
         HT3D_REQUIRE(which >= 0 && which <= 9 && a && out && n >= 0, "bad argument");
         const unsigned g = (unsigned)std::max<long long>(1, std::min<long long>((n + 255) / 256, ctx->num_sms * 16LL));
         if (n) HT3D_LAUNCH(ctx, k_law_eval, g, 256, 0, out, a, b, which, n);

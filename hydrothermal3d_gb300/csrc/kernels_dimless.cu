@@ -242,6 +242,7 @@ int ht3d_Init_vel(ht3d_ctx* ctx, double* Vx, double* Vy, double* Vz, const doubl
                   const double* kz, const double* Pc_ex, const double* Ty, double Ra, double _dx, double _dy,
                   double _dz, int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(Vx, Vy, Vz, kx, ky, kz, Pc_ex, Ty), "null argument");
         DIMS_OK(1);
         HT3D_LAUNCH(ctx, k_init_vel, G3(nx + 1, ny + 1, nz + 1), kBlock3, 0, Vx, Vy, Vz, kx, ky, kz, Pc_ex, Ty, Ra,
                     _dx, _dy, _dz, nx, ny, nz);
@@ -253,6 +254,7 @@ int ht3d_InitDarcy(ht3d_ctx* ctx, double* Ty, double* kx, double* ky, double* kz
                    const double* kfv, double _dt, int nx, int ny, int nz) {
     (void)_dt;
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(Ty, kx, ky, kz, Tc_ex, kfv), "null argument");
         DIMS_OK(1);
         HT3D_LAUNCH(ctx, k_init_darcy, G3(nx + 1, ny + 1, nz + 1), kBlock3, 0, Ty, kx, ky, kz, Tc_ex, kfv, nx, ny, nz);
         return HT3D_OK;
@@ -262,6 +264,7 @@ int ht3d_InitDarcy(ht3d_ctx* ctx, double* Ty, double* kx, double* ky, double* kz
 int ht3d_Compute_Rp(ht3d_ctx* ctx, double* Rp, const double* ky, const double* Ty, double Ra, double _dy, int nx,
                     int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(Rp, ky, Ty), "null argument");
         DIMS_OK(1);
         HT3D_LAUNCH(ctx, k_compute_rp, G3(nx, ny, nz), kBlock3, 0, Rp, ky, Ty, Ra, _dy, nx, ny, nz);
         return HT3D_OK;
@@ -271,6 +274,7 @@ int ht3d_Compute_Rp(ht3d_ctx* ctx, double* Rp, const double* ky, const double* T
 int ht3d_InitThermal(ht3d_ctx* ctx, double* Rt, double* kx, double* ky, double* kz, const double* Tc_ex,
                      const double* ktv, double _dt, int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(Rt, kx, ky, kz, Tc_ex, ktv), "null argument");
         DIMS_OK(1);
         HT3D_LAUNCH(ctx, k_init_thermal, G3(nx + 1, ny + 1, nz + 1), kBlock3, 0, Rt, kx, ky, kz, Tc_ex, ktv, _dt, nx,
                     ny, nz);
@@ -281,6 +285,7 @@ int ht3d_InitThermal(ht3d_ctx* ctx, double* Rt, double* kx, double* ky, double* 
 int ht3d_ComputeFlux(ht3d_ctx* ctx, double* qx, double* qy, double* qz, const double* kx, const double* ky,
                      const double* kz, const double* A, double _dx, double _dy, double _dz, int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(qx, qy, qz, kx, ky, kz, A), "null argument");
         DIMS_OK(1);
         HT3D_LAUNCH(ctx, k_compute_flux, G3(nx + 1, ny + 1, nz + 1), kBlock3, 0, qx, qy, qz, kx, ky, kz, A, _dx, _dy,
                     _dz, nx, ny, nz);
@@ -291,6 +296,7 @@ int ht3d_ComputeFlux(ht3d_ctx* ctx, double* qx, double* qy, double* qz, const do
 int ht3d_UpdateT(ht3d_ctx* ctx, double* F, double* T, const double* R, const double* qx, const double* qy,
                  const double* qz, double _dt, double dtau, double _dx, double _dy, double _dz, int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(F, T, R, qx, qy, qz), "null argument");
         DIMS_OK(1);
         HT3D_LAUNCH(ctx, k_residual<0>, G3(nx, ny, nz), kBlock3, 0, F, T, R, qx, qy, qz, _dt, dtau, _dx, _dy, _dz, nx,
                     ny, nz);
@@ -301,6 +307,7 @@ int ht3d_UpdateT(ht3d_ctx* ctx, double* F, double* T, const double* R, const dou
 int ht3d_ResidualDiffusion(ht3d_ctx* ctx, double* F, const double* R, const double* qx, const double* qy,
                            const double* qz, double _dx, double _dy, double _dz, int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(F, R, qx, qy, qz), "null argument");
         DIMS_OK(1);
         HT3D_LAUNCH(ctx, k_residual<1>, G3(nx, ny, nz), kBlock3, 0, F, (double*)nullptr, R, qx, qy, qz, 0.0, 0.0, _dx,
                     _dy, _dz, nx, ny, nz);
@@ -312,6 +319,7 @@ int ht3d_ResidualDiffusionTransient(ht3d_ctx* ctx, double* F, const double* T, c
                                     const double* qy, const double* qz, double _dt, double _dx, double _dy,
                                     double _dz, int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(F, T, R, qx, qy, qz), "null argument");
         DIMS_OK(1);
         HT3D_LAUNCH(ctx, k_residual<2>, G3(nx, ny, nz), kBlock3, 0, F, (double*)T, R, qx, qy, qz, _dt, 0.0, _dx, _dy,
                     _dz, nx, ny, nz);
@@ -322,6 +330,7 @@ int ht3d_ResidualDiffusionTransient(ht3d_ctx* ctx, double* F, const double* T, c
 int ht3d_UpdateP(ht3d_ctx* ctx, double* F0, double* P, const double* F, double dampx, double dtau, int nx, int ny,
                  int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(F0, P, F), "null argument");
         DIMS_OK(1);
         HT3D_LAUNCH(ctx, k_update<0>, G3(nx, ny, nz), kBlock3, 0, F0, P, F, dampx, 0.0, dtau, nx, ny, nz);
         return HT3D_OK;
@@ -331,6 +340,7 @@ int ht3d_UpdateP(ht3d_ctx* ctx, double* F0, double* P, const double* F, double d
 int ht3d_DYRELUpdate(ht3d_ctx* ctx, double* F0, double* X, const double* F, double h1, double h2, double dtau,
                      int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(F0, X, F), "null argument");
         DIMS_OK(1);
         HT3D_LAUNCH(ctx, k_update<1>, G3(nx, ny, nz), kBlock3, 0, F0, X, F, h1, h2, dtau, nx, ny, nz);
         return HT3D_OK;
@@ -354,6 +364,7 @@ int ht3d_SetPressureBCs(ht3d_ctx* ctx, double* Pc_ex, double Pbot, double Ptop, 
 
 int ht3d_KillNorthSouthFluxes(ht3d_ctx* ctx, double* Ty, int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(Ty), "null argument");
         DIMS_OK(1);
         HT3D_LAUNCH(ctx, k_kill_ns, G3(nx, ny + 1, nz), kBlock3, 0, Ty, nx, ny, nz);
         return HT3D_OK;
@@ -362,6 +373,7 @@ int ht3d_KillNorthSouthFluxes(ht3d_ctx* ctx, double* Ty, int nx, int ny, int nz)
 
 int ht3d_ResetA(ht3d_ctx* ctx, double* A, double* B, long long n) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(A, B), "null argument");
         HT3D_REQUIRE(n >= 0, "negative size");
         if (n) HT3D_LAUNCH(ctx, k_reset2, g1(ctx, n), 256, 0, A, B, n);
         return HT3D_OK;
@@ -370,6 +382,7 @@ int ht3d_ResetA(ht3d_ctx* ctx, double* A, double* B, long long n) {
 
 int ht3d_Cpy_inn_to_all(ht3d_ctx* ctx, double* A, const double* B_ex, int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(A, B_ex), "null argument");
         DIMS_OK(1);
         HT3D_LAUNCH(ctx, k_cpy_inn<0>, G3(nx, ny, nz), kBlock3, 0, A, B_ex, nx, ny, nz);
         return HT3D_OK;
@@ -378,6 +391,7 @@ int ht3d_Cpy_inn_to_all(ht3d_ctx* ctx, double* A, const double* B_ex, int nx, in
 
 int ht3d_Cpy_all_to_inn(ht3d_ctx* ctx, double* A_ex, const double* B, int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(A_ex, B), "null argument");
         DIMS_OK(1);
         HT3D_LAUNCH(ctx, k_cpy_inn<1>, G3(nx, ny, nz), kBlock3, 0, A_ex, B, nx, ny, nz);
         return HT3D_OK;
@@ -386,6 +400,7 @@ int ht3d_Cpy_all_to_inn(ht3d_ctx* ctx, double* A_ex, const double* B, int nx, in
 
 int ht3d_ArrayEqualArray(ht3d_ctx* ctx, double* A, const double* B, long long n) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(A, B), "null argument");
         HT3D_REQUIRE(n >= 0, "negative size");
         if (n) HT3D_LAUNCH(ctx, k_copy, g1(ctx, n), 256, 0, A, B, n);
         return HT3D_OK;
@@ -394,6 +409,7 @@ int ht3d_ArrayEqualArray(ht3d_ctx* ctx, double* A, const double* B, long long n)
 
 int ht3d_Multiply(ht3d_ctx* ctx, double* a, const double* b, const double* c, long long n) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(a, c), "null argument");
         HT3D_REQUIRE(n >= 0, "negative size");
         if (n) HT3D_LAUNCH(ctx, k_mul, g1(ctx, n), 256, 0, a, b, c, n);
         return HT3D_OK;
@@ -404,6 +420,7 @@ int ht3d_GershgorinPoisson(ht3d_ctx* ctx, double* G, double* D, const double* rh
                            const double* ky, const double* kz, double transient, double dt, double dx, double dy,
                            double dz, int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(G, D, rhoC_eff, kx, ky, kz), "null argument");
         DIMS_OK(1);
         HT3D_LAUNCH(ctx, k_gershgorin<0>, G3(nx, ny, nz), kBlock3, 0, G, D, rhoC_eff, kx, ky, kz, transient, dt, dx, dy,
                     dz, nx, ny, nz);
@@ -415,6 +432,7 @@ int ht3d_GershgorinHydro(ht3d_ctx* ctx, double* G, const double* phidrhodP, cons
                          const double* kz, double transient, double dt, double dx, double dy, double dz, int nx,
                          int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(G, phidrhodP, kx, ky, kz), "null argument");
         DIMS_OK(1);
         HT3D_LAUNCH(ctx, k_gershgorin<1>, G3(nx, ny, nz), kBlock3, 0, G, (double*)nullptr, phidrhodP, kx, ky, kz,
                     transient, dt, dx, dy, dz, nx, ny, nz);
@@ -425,6 +443,7 @@ int ht3d_GershgorinHydro(ht3d_ctx* ctx, double* G, const double* phidrhodP, cons
 int ht3d_SwapDYREL(ht3d_ctx* ctx, double* Xc, double* Yc, const double* X0c_ex, const double* Y0c, int nx, int ny,
                    int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(Xc, Yc, X0c_ex, Y0c), "null argument");
         DIMS_OK(1);
         HT3D_LAUNCH(ctx, k_swap_dyrel, G3(nx, ny, nz), kBlock3, 0, Xc, Yc, X0c_ex, Y0c, nx, ny, nz);
         return HT3D_OK;
@@ -434,6 +453,7 @@ int ht3d_SwapDYREL(ht3d_ctx* ctx, double* Xc, double* Yc, const double* X0c_ex, 
 int ht3d_RayleighQuotientNumerator(ht3d_ctx* ctx, double* G, const double* Fc0, const double* Fcit, const double* Fc,
                                    double dtau, long long n) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(G, Fc0, Fcit, Fc), "null argument");
         HT3D_REQUIRE(n >= 0, "negative size");
         if (n) HT3D_LAUNCH(ctx, k_rayleigh<0>, g1(ctx, n), 256, 0, G, Fc0, Fcit, Fc, dtau, n);
         return HT3D_OK;
@@ -442,6 +462,7 @@ int ht3d_RayleighQuotientNumerator(ht3d_ctx* ctx, double* G, const double* Fc0, 
 
 int ht3d_RayleighQuotientDenominator(ht3d_ctx* ctx, double* G, const double* Fc0, double dtau, long long n) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(G, Fc0), "null argument");
         HT3D_REQUIRE(n >= 0, "negative size");
         if (n) HT3D_LAUNCH(ctx, k_rayleigh<1>, g1(ctx, n), 256, 0, G, Fc0, (const double*)nullptr, (const double*)nullptr, dtau, n);
         return HT3D_OK;

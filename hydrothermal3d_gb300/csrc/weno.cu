@@ -248,6 +248,7 @@ extern "C" {
 
 int ht3d_VPlusMinus(ht3d_ctx* ctx, double* Vm, double* Vp, const double* V, int axis, int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(Vm, Vp, V), "null argument");
         ht3d_check_dims(nx, ny, nz, 1);
         HT3D_REQUIRE(axis >= 0 && axis <= 2, "axis must be 0, 1 or 2");
         HT3D_LAUNCH(ctx, k_vplusminus, G3(nx, ny, nz), kBlock3, 0, Vm, Vp, V, axis, nx, ny, nz);
@@ -258,6 +259,7 @@ int ht3d_VPlusMinus(ht3d_ctx* ctx, double* Vm, double* Vp, const double* V, int 
 int ht3d_dFdx_Weno5(ht3d_ctx* ctx, double* dFdxi, const double* V1, const double* V2, const double* V3,
                     const double* V4, const double* V5, long long n) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(dFdxi, V1, V2, V3, V4, V5), "null argument");
         HT3D_REQUIRE(n >= 0, "negative size");
         if (n) HT3D_LAUNCH(ctx, k_dfdx, g1(ctx, n), 256, 0, dFdxi, V1, V2, V3, V4, V5, n);
         return HT3D_OK;
@@ -268,6 +270,7 @@ int ht3d_Gradients_Weno5(ht3d_ctx* ctx, double* v1, double* v2, double* v3, doub
                          const double* Fc_exxx, int axis, int sign, double _dx, double _dy, double _dz, int nx, int ny,
                          int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(v1, v2, v3, v4, v5, Fc_exxx), "null argument");
         ht3d_check_dims(nx, ny, nz, 1);
         HT3D_REQUIRE(axis >= 0 && axis <= 2 && (sign == 1 || sign == -1), "bad axis/sign");
         const double h = axis == 0 ? _dx : (axis == 1 ? _dy : _dz);
@@ -279,6 +282,7 @@ int ht3d_Gradients_Weno5(ht3d_ctx* ctx, double* v1, double* v2, double* v3, doub
 int ht3d_Boundaries_Weno5(ht3d_ctx* ctx, double* Fc_exxx, const double* Fc, int axis, int type_L, double val_L,
                           int type_R, double val_R, int fc_ghosted, int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(Fc_exxx, Fc), "null argument");
         ht3d_check_dims(nx, ny, nz, 3);
         HT3D_REQUIRE(axis >= 0 && axis <= 2, "axis must be 0, 1 or 2");
         HT3D_REQUIRE(type_L >= 0 && type_L <= 2 && type_R >= 0 && type_R <= 2, "BC type must be 0, 1 or 2");
@@ -292,6 +296,7 @@ int ht3d_Boundaries_Weno5(ht3d_ctx* ctx, double* Fc_exxx, const double* Fc, int 
 int ht3d_Advect_v1(ht3d_ctx* ctx, double* Fc, const double* Vxp, const double* dTdxm, const double* Vxm,
                    const double* dTdxp, double dt, long long n) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(Fc, Vxp, dTdxm, Vxm, dTdxp), "null argument");
         HT3D_REQUIRE(n >= 0, "negative size");
         if (n) HT3D_LAUNCH(ctx, k_advect_v1, g1(ctx, n), 256, 0, Fc, Vxp, dTdxm, Vxm, dTdxp, dt, n);
         return HT3D_OK;
@@ -300,6 +305,7 @@ int ht3d_Advect_v1(ht3d_ctx* ctx, double* Fc, const double* Vxp, const double* d
 
 int ht3d_TimeAveraging_v1(ht3d_ctx* ctx, double* Fc, const double* Fold, double order, long long n) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(Fc, Fold), "null argument");
         HT3D_REQUIRE(n >= 0, "negative size");
         if (n) HT3D_LAUNCH(ctx, k_timeavg_v1, g1(ctx, n), 256, 0, Fc, Fold, order, n);
         return HT3D_OK;
@@ -309,6 +315,7 @@ int ht3d_TimeAveraging_v1(ht3d_ctx* ctx, double* Fc, const double* Fold, double 
 int ht3d_Advect_v2(ht3d_ctx* ctx, double* Fc_ex, const double* X_exxx, const double* V, int axis, double dt,
                    double _dx, double _dy, double _dz, int quirk, int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(Fc_ex, X_exxx, V), "null argument");
         ht3d_check_dims(nx, ny, nz, 1);
         HT3D_REQUIRE(axis >= 0 && axis <= 2, "axis must be 0, 1 or 2");
         const double h = axis == 0 ? _dx : (axis == 1 ? _dy : _dz);
@@ -320,6 +327,7 @@ int ht3d_Advect_v2(ht3d_ctx* ctx, double* Fc_ex, const double* X_exxx, const dou
 
 int ht3d_TimeAveraging_v2(ht3d_ctx* ctx, double* Fc_ex, const double* Fold, double order, int nx, int ny, int nz) {
     return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(Fc_ex, Fold), "null argument");
         ht3d_check_dims(nx, ny, nz, 1);
         HT3D_LAUNCH(ctx, k_timeavg_v2, G3(nx, ny, nz), kBlock3, 0, Fc_ex, Fold, order, nx, ny, nz);
         return HT3D_OK;

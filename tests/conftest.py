@@ -26,13 +26,31 @@ def golden():
 
 
 @pytest.fixture(scope="session")
-def ctx():
+def gpu_stream():
+    """One CUDA stream for the GPU tests: the library context runs on it and
+    every GPU test issues its torch work (allocations, fills, copies) on it,
+    so the library's kernels are ordered after the inputs they read."""
     import torch
-    from hydrothermal3d_gb300 import Context
     assert torch.cuda.is_available(), "GPU tests need a CUDA device"
-    c = Context(device=0)
+    return torch.cuda.Stream()
+
+
+@pytest.fixture(scope="session")
+def ctx(gpu_stream):
+    from hydrothermal3d_gb300 import Context
+    c = Context(device=0, stream=gpu_stream.cuda_stream)
     yield c
     c.close()
+
+
+@pytest.fixture(autouse=True)
+def _torch_on_gpu_stream(request):
+    if request.node.get_closest_marker("gpu") is None:
+        yield
+        return
+    import torch
+    with torch.cuda.stream(request.getfixturevalue("gpu_stream")):
+        yield
 
 
 def rel_err(a, b, mask=None):

@@ -37,6 +37,7 @@ def test_struct_layouts_match(lib):
     assert lib.ht3d_sizeof_dyrel_stats() == ctypes.sizeof(abi.DyrelStats)
     assert lib.ht3d_sizeof_hrl_params() == ctypes.sizeof(abi.HrlParams)
     assert lib.ht3d_sizeof_instance() == ctypes.sizeof(abi.Instance)
+    assert lib.ht3d_sizeof_v18_params() == ctypes.sizeof(abi.V18Params)
 
 
 def test_status_strings(lib):

@@ -84,6 +84,13 @@ def test_property_kernels(ctx, orc):
     orc.call("ComputeRhoCeffective", rC, T, P, phc, p.phi_i, p.sc_T, p.sc_sigma, p.sc_C, p.sc_rho, nx, ny, nz)
     api.ComputeRhoCeffective(ctx, rCd, Td, Pd, phcd, p.phi_i, p.sc_T, p.sc_sigma, p.sc_C, p.sc_rho)
     assert rel_err(ht.to_numpy(rCd), rC) <= TOL
+    Tc0 = np.asfortranarray(T[1:-1, 1:-1, 1:-1] * 0.995)
+    Pc0 = np.asfortranarray(P[1:-1, 1:-1, 1:-1] * 1.003)
+    o, od = np.zeros((nx, ny, nz), order="F"), ht.zeros(nx, ny, nz)
+    orc.call("phi_rhof", o, Tc0, Pc0, phc, p.phi_i, p.sc_rho, p.sc_T, p.sc_sigma, ctypes.c_int(1), ctypes.c_int(0),
+             nx, ny, nz)
+    api.PhiRhofOld(ctx, od, ht.from_numpy(Tc0), ht.from_numpy(Pc0), phcd, p.phi_i, p.sc_rho, p.sc_T, p.sc_sigma)
+    assert rel_err(ht.to_numpy(od), o) <= TOL, "PhiRhofOld"
     for name, args, cell in (("PhiRhof", (T, P), 0), ("PhiDrhodP", (T, P), 0)):
         o, od = np.zeros((nx, ny, nz), order="F"), ht.zeros(nx, ny, nz)
         orc.call("phi_rhof", o, *args, phc, p.phi_i, p.sc_rho, p.sc_T, p.sc_sigma, ctypes.c_int(cell),

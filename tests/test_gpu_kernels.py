@@ -206,3 +206,91 @@ def test_weno_granular_v1_and_v2(ctx, orc, n):
             orc.call("Advect_v2", To, X, V, ctypes.c_int(axis), 0.01, *h, ctypes.c_int(quirk), nx, ny, nz)
             api.Advect_v2(ctx, Td, Xd, dev(V), axis, 0.01, *h, quirk=quirk)
             assert rel_err(host(Td), To) <= 1e-14
+
+
+@pytest.mark.parametrize("n", [(4, 3, 5), (33, 17, 9)])
+def test_weno_v1_pieces_and_copies(ctx, orc, n):
+    """Advect! / TimeAveraging! (v1 and v2), Cpy_inn_to_all!, ArrayEqualArray!."""
+    nx, ny, nz = n
+    N = nx * ny * nz
+    rng = np.random.default_rng(71)
+    F, Vp, dm, Vm, dp = (rnd(rng, nx, ny, nz) for _ in range(5))
+    Fo, Fd = F.copy(order="F"), dev(F)
+    orc.call("Advect_v1", Fo, Vp, dm, Vm, dp, 0.013, N)
+    api.Advect_v1(ctx, Fd, dev(Vp), dev(dm), dev(Vm), dev(dp), 0.013)
+    assert rel_err(host(Fd), Fo) <= TOL
+    Fold = rnd(rng, nx, ny, nz)
+    for order in (1.0, 2.0):
+        Fo, Fd = F.copy(order="F"), dev(F)
+        orc.call("TimeAveraging_v1", Fo, Fold, order, N)
+        api.TimeAveraging_v1(ctx, Fd, dev(Fold), order)
+        assert rel_err(host(Fd), Fo) <= TOL
+        Fex = rnd(rng, nx + 2, ny + 2, nz + 2)
+        Fo, Fd = Fex.copy(order="F"), dev(Fex)
+        orc.call("TimeAveraging_v2", Fo, Fold, order, nx, ny, nz)
+        api.TimeAveraging_v2(ctx, Fd, dev(Fold), order)
+        assert rel_err(host(Fd), Fo) <= TOL
+    Bex = rnd(rng, nx + 2, ny + 2, nz + 2)
+    A, Ad = np.zeros((nx, ny, nz), order="F"), ht.zeros(nx, ny, nz)
+    orc.call("Cpy_inn_to_all", A, Bex, nx, ny, nz)
+    api.Cpy_inn_to_all(ctx, Ad, dev(Bex))
+    assert np.array_equal(host(Ad), A) and np.array_equal(A, Bex[1:-1, 1:-1, 1:-1])
+    C, Cd = np.zeros((nx, ny, nz), order="F"), ht.zeros(nx, ny, nz)
+    orc.call("ArrayEqualArray", C, F, N)
+    api.ArrayEqualArray(ctx, Cd, dev(F))
+    assert np.array_equal(host(Cd), C) and np.array_equal(C, F)
+
+
+def test_dyrel_iterate_f32_tracks_fp64(ctx):
+    """The FP32 iteration on the reference layout (ht3d_dyrel_iterate_f32,
+    1/PC) follows the FP64 one (ht3d_dyrel_iterate, PC) to FP32 accuracy."""
+    nx, ny, nz = 19, 11, 7
+    rng = np.random.default_rng(73)
+    X = rnd(rng, nx + 2, ny + 2, nz + 2)
+    R = rnd(rng, nx, ny, nz)
+    k = [rnd(rng, *s, lo=0.5, hi=2.0) for s in ((nx + 1, ny, nz), (nx, ny + 1, nz), (nx, ny, nz + 1))]
+    PC = rnd(rng, nx, ny, nz, lo=600.0, hi=900.0)
+    bt, bv = abi.int6(0, 0, 1, 1, 0, 0), abi.dbl6(0, 0, 1.0, 0.0, 0, 0)
+    d = (1 / nx, 1 / ny, 1 / nz)
+    out = {}
+    for prec in ("f64", "f32"):
+        t = torch.float64 if prec == "f64" else torch.float32
+        Xd = dev(X).to(t).permute(2, 1, 0).contiguous().permute(2, 1, 0)
+        Rd, F0 = dev(R).to(t), ht.zeros(nx, ny, nz, dtype=t)
+        kd = [dev(a).to(t) for a in k]
+        Pd = dev(PC).to(t) if prec == "f64" else (1.0 / dev(PC)).to(t)
+        fields = [a.permute(2, 1, 0).contiguous().permute(2, 1, 0) for a in (Rd, *kd, Pd)]
+        name = "ht3d_dyrel_iterate" if prec == "f64" else "ht3d_dyrel_iterate_f32"
+        ctx.call(name, Xd.data_ptr(), *[a.data_ptr() for a in fields], F0.data_ptr(), 25.0, *d, bt, bv, 0.9, 0.05,
+                 0.0008, 30, nx, ny, nz)
+        out[prec] = Xd.double().cpu().numpy()
+    inner = (slice(1, -1),) * 3
+    du64, du32 = (out["f64"] - X)[inner], (out["f32"] - X)[inner]
+    assert rel_err(du32, du64) <= 1e-4
+
+
+def test_ctx_stream_and_sync_controls(ctx):
+    """ht3d_ctx_set_sync / _set_stream / _synchronize and the last-error text."""
+    lib = ctx.lib
+    s = torch.cuda.Stream()
+    assert lib.ht3d_ctx_set_stream(ctx.ptr, s.cuda_stream) == abi.OK
+    assert lib.ht3d_ctx_set_sync(ctx.ptr, 0) == abi.OK
+    a = ht.zeros(8, 8, 8) + 1.0
+    b = ht.zeros(8, 8, 8)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(s):
+        api.ArrayEqualArray(ctx, b, a)
+    assert lib.ht3d_ctx_synchronize(ctx.ptr) == abi.OK
+    assert float(b.min()) == 1.0
+    assert lib.ht3d_ctx_set_sync(ctx.ptr, 1) == abi.OK
+    assert lib.ht3d_ctx_set_stream(ctx.ptr, None) == abi.OK  # a private stream of its own
+    assert lib.ht3d_ctx_synchronize(ctx.ptr) == abi.OK
+    assert lib.ht3d_ctx_set_stream(ctx.ptr, ctx.stream) == abi.OK  # back to the tests' stream
+    # rejected calls (checked on the host before any launch) leave a readable
+    # message and an unchanged, usable context
+    p = a.data_ptr()
+    st = lib.ht3d_ComputeFlux(ctx.ptr, p, p, p, p, p, p, p, 1.0, 1.0, 1.0, 0, 4, 4)  # zero cells
+    assert st == abi.ERR_ARG and len(lib.ht3d_ctx_last_error(ctx.ptr)) > 0
+    st = lib.ht3d_ComputeFlux(ctx.ptr, None, None, None, None, None, None, None, 1.0, 1.0, 1.0, 4, 4, 4)
+    assert st == abi.ERR_ARG and b"null" in lib.ht3d_ctx_last_error(ctx.ptr)
+    api.ArrayEqualArray(ctx, b, a)
