@@ -572,6 +572,7 @@ def sweep_bench(ctx, stream, n, reps=3):
     from hydrothermal3d_gb300 import api, abi, sweep
     V = sweep.curl_velocity(n, n, n, seed=6)
     T0 = sweep.blob(n, n, n)
+    torch.cuda.synchronize()  # built on torch's stream; the sweeps run on the ctx stream
     dt = sweep.cfl_dt(n, n, n, cfl=0.5)
     h = (float(n),) * 3
     bc, bv = [0, 0, 1, 1, 0, 0], [0, 0, 1.0, 0.0, 0, 0]

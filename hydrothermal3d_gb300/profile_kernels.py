@@ -53,6 +53,7 @@ def main():
         PCx = ht.ones(n, n, n, dtype=dt) * (1.0 / pc if a.kernel == "dyrel_f32" else pc)
         F0 = ht.zeros(n, n, n, dtype=dt)
         name = "ht3d_dyrel_iterate_f32" if a.kernel == "dyrel_f32" else "ht3d_dyrel_iterate"
+        torch.cuda.synchronize()  # inputs were built on torch's stream
         args = lambda m: (X.data_ptr(), R.data_ptr(), k[0].data_ptr(), k[1].data_ptr(), k[2].data_ptr(),
                           PCx.data_ptr(), F0.data_ptr(), 0.0, d, d, d, bt, bv, 0.99, 0.05, 0.01, m, n, n, n)
         torch.cuda.synchronize()
@@ -74,6 +75,7 @@ def main():
         F, F0 = ht.zeros(n, n, n), ht.zeros(n, n, n)
         prm = abi.DyrelParams.reference()
         ctx.set_tuning(abi.TUNE_TIME_INNER, 1)
+        torch.cuda.synchronize()  # inputs were built on torch's stream
         with torch.cuda.stream(stream):
             api.dyrel_solve_dimless(ctx, X, R, *k, float(n * n), d, d, d, (0, 0, 1, 1, 0, 0), (0, 0, 1, 0, 0, 0), prm,
                                     F, F0, abi.MIXED, n_iter_fixed=a.iters)
@@ -91,6 +93,7 @@ def main():
             mem.append(api.Member(ht.from_numpy(T), ht.from_numpy(P), ht.from_numpy(ktv), ht.from_numpy(kfv),
                                   ht.zeros(nx + 1, ny, nz), ht.zeros(nx, ny + 1, nz), ht.zeros(nx, ny, nz + 1), p))
         ctx.set_tuning(abi.TUNE_TIME_INNER, 1)
+        torch.cuda.synchronize()  # inputs were built on torch's stream
         with torch.cuda.stream(stream):
             for _ in range(a.iters):
                 api.ensemble_step(ctx, mem, abi.MIXED)
@@ -104,6 +107,7 @@ def main():
         V = [v.float().permute(2, 1, 0).contiguous().permute(2, 1, 0) for v in sweep.curl_velocity(n, n, n, seed=6)]
         T = sweep.blob(n, n, n).float().permute(2, 1, 0).contiguous().permute(2, 1, 0)
         dtc = sweep.cfl_dt(n, n, n)
+        torch.cuda.synchronize()  # inputs were built on torch's stream
         run = lambda: api.weno5_advect_f32(ctx, T, *V, dtc, float(n), float(n), float(n), [0, 0, 1, 1, 0, 0],
                                            [0, 0, 1.0, 0.0, 0, 0], abi.WENO_V1)
         run()
@@ -120,6 +124,7 @@ def main():
         prec = abi.FP64 if a.kernel == "weno_f64" else abi.MIXED
         T = ht.zeros(n + 2, n + 2, n + 2).uniform_(0, 1)
         V = [ht.zeros(n + 1, n, n).uniform_(-1, 1), ht.zeros(n, n + 1, n).uniform_(-1, 1), ht.zeros(n, n, n + 1).uniform_(-1, 1)]
+        torch.cuda.synchronize()  # inputs were built on torch's stream
         args = (T.data_ptr(), V[0].data_ptr(), V[1].data_ptr(), V[2].data_ptr(), 0.1 * d, float(n), float(n), float(n),
                 abi.int6(0, 0, 1, 1, 0, 0), abi.dbl6(0, 0, 1, 0, 0, 0), abi.WENO_V1, prec, n, n, n)
         ctx.call("ht3d_weno5_advect", *args)
