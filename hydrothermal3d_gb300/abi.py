@@ -87,6 +87,16 @@ class HrlParams(ctypes.Structure):
     ]
 
 
+class KhaledGeom(ctypes.Structure):
+    """ht3d_khaled_geom: the detachment-fault geometry (lines y = a x + b)."""
+    _fields_ = [
+        ("y_plateau", ctypes.c_double),
+        ("surf_a1", ctypes.c_double),
+        ("surf_b1", ctypes.c_double),
+        ("fault", (ctypes.c_double * 6) * 4),
+    ]
+
+
 class Instance(ctypes.Structure):
     """ht3d_instance: one member of an ensemble (the arguments of one ht3d_step_hrl)."""
     _fields_ = [

@@ -108,8 +108,10 @@ def from_numpy(a, device="cuda"):
 
 
 def to_numpy(t):
-    """Device tensor -> Fortran-ordered numpy array of the same shape."""
+    """Device tensor (3-D, or 2-D like wN) -> Fortran-ordered numpy array of the same shape."""
     import numpy as np
+    if t.dim() == 2:
+        return np.asfortranarray(t.detach().t().contiguous().cpu().numpy().T)
     return np.asfortranarray(t.detach().permute(2, 1, 0).contiguous().cpu().numpy().transpose(2, 1, 0))
 
 
@@ -424,6 +426,16 @@ class Member:
         self.params = params
         self.st_thermal, self.st_darcy = abi.DyrelStats(), abi.DyrelStats()
         self.status = abi.OK
+
+
+def SetInitialConditions_Khaled(ctx, phc_ex, phv, wN, case, Tc_ex, Pc_ex):
+    """Device SetInitialConditions_Khaled; `case` is v18.khaled_case()'s dict."""
+    nx, ny, nz = case["nx"], case["ny"], case["nz"]
+    S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_SetInitialConditions_Khaled", _ptr(phc_ex, S["ex"], "phc_ex"), _ptr(phv, S["v"], "phv"),
+             _ptr(wN, (nx + 2, nz + 2), "wN"), ctypes.byref(case["geom"]), _ptr(Tc_ex, S["ex"], "Tc_ex"),
+             _ptr(Pc_ex, S["ex"], "Pc_ex"), case["Tbot"], case["Ttop"], case["Pbot"], case["Ptop"], case["xmin"],
+             case["ymin"], case["zmin"], case["xmax"], case["ymax"], case["zmax"], case["L"], nx, ny, nz)
 
 
 def ensemble_step(ctx, members, precision=abi.MIXED):

@@ -835,3 +835,129 @@ extern "C" int ht3d_step_v18(ht3d_ctx* ctx, double* Tc_ex, double* Pc_ex, const 
         return HT3D_OK;
     });
 }
+
+
+// ---------------------------------------------------------------------------
+// SetInitialConditions_Khaled (Dimensional/HydroThermal3D_v18.jl:59-129).
+// Every value is a pure function of the point's coordinates, so the
+// reference's sequence of whole-array statements (phase masks overriding one
+// another; T, P profiles followed by the x-, y- and z-ghost statements and the
+// air override) is evaluated per point in that order.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct KhaledArgs {
+    ht3d_khaled_geom g;
+    double Tbot, Ttop, Pbot, Ptop, xmin, ymin, zmin, xmax, ymax, zmax, L;
+    double dx, dy, dz, cos_t, sin_t;
+};
+
+// element i of Julia's LinRange(a, b, n): (1 - t) a + t b, t = i / (n - 1)
+__device__ __forceinline__ double linrange(double a, double b, long long n, long long i) {
+    const double t = (double)i / (double)(n - 1);
+    return (1.0 - t) * a + t * b;
+}
+
+// Topography (v18.jl:43-57)
+__device__ __forceinline__ double topography(double x, double y_plateau, double a2, double b2) {
+    const double xW = -b2 / a2;
+    const double xE = (y_plateau - b2) / a2;
+    if (x <= xW) return 0.0;
+    if (x >= xE) return y_plateau;
+    return a2 * x + b2;
+}
+
+__device__ double khaled_phase(double x, double y, double z, double y0, const KhaledArgs& A) {
+    double ph = 0.0;  // crust
+#pragma unroll
+    for (int f = 0; f < 4; ++f) {
+        const double* c = A.g.fault[f];
+        if (y < (x * c[0] + c[1]) && y > (x * c[2] + c[3]) && y > (x * c[4] + c[5])) ph = 2.0;
+    }
+    const double a = 1e3 / A.L, b = 10e3 / A.L, cz = 500e3 / A.L, z0 = A.zmax / 2;
+    const double x0 = 53057.07323 / A.L, yp = -8992.45195 / A.L;
+    const double u = ((x - x0) * A.cos_t - (y - yp) * A.sin_t) / a;
+    const double v = ((x - x0) * A.sin_t + (y - yp) * A.cos_t) / b;
+    const double w = (z - z0) / cz;
+    if (u * u + v * v + w * w < 1) ph = 3.0;
+    const double tiny = 1e-9;
+    if (y > (y0 - tiny)) ph = 1.0;  // air
+    return ph;
+}
+
+__global__ void k_khaled_vertices(double* __restrict__ phv, KhaledArgs A, int nx, int ny, int nz) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i > nx || j > ny || k > nz) return;
+    const double x = linrange(A.xmin, A.xmax, nx + 1, i), y = linrange(A.ymin, A.ymax, ny + 1, j),
+                 z = linrange(A.zmin, A.zmax, nz + 1, k);
+    const double y0 = topography(x, A.g.y_plateau, A.g.surf_a1, A.g.surf_b1);
+    phv[i + (long long)(nx + 1) * (j + (long long)(ny + 1) * k)] = khaled_phase(x, y, z, y0, A);
+}
+
+__device__ double khaled_field(double Vtop, double Vbot, int i, int j, const KhaledArgs& A, int n1, int n2) {
+    const double y_bot = -30e3 / A.L;
+    auto xce = [&](int ii) { return linrange(A.xmin - A.dx / 2, A.xmax + A.dx / 2, n1, ii); };
+    auto yce = [&](int jj) { return linrange(A.ymin - A.dy / 2, A.ymax + A.dy / 2, n2, jj); };
+    auto profile = [&](int ii, int jj) {
+        const double y0 = topography(xce(ii), A.g.y_plateau, A.g.surf_a1, A.g.surf_b1);
+        const double dVdy = (Vtop - Vbot) / (y0 - y_bot);
+        return Vtop + dVdy * (yce(jj) - y0);
+    };
+    auto vx = [&](int ii, int jj) { return profile(ii == 0 ? 1 : (ii == n1 - 1 ? n1 - 2 : ii), jj); };
+    double v;
+    if (j == 0) v = 2 * Vbot - vx(i, 1);
+    else if (j == n2 - 1) v = 2 * Vtop - vx(i, n2 - 2);
+    else v = vx(i, j);
+    const double x = xce(i), y = yce(j);
+    if ((y > 0 && (y > (x * A.g.surf_a1 + A.g.surf_b1))) || y > A.g.y_plateau) v = Vtop;
+    return v;
+}
+
+__global__ void k_khaled_cells(double* __restrict__ phc, double* __restrict__ T, double* __restrict__ P, KhaledArgs A,
+                               int nx, int ny, int nz) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    const int n1 = nx + 2, n2 = ny + 2, n3 = nz + 2;
+    if (i >= n1 || j >= n2 || k >= n3) return;
+    const long long e = i + (long long)n1 * (j + (long long)n2 * k);
+    const double x = linrange(A.xmin - A.dx / 2, A.xmax + A.dx / 2, n1, i);
+    const double y = linrange(A.ymin - A.dy / 2, A.ymax + A.dy / 2, n2, j);
+    const double z = linrange(A.zmin - A.dz / 2, A.zmax + A.dz / 2, n3, k);
+    const double y0 = topography(x, A.g.y_plateau, A.g.surf_a1, A.g.surf_b1);
+    phc[e] = khaled_phase(x, y, z, y0, A);
+    T[e] = khaled_field(A.Ttop, A.Tbot, i, j, A, n1, n2);
+    P[e] = khaled_field(A.Ptop, A.Pbot, i, j, A, n1, n2);
+}
+
+}  // namespace
+
+extern "C" int ht3d_SetInitialConditions_Khaled(ht3d_ctx* ctx, double* phc_ex, double* phv, double* wN,
+                                                const ht3d_khaled_geom* geom, double* Tc_ex, double* Pc_ex,
+                                                double Tbot, double Ttop, double Pbot, double Ptop, double xmin,
+                                                double ymin, double zmin, double xmax, double ymax, double zmax,
+                                                double L, int nx, int ny, int nz) {
+    (void)wN;
+    return ht3d_guard(ctx, [&]() {
+        HT3D_REQUIRE(all_nonnull(phc_ex, phv, geom, Tc_ex, Pc_ex), "null argument");
+        ht3d_check_dims(nx, ny, nz, 1);
+        HT3D_REQUIRE(xmax > xmin && ymax > ymin && zmax > zmin && L > 0, "empty domain");
+        KhaledArgs A;
+        A.g = *geom;
+        A.Tbot = Tbot; A.Ttop = Ttop; A.Pbot = Pbot; A.Ptop = Ptop;
+        A.xmin = xmin; A.ymin = ymin; A.zmin = zmin; A.xmax = xmax; A.ymax = ymax; A.zmax = zmax; A.L = L;
+        A.dx = (xmax - xmin) / nx;
+        A.dy = (ymax - ymin) / ny;
+        A.dz = (zmax - zmin) / nz;
+        const double t_ta = 60 * (M_PI / 180);  // the pluton's rotation, evaluated on the host like the oracle's
+        A.cos_t = cos(t_ta);
+        A.sin_t = sin(t_ta);
+        const dim3 b(32, 8, 1);
+        HT3D_LAUNCH(ctx, k_khaled_vertices, dim3((nx + 1 + 31) / 32, (ny + 1 + 7) / 8, nz + 1), b, 0, phv, A, nx, ny, nz);
+        HT3D_LAUNCH(ctx, k_khaled_cells, dim3((nx + 2 + 31) / 32, (ny + 2 + 7) / 8, nz + 2), b, 0, phc_ex, Tc_ex, Pc_ex,
+                    A, nx, ny, nz);
+        return HT3D_OK;
+    });
+}

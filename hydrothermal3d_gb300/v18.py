@@ -117,3 +117,47 @@ def bytes_per_iteration(nx, ny, nz, s=8):
     + phase: 11 N s + N.  Returns (thermal, darcy)."""
     N = nx * ny * nz
     return 10 * N * s + N, 11 * N * s + N
+
+
+def _slope(x1, x2, y1, y2):
+    """a(x1, x2, y1, y2) of v18.jl:40: slope of the line through two points."""
+    return (y1 - y2) / (x1 - x2)
+
+
+def _intercept(x1, x2, y1, y2):
+    """b(x1, x2, y1, y2) of v18.jl:41: its intercept."""
+    return y1 - x1 * (y1 - y2) / (x1 - x2)
+
+
+def khaled_case(nx=250, ny=106, nz=3):
+    """The detachment-fault model of the v18 driver (Dimensional/HydroThermal3D_v18.jl:162-287):
+    domain, boundary values and the geometry of the main detachment, three
+    secondary faults and the topography, in scaled units.  Returns a dict of
+    the arguments of SetInitialConditions_Khaled.  The default grid is the
+    driver's fact = 8 grid (ncx = 8*32-6, ncy = 8*14-6, ncz = 3); zmin is the
+    driver's -25 m as written there."""
+    sc = scaling()
+    L = sc["L"]
+    # corner points of each wedge: three lines (top, bottom, closing edge), v18.jl:184-233
+    corners = {
+        "fault": ((75.8e3, 31498.437753425103, 3e3, -16897.187956165293),
+                  (32000.0, 77e3, -17800.0, 3e3),
+                  (32000.0, 31498.437753425103, -17800.0, -16897.187956165293)),
+        "fault1": ((59.5e3, 62.5e3, 0e3, -3e3), (61.8e3, 58.8e3, -3e3, 0e3), (62.5e3, 61.8e3, -3e3, -3e3)),
+        "fault2": ((48.5e3, 54.5e3, 0e3, -7e3), (53.8e3, 47.8e3, -7e3, 0e3), (54.5e3, 53.8e3, -7e3, -7e3)),
+        "fault3": ((36.8e3, 46.8e3, 0e3, -10.5e3), (46e3, 36e3, -10.5e3, 0e3), (46.8e3, 46e3, -10.5e3, -10.5e3)),
+    }
+    g = abi.KhaledGeom()
+    g.y_plateau = 1.5e3 / L
+    sx1, sx2, sy1, sy2 = 32000.0 / L, 69397.54576150524 / L, -17800.0 / L, 0.0 / L
+    g.surf_a1, g.surf_b1 = _slope(sx1, sx2, sy1, sy2), _intercept(sx1, sx2, sy1, sy2)
+    for f, name in enumerate(("fault", "fault1", "fault2", "fault3")):
+        for e, (x1, x2, y1, y2) in enumerate(corners[name]):
+            x1, x2, y1, y2 = x1 / L, x2 / L, y1 / L, y2 / L
+            g.fault[f][2 * e] = _slope(x1, x2, y1, y2)
+            g.fault[f][2 * e + 1] = _intercept(x1, x2, y1, y2)
+    Ttop = 293.15 / sc["T"]
+    Ptop = 1e5 / sc["sigma"]
+    return dict(geom=g, Tbot=Ttop + 600.0 / sc["T"], Ttop=Ttop, Pbot=Ptop + 294e6 / sc["sigma"], Ptop=Ptop,
+                xmin=30e3 / L, ymin=-30e3 / L, zmin=-25.0 / L, xmax=100e3 / L, ymax=5e3 / L, zmax=25e3 / L, L=L,
+                nx=nx, ny=ny, nz=nz)

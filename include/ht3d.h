@@ -463,7 +463,29 @@ typedef struct ht3d_instance {
    the first failing member's status, or HT3D_OK. */
 int ht3d_ensemble_step(ht3d_ctx* ctx, ht3d_instance* members, int n_members, int precision);
 
-/* One time step of the dimensional model, Dimensional/HydroThermal3D_v18.jl:404-572:
+/* Geometry of the detachment-fault model: the driver's `geometry` NamedTuple
+   (Dimensional/HydroThermal3D_v18.jl:236-287), lines y = a x + b. */
+typedef struct ht3d_khaled_geom {
+    double y_plateau;
+    double surf_a1, surf_b1;   /* topography slope */
+    double fault[4][6];        /* detachment, fault1, fault2, fault3: a1, b1, a2, b2, a3, b3 */
+} ht3d_khaled_geom;
+
+/* SetInitialConditions_Khaled (Dimensional/HydroThermal3D_v18.jl:59-129) on the
+   device: phases of the ghosted cells (phc_ex) and vertices (phv) -- crust 0,
+   fault wedges 2, rotated pluton 3, air 1 above the topography -- and the
+   initial T and P (linear from the topography down to y = -30 km in scaled
+   units L, ghost rules and the air override of the reference).  The grid is
+   the driver's: cell centres LinRange(xmin - dx/2, xmax + dx/2, nx + 2), vertices
+   LinRange(xmin, xmax, nx + 1).  wN is left unchanged, as in the reference (its
+   loop looks for phase -1, which the function never assigns).  geom is a host
+   pointer. */
+int ht3d_SetInitialConditions_Khaled(ht3d_ctx* ctx, double* phc_ex, double* phv, double* wN,
+                                     const ht3d_khaled_geom* geom, double* Tc_ex, double* Pc_ex, double Tbot,
+                                     double Ttop, double Pbot, double Ptop, double xmin, double ymin, double zmin,
+                                     double xmax, double ymax, double zmax, double L, int nx, int ny, int nz);
+
+/* One time step of the dimensional model/* One time step of the dimensional model, Dimensional/HydroThermal3D_v18.jl:404-572:
    pluton insertion at it == 1, thermal DYREL solve (conductivity, smoothing,
    ρC_eff, Gershgorin), Darcy DYREL solve (ρk/μ, ϕ∂ρ/∂P, ϕρf_old, ρf), Darcy
    velocity and WENO5-v2 advection with sub-stepping.  phc_ex (ex) and phv

@@ -1156,3 +1156,106 @@ int orc_step_v18(double* T, double* P, const double* phc, const double* phv, con
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// SetInitialConditions_Khaled (Dimensional/HydroThermal3D_v18.jl:59-129) and
+// Topography (v18.jl:43-57): phases, T and P of the dimensional model's
+// detachment-fault geometry.  The grid coordinates are the driver's
+// (v18.jl:355-367): ghosted cell centres xce = LinRange(xmin-dx/2, xmax+dx/2,
+// nx+2), vertices xv = LinRange(xmin, xmax, nx+1); Julia evaluates element i
+// of LinRange(a, b, n) as (1-t)*a + t*b with t = i/(n-1).
+// ---------------------------------------------------------------------------
+extern "C" {
+
+struct orc_khaled_geom {      // the driver's `geometry` NamedTuple (v18.jl:236-287)
+    double y_plateau;
+    double surf_a1, surf_b1;
+    double fault[4][6];       // detachment, fault1, fault2, fault3: a1, b1, a2, b2, a3, b3
+};
+
+static double orc_linrange(double a, double b, i64 n, i64 i) {
+    const double t = (double)i / (double)(n - 1);
+    return (1.0 - t) * a + t * b;
+}
+
+static double orc_topography(double x, double y_plateau, double a2, double b2) {
+    const double xW = -b2 / a2;
+    const double xE = (y_plateau - b2) / a2;
+    if (x <= xW) return 0.0;
+    if (x >= xE) return y_plateau;
+    return a2 * x + b2;
+}
+
+static double orc_khaled_phase(double x, double y, double z, double y0, const orc_khaled_geom* g, double L,
+                               double zmax) {
+    double ph = 0.0;  // crust
+    for (int f = 0; f < 4; ++f) {
+        const double* c = g->fault[f];
+        if (y < (x * c[0] + c[1]) && y > (x * c[2] + c[3]) && y > (x * c[4] + c[5])) ph = 2.0;
+    }
+    // pluton: an ellipsoid rotated by 60 degrees in the x-y plane
+    const double a = 1e3 / L, b = 10e3 / L, cz = 500e3 / L, z0 = zmax / 2;
+    const double x0 = 53057.07323 / L, yp = -8992.45195 / L;
+    const double t_ta = 60 * (M_PI / 180);
+    const double u = ((x - x0) * cos(t_ta) - (y - yp) * sin(t_ta)) / a;
+    const double v = ((x - x0) * sin(t_ta) + (y - yp) * cos(t_ta)) / b;
+    const double w = (z - z0) / cz;
+    if (u * u + v * v + w * w < 1) ph = 3.0;
+    const double tiny = 1e-9;
+    if (y > (y0 - tiny)) ph = 1.0;  // air
+    return ph;
+}
+
+void orc_SetInitialConditions_Khaled(double* phc, double* phv, double* wN, const orc_khaled_geom* g, double* Tc_ex,
+                                     double* Pc_ex, double Tbot, double Ttop, double Pbot, double Ptop, double xmin,
+                                     double ymin, double zmin, double xmax, double ymax, double zmax, double L, i64 nx,
+                                     i64 ny, i64 nz) {
+    (void)wN;  // the weight loop looks for phase -1, which is never assigned: wN keeps its values
+    const double dx = (xmax - xmin) / nx, dy = (ymax - ymin) / ny, dz = (zmax - zmin) / nz;
+    const i64 n1 = nx + 2, n2 = ny + 2, n3 = nz + 2;
+    auto xce = [&](i64 i) { return orc_linrange(xmin - dx / 2, xmax + dx / 2, n1, i); };
+    auto yce = [&](i64 j) { return orc_linrange(ymin - dy / 2, ymax + dy / 2, n2, j); };
+    auto zce = [&](i64 k) { return orc_linrange(zmin - dz / 2, zmax + dz / 2, n3, k); };
+    // vertices
+    for (i64 k = 0; k <= nz; ++k)
+        for (i64 j = 0; j <= ny; ++j)
+            for (i64 i = 0; i <= nx; ++i) {
+                const double x = orc_linrange(xmin, xmax, nx + 1, i), y = orc_linrange(ymin, ymax, ny + 1, j),
+                             z = orc_linrange(zmin, zmax, nz + 1, k);
+                const double y0 = orc_topography(x, g->y_plateau, g->surf_a1, g->surf_b1);
+                phv[i + (nx + 1) * (j + (ny + 1) * k)] = orc_khaled_phase(x, y, z, y0, g, L, zmax);
+            }
+    // cells (ghosted): phases, then T and P as the sequence of whole-array statements
+    const double y_bot = -30e3 / L;
+    auto profile = [&](double V0top, double Vbot, i64 i, i64 j) {
+        const double y0 = orc_topography(xce(i), g->y_plateau, g->surf_a1, g->surf_b1);
+        const double dVdy = (V0top - Vbot) / (y0 - y_bot);
+        return V0top + dVdy * (yce(j) - y0);
+    };
+    auto field = [&](double Vtop, double Vbot, i64 i, i64 j, i64 k) {
+        // V = profile; x ghosts copy; y ghosts Dirichlet (2 Vbot / 2 Vtop - inner); z: last plane copies
+        auto vx = [&](i64 ii, i64 jj) { return profile(Vtop, Vbot, ii == 0 ? 1 : (ii == n1 - 1 ? n1 - 2 : ii), jj); };
+        auto vy = [&](i64 ii, i64 jj) {
+            if (jj == 0) return 2 * Vbot - vx(ii, 1);
+            if (jj == n2 - 1) return 2 * Vtop - vx(ii, n2 - 2);
+            return vx(ii, jj);
+        };
+        (void)k;  // the profile does not depend on z; the z-ghost statements copy equal values
+        double v = vy(i, j);
+        const double x = xce(i), y = yce(j);
+        if ((y > 0 && (y > (x * g->surf_a1 + g->surf_b1))) || y > g->y_plateau) v = Vtop;
+        return v;
+    };
+    for (i64 k = 0; k < n3; ++k)
+        for (i64 j = 0; j < n2; ++j)
+            for (i64 i = 0; i < n1; ++i) {
+                const i64 e = i + n1 * (j + n2 * k);
+                const double x = xce(i), y = yce(j), z = zce(k);
+                const double y0 = orc_topography(x, g->y_plateau, g->surf_a1, g->surf_b1);
+                phc[e] = orc_khaled_phase(x, y, z, y0, g, L, zmax);
+                Tc_ex[e] = field(Ttop, Tbot, i, j, k);
+                Pc_ex[e] = field(Ptop, Pbot, i, j, k);
+            }
+}
+
+}  // extern "C"

@@ -3,6 +3,8 @@
 The material laws call pow/exp, whose last bit may differ between CUDA's and
 the host's math library; granular kernels are therefore compared at 1e-13
 (relative, max-norm), full solves at 1e-10."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -173,3 +175,29 @@ def test_step_v18_matches_oracle(ctx, orc, n):
         assert p_d.n_adv == p_o.n_adv
         assert rel_err(ht.to_numpy(Td)[1:-1, 1:-1, 1:-1], T[1:-1, 1:-1, 1:-1]) <= 1e-10
         assert rel_err(ht.to_numpy(Pd)[1:-1, 1:-1, 1:-1], P[1:-1, 1:-1, 1:-1]) <= 1e-10
+
+
+@pytest.mark.parametrize("grid", [(250, 106, 3), (47, 31, 9)])
+def test_set_initial_conditions_khaled(ctx, orc, grid):
+    """Device SetInitialConditions_Khaled against the oracle: phases of cells
+    and vertices, T and P identical; every phase present on the driver's grid;
+    wN untouched."""
+    from hydrothermal3d_gb300 import v18
+    case = v18.khaled_case(*grid)
+    nx, ny, nz = grid
+    phc, phv = np.zeros((nx + 2, ny + 2, nz + 2), order="F"), np.zeros((nx + 1, ny + 1, nz + 1), order="F")
+    T, P = np.zeros_like(phc, order="F"), np.zeros_like(phc, order="F")
+    wN = np.asfortranarray(np.full((nx + 2, nz + 2), 0.25))
+    orc.call("SetInitialConditions_Khaled", phc, phv, wN, ctypes.byref(case["geom"]), T, P, case["Tbot"],
+             case["Ttop"], case["Pbot"], case["Ptop"], case["xmin"], case["ymin"], case["zmin"], case["xmax"],
+             case["ymax"], case["zmax"], case["L"], nx, ny, nz)
+    d = [ht.zeros(*a.shape) for a in (phc, phv, T, P)]
+    wNd = ht.from_numpy(wN)
+    api.SetInitialConditions_Khaled(ctx, d[0], d[1], wNd, case, d[2], d[3])
+    for a, b in zip(d, (phc, phv, T, P)):
+        np.testing.assert_array_equal(ht.to_numpy(a), b)
+    np.testing.assert_array_equal(ht.to_numpy(wNd), wN)
+    if grid == (250, 106, 3):
+        assert set(np.unique(phc)) == {0.0, 1.0, 2.0, 3.0}
+    inner = (slice(1, -1),) * 3
+    assert T[inner].max() <= case["Tbot"] and T[inner].min() >= case["Ttop"] - 1e-12
