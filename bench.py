@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--ens-members", type=int, default=64)
     ap.add_argument("--ens-steps", type=int, default=20)
     ap.add_argument("--skip-ensemble", action="store_true")
+    ap.add_argument("--post-n", type=int, default=255, help="cells per axis of the output-diagnostics pass (0 = skip)")
     ap.add_argument("--sweep-n", type=int, default=511, help="cells per axis of the standalone WENO5 sweep (0 = skip)")
     ap.add_argument("--c63-steps", type=int, default=10,
                     help="time steps of the 63^3 HRL case (config 1): oracle on the host cores and GPU forms "
@@ -376,6 +377,8 @@ def run_ours(a):
         out["error_growth_127"] = growth_bench(ctx, stream, a.growth_steps)
     if a.c63_steps and rank == 0:
         out["config_63"] = c63_bench(ctx, stream, a.c63_steps)
+    if a.post_n:
+        out["diagnostics"] = post_bench(ctx, stream, a.post_n)
 
     if rank == 0:
         v, cores, desc, _ = cpu_sample(n, a.cpu_seconds, threads=os.cpu_count())
@@ -672,6 +675,41 @@ def v18_bench(ctx, stream, steps, n=127):
             "per_step": rows, "dtype": "f64",
             "case": "10x10x5 km box, T 600->20 C, log10 k ~ N(-15, 0.5) with 500 m correlation (seed 2), "
                     "DYREL tol 1e-10 relative, nitmax 1e4, WENO5 v2 with the reference's stencil, CFL 0.5"}
+
+
+def post_bench(ctx, stream, n, reps=5):
+    """Output diagnostics of the v18 VTK step at n^3: the reference's ten
+    kernels one after another against the fused single pass (bit-identical
+    fields), and the Nusselt reduction.  Inputs and outputs (4 GB at 255^3)
+    exceed L2."""
+    import torch
+    from hydrothermal3d_gb300 import api, post
+    d = post.device_case(n, n, n, seed=3)
+    o = post.outputs(n, n, n)
+    qy = d["Vy"]
+    torch.cuda.synchronize()  # inputs were built on torch's stream
+
+    def timed(fn):
+        fn()
+        fn()
+        ctx.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    t_sep = timed(lambda: post.run_separate(ctx, d, o))
+    t_fus = timed(lambda: post.run_fused(ctx, d, o))
+    t_nu = timed(lambda: api.Nusselt(ctx, qy, 1.0, 1.0))
+    bs, bf = post.bytes_separate(n, n, n), post.bytes_fused(n, n, n)
+    return {"n": n, "separate_ms": t_sep, "fused_ms": t_fus, "fused_speedup": t_sep / t_fus,
+            "separate_alg_GBs": bs / t_sep / 1e6, "fused_alg_GBs": bf / t_fus / 1e6, "nusselt_ms": t_nu,
+            "alg_bytes_per_cell": {"separate": bs // n ** 3, "fused": bf // n ** 3}, "dtype": "f64",
+            "case": "seeded phases (crust, fault, pluton, immersed, 5 % air rows), T 300-900 K, P 0.1-300 MPa, "
+                    "face velocities; all twelve VTK fields"}
 
 
 def fault_bench(ctx, stream, a):

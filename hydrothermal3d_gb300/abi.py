@@ -2,7 +2,7 @@
 import ctypes
 
 OK = 0
-ERR_ARG, ERR_CUDA, ERR_NAN, ERR_DIVERGED, ERR_MAXITER, ERR_TIMEOUT, ERR_NOMEM, ERR_SCRATCH = 1, 2, 3, 4, 5, 6, 7, 8
+ERR_ARG, ERR_CUDA, ERR_NAN, ERR_DIVERGED, ERR_MAXITER, ERR_TIMEOUT, ERR_NOMEM, ERR_SCRATCH, ERR_IO = 1, 2, 3, 4, 5, 6, 7, 8, 9
 FP64, MIXED = 0, 1
 BC_NEUMANN, BC_DIRICHLET, BC_PERIODIC = 0, 1, 2
 WENO_V1, WENO_V2_REF, WENO_V2_FIXED = 0, 1, 2
@@ -95,6 +95,21 @@ class KhaledGeom(ctypes.Structure):
         ("surf_b1", ctypes.c_double),
         ("fault", (ctypes.c_double * 6) * 4),
     ]
+
+
+class PostParams(ctypes.Structure):
+    """ht3d_post_params: scales and constants of the output diagnostics."""
+    _fields_ = [(f, ctypes.c_double) for f in (
+        "phi0", "scale_T", "scale_sigma", "scale_V", "scale_L", "k_fact", "ymin", "dy", "delta")]
+
+
+POST_FIELDS = ("phase", "pressure", "temperature", "vx", "vy", "vz", "k_thermal", "heat_capacity", "permeability",
+               "density", "viscosity", "peclet")
+
+
+class PostFields(ctypes.Structure):
+    """ht3d_post_fields: device output pointers of ht3d_postprocess_fields (NULL skips a field)."""
+    _fields_ = [(f, ctypes.c_void_p) for f in POST_FIELDS]
 
 
 class Instance(ctypes.Structure):

@@ -573,3 +573,143 @@ def step_v18(ctx, Tc_ex, Pc_ex, phc_ex, phv, wN, kmul, Vx, Vy, Vz, params):
              _ptr(Vy, S["fy"]), _ptr(Vz, S["fz"]), ctypes.byref(params), ctypes.byref(st_t), ctypes.byref(st_d),
              nx, ny, nz)
     return st_t, st_d
+
+
+# ------------------------------------------------------ output diagnostics
+# Dimensional/kernels_HT3D_postprocessing.jl: X is a cell array (nx, ny, nz);
+# phc_ex, Tc_ex, Pc_ex are ghosted; Vx/Vy/Vz are face arrays.
+def Phase(ctx, X, phc_ex):
+    nx, ny, nz = _cells(X); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_Phase", _ptr(X, S["c"], "X"), _ptr(phc_ex, S["ex"], "phc_ex"), nx, ny, nz)
+
+
+def Pressure(ctx, X, Pc_ex, phc_ex, scale_sigma):
+    nx, ny, nz = _cells(X); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_Pressure", _ptr(X, S["c"], "X"), _ptr(Pc_ex, S["ex"], "Pc_ex"), _ptr(phc_ex, S["ex"], "phc_ex"),
+             scale_sigma, nx, ny, nz)
+
+
+def Temperature(ctx, X, Tc_ex, phc_ex, scale_T):
+    nx, ny, nz = _cells(X); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_Temperature", _ptr(X, S["c"], "X"), _ptr(Tc_ex, S["ex"], "Tc_ex"), _ptr(phc_ex, S["ex"], "phc_ex"),
+             scale_T, nx, ny, nz)
+
+
+def Velocity(ctx, X, Y, Z, Vx, Vy, Vz, phc_ex, scale_V):
+    nx, ny, nz = _cells(X); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_Velocity", _ptr(X, S["c"], "X"), _ptr(Y, S["c"], "Y"), _ptr(Z, S["c"], "Z"),
+             _ptr(Vx, S["fx"], "Vx"), _ptr(Vy, S["fy"], "Vy"), _ptr(Vz, S["fz"], "Vz"),
+             _ptr(phc_ex, S["ex"], "phc_ex"), scale_V, nx, ny, nz)
+
+
+def EffectiveThermalConductivity(ctx, X, Tc_ex, phi0, phc_ex, scale_T):
+    nx, ny, nz = _cells(X); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_EffectiveThermalConductivity", _ptr(X, S["c"], "X"), _ptr(Tc_ex, S["ex"], "Tc_ex"), phi0,
+             _ptr(phc_ex, S["ex"], "phc_ex"), scale_T, nx, ny, nz)
+
+
+def EffectiveHeatCapacity(ctx, Ceff, Tc_ex, Pc_ex, phc_ex, phi_i, sca_T, sca_sigma, sca_C, sca_rho):
+    nx, ny, nz = _cells(Ceff); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_EffectiveHeatCapacity", _ptr(Ceff, S["c"], "Ceff"), _ptr(Tc_ex, S["ex"], "Tc_ex"),
+             None if Pc_ex is None else _ptr(Pc_ex, S["ex"], "Pc_ex"), _ptr(phc_ex, S["ex"], "phc_ex"), phi_i, sca_T,
+             sca_sigma, sca_C, sca_rho, nx, ny, nz)
+
+
+def Permeability(ctx, X, k_fact, ymin, dy, phc_ex, delta, scale_L):
+    nx, ny, nz = _cells(X); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_Permeability", _ptr(X, S["c"], "X"), k_fact, ymin, dy, _ptr(phc_ex, S["ex"], "phc_ex"), delta,
+             scale_L, nx, ny, nz)
+
+
+def FluidDensity(ctx, X, Tc_ex, Pc_ex, phc_ex, scale_T, scale_sigma):
+    nx, ny, nz = _cells(X); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_FluidDensity", _ptr(X, S["c"], "X"), _ptr(Tc_ex, S["ex"], "Tc_ex"), _ptr(Pc_ex, S["ex"], "Pc_ex"),
+             _ptr(phc_ex, S["ex"], "phc_ex"), scale_T, scale_sigma, nx, ny, nz)
+
+
+def Viscosity(ctx, X, Tc_ex, phc_ex, scale_T):
+    nx, ny, nz = _cells(X); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_Viscosity", _ptr(X, S["c"], "X"), _ptr(Tc_ex, S["ex"], "Tc_ex"), _ptr(phc_ex, S["ex"], "phc_ex"),
+             scale_T, nx, ny, nz)
+
+
+def Peclet(ctx, X, Tc_ex, Pc_ex, Vx, Vy, Vz, phc_ex, phi0, scale_T, scale_sigma, scale_V, scale_L):
+    nx, ny, nz = _cells(X); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_Peclet", _ptr(X, S["c"], "X"), _ptr(Tc_ex, S["ex"], "Tc_ex"), _ptr(Pc_ex, S["ex"], "Pc_ex"),
+             _ptr(Vx, S["fx"], "Vx"), _ptr(Vy, S["fy"], "Vy"), _ptr(Vz, S["fz"], "Vz"),
+             _ptr(phc_ex, S["ex"], "phc_ex"), phi0, scale_T, scale_sigma, scale_V, scale_L, nx, ny, nz)
+
+
+def postprocess_fields(ctx, out, Tc_ex, Pc_ex, Vx, Vy, Vz, phc_ex, **params):
+    """Every diagnostic named in `out` (a dict field name -> cell tensor, field
+    names as abi.POST_FIELDS) in one pass; `params` are abi.PostParams fields."""
+    nx, ny, nz = _cells_ex(phc_ex, "phc_ex"); S = _shapes(nx, ny, nz)
+    f = abi.PostFields()
+    for name, t in out.items():
+        if name not in abi.POST_FIELDS:
+            raise ValueError(f"unknown diagnostic {name!r}")
+        setattr(f, name, _ptr(t, S["c"], name))
+    p = abi.PostParams(**{k: float(v) for k, v in params.items()})
+    opt = lambda t, shape, name: None if t is None else _ptr(t, shape, name)
+    ctx.call("ht3d_postprocess_fields", ctypes.byref(f), opt(Tc_ex, S["ex"], "Tc_ex"), opt(Pc_ex, S["ex"], "Pc_ex"),
+             opt(Vx, S["fx"], "Vx"), opt(Vy, S["fy"], "Vy"), opt(Vz, S["fz"], "Vz"), _ptr(phc_ex, S["ex"], "phc_ex"),
+             ctypes.byref(p), nx, ny, nz)
+
+
+def Nusselt(ctx, qy, Lx, Lz):
+    """Nu = sum(qy[:,end,:]) / (Lx*Lz) / (nx*nz) of the (nx, ny+1, nz) y-flux."""
+    nx, ny1, nz = _cells(qy)
+    out = ctypes.c_double()
+    ctx.call("ht3d_Nusselt", _ptr(qy, (nx, ny1, nz), "qy"), Lx, Lz, nx, ny1 - 1, nz, ctypes.byref(out))
+    return out.value
+
+
+# ------------------------------------------------------ output and restart files
+def write_vtr(path, xc, yc, zc, fields):
+    """vtk_grid(path, xc, yc, zc) + vtkfile[name] = array (v18.jl:664-686).
+
+    fields: dict name -> (nx, ny, nz) array, or a tuple of three for a vector
+    field; numpy arrays or device tensors (copied to the host).  Returns the
+    file name written (".vtr" appended)."""
+    import numpy as np
+    lib = _lib.load()
+    host = lambda a: np.asfortranarray(to_numpy(a) if isinstance(a, torch.Tensor) else a, dtype=np.float64)
+    xc, yc, zc = (np.ascontiguousarray(np.asarray(c, dtype=np.float64).ravel()) for c in (xc, yc, zc))
+    n = (xc.size, yc.size, zc.size)
+    names, ncomp, arrs = [], [], []
+    for name, v in fields.items():
+        comps = v if isinstance(v, (tuple, list)) else (v,)
+        if len(comps) not in (1, 3):
+            raise ValueError(f"{name}: a field has 1 or 3 components")
+        for a in comps:
+            a = host(a)
+            if a.shape != n:
+                raise ValueError(f"{name}: shape {a.shape} does not match the coordinates {n}")
+            arrs.append(a)
+        names.append(name.encode())
+        ncomp.append(len(comps))
+    c_names = (ctypes.c_char_p * max(1, len(names)))(*names)
+    c_ncomp = (ctypes.c_int * max(1, len(ncomp)))(*ncomp)
+    c_data = (ctypes.c_void_p * max(1, len(arrs)))(*[a.ctypes.data for a in arrs])
+    st = lib.ht3d_write_vtr(str(path).encode(), xc.ctypes.data, yc.ctypes.data, zc.ctypes.data, *n, len(names),
+                            c_names, c_ncomp, c_data)
+    if st != abi.OK:
+        raise Ht3dError(st, lib.ht3d_status_string(st).decode())
+    p = str(path)
+    return p if p.endswith(".vtr") else p + ".vtr"
+
+
+def breakpoint_write(ctx, path, Tc_ex, Pc_ex, time, dt):
+    """Restart state Tc_ex, Pc_ex, time, dt to a file (v18.jl:579-588)."""
+    nx, ny, nz = _cells_ex(Tc_ex, "Tc_ex"); S = _shapes(nx, ny, nz)
+    ctx.call("ht3d_breakpoint_write", str(path).encode(), _ptr(Tc_ex, S["ex"], "Tc_ex"), _ptr(Pc_ex, S["ex"], "Pc_ex"),
+             float(time), float(dt), nx, ny, nz)
+
+
+def breakpoint_read(ctx, path, Tc_ex, Pc_ex):
+    """Fill Tc_ex, Pc_ex from a restart file (v18.jl:384-395); returns (time, dt)."""
+    nx, ny, nz = _cells_ex(Tc_ex, "Tc_ex"); S = _shapes(nx, ny, nz)
+    t, d = ctypes.c_double(), ctypes.c_double()
+    ctx.call("ht3d_breakpoint_read", str(path).encode(), _ptr(Tc_ex, S["ex"], "Tc_ex"), _ptr(Pc_ex, S["ex"], "Pc_ex"),
+             ctypes.byref(t), ctypes.byref(d), nx, ny, nz)
+    return t.value, d.value

@@ -24,7 +24,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3", "-Xcompiler",
           "-ffp-contract=off", "--expt-relaxed-constexpr", "-I", INCLUDE]
 # translation units that restate reference kernels statement by statement
-NO_FMA = {"kernels_dimless.cu", "kernels_dim.cu", "dyrel_fp64.cu", "step.cu", "weno.cu", "noalloc.cu", "ensemble.cu"}
+NO_FMA = {"kernels_dimless.cu", "kernels_dim.cu", "dyrel_fp64.cu", "step.cu", "weno.cu", "noalloc.cu", "ensemble.cu",
+          "postprocess.cu"}
 
 
 def _nvcc() -> str:

@@ -83,6 +83,7 @@ const char* ht3d_status_string(int s) {
         case HT3D_ERR_TIMEOUT: return "bounded device wait timed out";
         case HT3D_ERR_NOMEM: return "out of device memory";
         case HT3D_ERR_SCRATCH: return "grid exceeds the 2^20-double static scratch of ht3d_dyrel_iterate_noalloc";
+        case HT3D_ERR_IO: return "file could not be opened, written or read";
     }
     return "unknown status";
 }

@@ -9,7 +9,7 @@ dyrel_f32 (FP32 pseudo-iteration on the reference layout),
 dyrel_f64 (plain FP64 pseudo-iteration), mixed_solve (a mixed-form DYREL
 solve of --iters pseudo-iterations: two FP64 checks, then the padded FP32
 inner kernel k_mixed_inner), weno_f64 / weno_mixed (one fused WENO5
-advection).
+advection), post (one fused pass of the twelve output diagnostics, k_post).
 Prints the average time per launch measured with CUDA events.
 """
 import argparse
@@ -25,7 +25,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--kernel", default="dyrel_f32",
                     choices=["dyrel_f32", "dyrel_f64", "mixed_solve", "weno_f64", "weno_mixed", "weno_f32",
-                             "ensemble"])
+                             "ensemble", "post"])
     ap.add_argument("--members", type=int, default=16, help="ensemble members (--kernel ensemble)")
     ap.add_argument("--n", type=int, default=255)
     ap.add_argument("--iters", type=int, default=5)
@@ -102,6 +102,21 @@ def main():
         cells = sum(int(m.Tc_ex.shape[0] - 2) * int(m.Tc_ex.shape[1] - 2) * int(m.Tc_ex.shape[2] - 2) for m in mem)
         print(json.dumps({"kernel": "k_ens_inner", "members": len(mem), "cells": cells, "inner_iterations": nl,
                           "us_per_iteration": 1e3 * ms / max(1, nl)}))
+    elif a.kernel == "post":
+        from hydrothermal3d_gb300 import post
+        d = post.device_case(n, n, n, seed=3)
+        o = post.outputs(n, n, n)
+        torch.cuda.synchronize()  # inputs were built on torch's stream
+        post.run_fused(ctx, d, o)
+        ctx.synchronize()
+        e0.record(stream)
+        for _ in range(a.iters):
+            post.run_fused(ctx, d, o)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1e3 / a.iters
+        print(json.dumps({"kernel": "k_post", "n": n, "us_per_pass": t * 1e6,
+                          "alg_GBs": post.bytes_fused(n, n, n) / t / 1e9}))
     elif a.kernel == "weno_f32":
         from hydrothermal3d_gb300 import api, sweep
         V = [v.float().permute(2, 1, 0).contiguous().permute(2, 1, 0) for v in sweep.curl_velocity(n, n, n, seed=6)]

@@ -42,6 +42,7 @@ extern "C" {
 #define HT3D_ERR_TIMEOUT 6     /* a bounded device wait gave up */
 #define HT3D_ERR_NOMEM 7
 #define HT3D_ERR_SCRATCH 8     /* grid larger than the static scratch of ht3d_dyrel_iterate_noalloc */
+#define HT3D_ERR_IO 9          /* a file could not be opened, written or read */
 
 /* precision forms */
 #define HT3D_FP64 0            /* plain FP64, reproduces the reference */
@@ -485,7 +486,7 @@ int ht3d_SetInitialConditions_Khaled(ht3d_ctx* ctx, double* phc_ex, double* phv,
                                      double Ttop, double Pbot, double Ptop, double xmin, double ymin, double zmin,
                                      double xmax, double ymax, double zmax, double L, int nx, int ny, int nz);
 
-/* One time step of the dimensional model/* One time step of the dimensional model, Dimensional/HydroThermal3D_v18.jl:404-572:
+/* One time step of the dimensional model, Dimensional/HydroThermal3D_v18.jl:404-572:
    pluton insertion at it == 1, thermal DYREL solve (conductivity, smoothing,
    ρC_eff, Gershgorin), Darcy DYREL solve (ρk/μ, ϕ∂ρ/∂P, ϕρf_old, ρf), Darcy
    velocity and WENO5-v2 advection with sub-stepping.  phc_ex (ex) and phv
@@ -495,6 +496,101 @@ int ht3d_SetInitialConditions_Khaled(ht3d_ctx* ctx, double* phc_ex, double* phv,
 int ht3d_step_v18(ht3d_ctx* ctx, double* Tc_ex, double* Pc_ex, const double* phc_ex, const double* phv,
                   const double* wN, const double* kmul_v, double* Vx, double* Vy, double* Vz, ht3d_v18_params* p,
                   ht3d_dyrel_stats* st_thermal, ht3d_dyrel_stats* st_darcy, int nx, int ny, int nz);
+
+/* ------------------------------------------------------------------ */
+/* Output diagnostics (Dimensional/kernels_HT3D_postprocessing.jl) and */
+/* the Nusselt number (Dimensionless/HydroThermal3D_Alban_v6.jl:345-348)*/
+/* ------------------------------------------------------------------ */
+/* Every output is a cell array (nx, ny, nz).  Cells whose phase phc_ex is 1
+   (air) get NaN, except the Y/Z outputs of ht3d_Velocity and
+   ht3d_EffectiveHeatCapacity, which leave air cells untouched as the
+   reference does.  Vx (nx+1,ny,nz), Vy (nx,ny+1,nz), Vz (nx,ny,nz+1). */
+/* Phase!                         kernels_HT3D_postprocessing.jl:1-10 */
+int ht3d_Phase(ht3d_ctx* ctx, double* X, const double* phc_ex, int nx, int ny, int nz);
+/* Pressure!                      :12-21 */
+int ht3d_Pressure(ht3d_ctx* ctx, double* X, const double* Pc_ex, const double* phc_ex, double scale_sigma, int nx,
+                  int ny, int nz);
+/* Temperature!                   :23-32 */
+int ht3d_Temperature(ht3d_ctx* ctx, double* X, const double* Tc_ex, const double* phc_ex, double scale_T, int nx,
+                     int ny, int nz);
+/* Velocity!                      :34-45 */
+int ht3d_Velocity(ht3d_ctx* ctx, double* X, double* Y, double* Z, const double* Vx, const double* Vy, const double* Vz,
+                  const double* phc_ex, double scale_V, int nx, int ny, int nz);
+/* EffectiveThermalConductivity!  :47-57 */
+int ht3d_EffectiveThermalConductivity(ht3d_ctx* ctx, double* X, const double* Tc_ex, double phi0,
+                                      const double* phc_ex, double scale_T, int nx, int ny, int nz);
+/* EffectiveHeatCapacity!         :60-70 (solid Cs(T) only; Pc_ex, phi_i and the
+   sigma/C/rho scales are accepted and unused, as in the reference) */
+int ht3d_EffectiveHeatCapacity(ht3d_ctx* ctx, double* Ceff, const double* Tc_ex, const double* Pc_ex,
+                               const double* phc_ex, double phi_i, double sca_T, double sca_sigma, double sca_C,
+                               double sca_rho, int nx, int ny, int nz);
+/* Permeability!                  :72-85 */
+int ht3d_Permeability(ht3d_ctx* ctx, double* X, double k_fact, double ymin, double dy, const double* phc_ex,
+                      double delta, double scale_L, int nx, int ny, int nz);
+/* FluidDensity!                  :87-98 */
+int ht3d_FluidDensity(ht3d_ctx* ctx, double* X, const double* Tc_ex, const double* Pc_ex, const double* phc_ex,
+                      double scale_T, double scale_sigma, int nx, int ny, int nz);
+/* Viscosity!                     :100-109 */
+int ht3d_Viscosity(ht3d_ctx* ctx, double* X, const double* Tc_ex, const double* phc_ex, double scale_T, int nx,
+                   int ny, int nz);
+/* Peclet!                        :111-129 */
+int ht3d_Peclet(ht3d_ctx* ctx, double* X, const double* Tc_ex, const double* Pc_ex, const double* Vx, const double* Vy,
+                const double* Vz, const double* phc_ex, double phi0, double scale_T, double scale_sigma, double scale_V,
+                double scale_L, int nx, int ny, int nz);
+
+/* Scales and constants of the diagnostics (the driver's sc.T, sc.σ, sc.V,
+   sc.L, ϕi, k_fact, ymin, Δy, δ). */
+typedef struct ht3d_post_params {
+    double phi0, scale_T, scale_sigma, scale_V, scale_L, k_fact, ymin, dy, delta;
+} ht3d_post_params;
+/* Output arrays of ht3d_postprocess_fields, named as the driver's VTK fields
+   (Dimensional/HydroThermal3D_v18.jl:664-685); NULL skips a field.  vx, vy
+   and vz go together. */
+typedef struct ht3d_post_fields {
+    double *phase, *pressure, *temperature, *vx, *vy, *vz, *k_thermal, *heat_capacity, *permeability, *density,
+        *viscosity, *peclet;
+} ht3d_post_fields;
+/* All requested diagnostics in one pass over the grid (the ten kernels above
+   fused: phc_ex, T, P and V are read once).  Each field is bit-identical to
+   the single-field entry point's.  out and prm are host pointers. */
+int ht3d_postprocess_fields(ht3d_ctx* ctx, const ht3d_post_fields* out, const double* Tc_ex, const double* Pc_ex,
+                            const double* Vx, const double* Vy, const double* Vz, const double* phc_ex,
+                            const ht3d_post_params* prm, int nx, int ny, int nz);
+int ht3d_sizeof_post_params(void);
+int ht3d_sizeof_post_fields(void);
+
+/* Nusselt number Nu = sum(qy[:,end,:]) / (Lx*Lz) / (nx*nz)
+   (Dimensionless/HydroThermal3D_Alban_v6.jl:345-348); qy is the (nx, ny+1, nz)
+   y-flux of ComputeFlux!.  The top-face sum uses the library's canonical tree
+   order (deterministic).  Result to *Nu (host). */
+int ht3d_Nusselt(ht3d_ctx* ctx, const double* qy, double Lx, double Lz, int nx, int ny, int nz, double* Nu);
+
+/* ------------------------------------------------------------------ */
+/* Output and restart files (Dimensional/HydroThermal3D_v18.jl)        */
+/* ------------------------------------------------------------------ */
+/* VTK rectilinear-grid file of vtk_grid(path, xc, yc, zc) with fields
+   vtkfile[name] = array (v18.jl:664-686): x (nx), y (ny), z (nz) are the
+   cell-centre coordinates, each field has one value per cell (column-major)
+   and 1 or 3 components; data holds ncomp[f] HOST pointers per field, in
+   field order (a 3-component field gives its X, Y, Z arrays, interleaved in
+   the file like WriteVTK's tuple).  VTK XML, Float64, one appended raw block
+   (UInt64 headers, little-endian).  ".vtr" is appended to path unless present.
+   Host-only: needs no context or GPU.  HT3D_ERR_IO if the file cannot be
+   written. */
+int ht3d_write_vtr(const char* path, const double* x, const double* y, const double* z, int nx, int ny, int nz,
+                   int nfields, const char* const* names, const int* ncomp, const double* const* data);
+
+/* Restart state of v18.jl:579-588 (write) and :384-395 (read): the device
+   arrays Tc_ex and Pc_ex ((nx+2)(ny+2)(nz+2) each) and time, dt.  The
+   reference writes HDF5 (Breakpoint%05d.h5); this library writes a raw
+   binary file: the 8 bytes "HT3DBRK1", int64 nx, ny, nz, float64 time, dt,
+   then Tc_ex and Pc_ex as column-major float64, little-endian.  Reading
+   checks the magic and the grid (HT3D_ERR_ARG on a different grid,
+   HT3D_ERR_IO on a missing, foreign or truncated file). */
+int ht3d_breakpoint_write(ht3d_ctx* ctx, const char* path, const double* Tc_ex, const double* Pc_ex, double time,
+                          double dt, int nx, int ny, int nz);
+int ht3d_breakpoint_read(ht3d_ctx* ctx, const char* path, double* Tc_ex, double* Pc_ex, double* time, double* dt,
+                         int nx, int ny, int nz);
 
 #ifdef __cplusplus
 }

@@ -80,6 +80,15 @@ def law(which, a, b=0.0):
     return fn(ctypes.c_int(which), ctypes.c_double(a), ctypes.c_double(b))
 
 
+def nusselt(qy, Lx, Lz):
+    """Nu of the (nx, ny+1, nz) y-flux (orc_Nusselt)."""
+    fn = load().orc_Nusselt
+    fn.restype = ctypes.c_double
+    nx, ny1, nz = qy.shape
+    return fn(_p(qy), ctypes.c_double(Lx), ctypes.c_double(Lz), ctypes.c_longlong(nx), ctypes.c_longlong(ny1 - 1),
+              ctypes.c_longlong(nz))
+
+
 def zeros(*shape):
     return np.zeros(shape, order="F")
 

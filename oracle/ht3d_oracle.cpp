@@ -1259,3 +1259,144 @@ void orc_SetInitialConditions_Khaled(double* phc, double* phv, double* wN, const
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Output diagnostics, Dimensional/kernels_HT3D_postprocessing.jl, and the
+// Nusselt number of Dimensionless/HydroThermal3D_Alban_v6.jl:345-348.
+// Every output is a cell array (nx,ny,nz); cells whose phase phc_ex is 1
+// (air) get NaN, except where the reference leaves them untouched (the Y/Z
+// components of Velocity!, and EffectiveHeatCapacity!).
+// ===========================================================================
+extern "C" {
+
+#define POST_LOOP                                                                         \
+    A3 phc = mk((double*)phc_ex_, nx + 2, ny + 2, nz + 2);                                \
+    PARFOR3(nx, ny, nz)
+#define POST_AIR (phc(i + 1, j + 1, k + 1) == 1.0)
+#define POST_PH phc(i + 1, j + 1, k + 1)
+#define POST_OUT(X_) X_[i + nx * (j + ny * k)]
+
+// Phase!  :1-10
+void orc_Phase(double* X, const double* phc_ex_, i64 nx, i64 ny, i64 nz) {
+    POST_LOOP { POST_OUT(X) = POST_AIR ? NAN : POST_PH; }
+}
+// Pressure!  :12-21
+void orc_Pressure(double* X, const double* Pc_ex_, const double* phc_ex_, double scale_s, i64 nx, i64 ny, i64 nz) {
+    A3 Pc = mk((double*)Pc_ex_, nx + 2, ny + 2, nz + 2);
+    POST_LOOP { POST_OUT(X) = POST_AIR ? NAN : Pc(i + 1, j + 1, k + 1) * scale_s; }
+}
+// Temperature!  :23-32
+void orc_Temperature(double* X, const double* Tc_ex_, const double* phc_ex_, double scale_T, i64 nx, i64 ny, i64 nz) {
+    A3 Tc = mk((double*)Tc_ex_, nx + 2, ny + 2, nz + 2);
+    POST_LOOP { POST_OUT(X) = POST_AIR ? NAN : Tc(i + 1, j + 1, k + 1) * scale_T; }
+}
+// Velocity!  :34-45 -- face averages to centres; air sets only X
+void orc_Velocity(double* X, double* Y, double* Z, const double* Vx_, const double* Vy_, const double* Vz_,
+                  const double* phc_ex_, double scale_V, i64 nx, i64 ny, i64 nz) {
+    A3 Vx = mk((double*)Vx_, nx + 1, ny, nz), Vy = mk((double*)Vy_, nx, ny + 1, nz), Vz = mk((double*)Vz_, nx, ny, nz + 1);
+    POST_LOOP {
+        if (!POST_AIR) {
+            POST_OUT(X) = 0.5 * (Vx(i, j, k) + Vx(i + 1, j, k)) * scale_V;
+            POST_OUT(Y) = 0.5 * (Vy(i, j, k) + Vy(i, j + 1, k)) * scale_V;
+            POST_OUT(Z) = 0.5 * (Vz(i, j, k) + Vz(i, j, k + 1)) * scale_V;
+        } else {
+            POST_OUT(X) = NAN;
+        }
+    }
+}
+// EffectiveThermalConductivity!  :47-57
+void orc_EffectiveThermalConductivity(double* X, const double* Tc_ex_, double phi0, const double* phc_ex_,
+                                      double scale_T, i64 nx, i64 ny, i64 nz) {
+    A3 Tc = mk((double*)Tc_ex_, nx + 2, ny + 2, nz + 2);
+    POST_LOOP {
+        if (!POST_AIR) {
+            const double T = Tc(i + 1, j + 1, k + 1) * scale_T;
+            POST_OUT(X) = ((1.0 - phi_of(POST_PH, phi0)) * kTs(T) + phi_of(POST_PH, phi0) * kTf(T));
+        } else {
+            POST_OUT(X) = NAN;
+        }
+    }
+}
+// EffectiveHeatCapacity!  :60-70 -- solid heat capacity only; air untouched
+// (Pc_ex, phi_i and the sigma/C/rho scales are accepted and unused, as there)
+void orc_EffectiveHeatCapacity(double* X, const double* Tc_ex_, const double* Pc_ex_, const double* phc_ex_,
+                               double phi_i, double sca_T, double sca_s, double sca_C, double sca_rho, i64 nx, i64 ny,
+                               i64 nz) {
+    (void)Pc_ex_, (void)phi_i, (void)sca_s, (void)sca_C, (void)sca_rho;
+    A3 Tc = mk((double*)Tc_ex_, nx + 2, ny + 2, nz + 2);
+    POST_LOOP {
+        if (!POST_AIR) POST_OUT(X) = Cs(Tc(i + 1, j + 1, k + 1) * sca_T);
+    }
+}
+// Permeability!  :72-85 -- y of the cell centre; fault phase (2) scaled by k_fact
+void orc_Permeability(double* X, double k_fact, double ymin, double dy, const double* phc_ex_, double delta,
+                      double scale_L, i64 nx, i64 ny, i64 nz) {
+    POST_LOOP {
+        if (!POST_AIR) {
+            const double y = ymin + (double)j * dy + dy / 2;
+            double v = k_F(y * scale_L, delta * scale_L);
+            if (POST_PH == 2.0) v *= k_fact;
+            POST_OUT(X) = v;
+        } else {
+            POST_OUT(X) = NAN;
+        }
+    }
+}
+// FluidDensity!  :87-98
+void orc_FluidDensity(double* X, const double* Tc_ex_, const double* Pc_ex_, const double* phc_ex_, double scale_T,
+                      double scale_s, i64 nx, i64 ny, i64 nz) {
+    A3 Tc = mk((double*)Tc_ex_, nx + 2, ny + 2, nz + 2), Pc = mk((double*)Pc_ex_, nx + 2, ny + 2, nz + 2);
+    POST_LOOP {
+        if (!POST_AIR) {
+            const double T = Tc(i + 1, j + 1, k + 1) * scale_T - 273.15;
+            const double P = Pc(i + 1, j + 1, k + 1) * scale_s;
+            POST_OUT(X) = rhof_C(T, P);
+        } else {
+            POST_OUT(X) = NAN;
+        }
+    }
+}
+// Viscosity!  :100-109
+void orc_Viscosity(double* X, const double* Tc_ex_, const double* phc_ex_, double scale_T, i64 nx, i64 ny, i64 nz) {
+    A3 Tc = mk((double*)Tc_ex_, nx + 2, ny + 2, nz + 2);
+    POST_LOOP { POST_OUT(X) = POST_AIR ? NAN : mu_f(Tc(i + 1, j + 1, k + 1) * scale_T); }
+}
+// Peclet!  :111-129 -- L rho_f C_f |V| / k_eff; x^2 is x*x (Julia literal power)
+void orc_Peclet(double* X, const double* Tc_ex_, const double* Pc_ex_, const double* Vx_, const double* Vy_,
+                const double* Vz_, const double* phc_ex_, double phi0, double scale_T, double scale_s, double scale_V,
+                double scale_L, i64 nx, i64 ny, i64 nz) {
+    A3 Tc = mk((double*)Tc_ex_, nx + 2, ny + 2, nz + 2), Pc = mk((double*)Pc_ex_, nx + 2, ny + 2, nz + 2);
+    A3 Vx = mk((double*)Vx_, nx + 1, ny, nz), Vy = mk((double*)Vy_, nx, ny + 1, nz), Vz = mk((double*)Vz_, nx, ny, nz + 1);
+    POST_LOOP {
+        if (!POST_AIR) {
+            const double x = 0.5 * (Vx(i, j, k) + Vx(i + 1, j, k)) * scale_V;
+            const double y = 0.5 * (Vy(i, j, k) + Vy(i, j + 1, k)) * scale_V;
+            const double z = 0.5 * (Vz(i, j, k) + Vz(i, j, k + 1)) * scale_V;
+            const double V = std::sqrt(x * x + y * y + z * z);
+            const double T = Tc(i + 1, j + 1, k + 1) * scale_T;
+            const double P = Pc(i + 1, j + 1, k + 1) * scale_s;
+            const double rho = rhof_C(T - 273.15, P);
+            const double C = Cf(T);
+            const double keff = ((1 - phi_of(POST_PH, phi0)) * kTs(T) + phi_of(POST_PH, phi0) * kTf(T));
+            POST_OUT(X) = scale_L * rho * C * V / keff;
+        } else {
+            POST_OUT(X) = NAN;
+        }
+    }
+}
+#undef POST_LOOP
+#undef POST_AIR
+#undef POST_PH
+#undef POST_OUT
+
+// Nu = sum(qy[:,end,:]) / (Lx*Lz) / (nx*nz), Dimensionless/HydroThermal3D_Alban_v6.jl:345-348.
+// qy is (nx, ny+1, nz); the top-face values are summed in the canonical tree
+// order over the (i fastest, then k) linear index of the face.
+double orc_Nusselt(const double* qy, double Lx, double Lz, i64 nx, i64 ny, i64 nz) {
+    std::vector<double> face((size_t)(nx * nz));
+    for (i64 k = 0; k < nz; ++k)
+        for (i64 i = 0; i < nx; ++i) face[(size_t)(i + nx * k)] = qy[i + nx * (ny + (ny + 1) * k)];
+    return tree_sum(face.data(), nx * nz) / (Lx * Lz) / (double)(nx * nz);
+}
+
+}  // extern "C"

@@ -38,6 +38,8 @@ def test_struct_layouts_match(lib):
     assert lib.ht3d_sizeof_hrl_params() == ctypes.sizeof(abi.HrlParams)
     assert lib.ht3d_sizeof_instance() == ctypes.sizeof(abi.Instance)
     assert lib.ht3d_sizeof_v18_params() == ctypes.sizeof(abi.V18Params)
+    assert lib.ht3d_sizeof_post_params() == ctypes.sizeof(abi.PostParams)
+    assert lib.ht3d_sizeof_post_fields() == ctypes.sizeof(abi.PostFields)
 
 
 def test_status_strings(lib):
