@@ -703,11 +703,17 @@ def post_bench(ctx, stream, n, reps=5):
 
     t_sep = timed(lambda: post.run_separate(ctx, d, o))
     t_fus = timed(lambda: post.run_fused(ctx, d, o))
+    # one field at a time through the fused kernel: which law costs what
+    per_field = {}
+    for name in ("phase", "pressure", "temperature", "k_thermal", "heat_capacity", "permeability", "density",
+                 "viscosity", "peclet"):
+        per_field[name] = timed(lambda: post.run_fused(ctx, d, {name: o[name]}))
+    per_field["velocity"] = timed(lambda: post.run_fused(ctx, d, {k: o[k] for k in ("vx", "vy", "vz")}))
     t_nu = timed(lambda: api.Nusselt(ctx, qy, 1.0, 1.0))
     bs, bf = post.bytes_separate(n, n, n), post.bytes_fused(n, n, n)
     return {"n": n, "separate_ms": t_sep, "fused_ms": t_fus, "fused_speedup": t_sep / t_fus,
             "separate_alg_GBs": bs / t_sep / 1e6, "fused_alg_GBs": bf / t_fus / 1e6, "nusselt_ms": t_nu,
-            "alg_bytes_per_cell": {"separate": bs // n ** 3, "fused": bf // n ** 3}, "dtype": "f64",
+            "single_field_ms": per_field, "alg_bytes_per_cell": {"separate": bs // n ** 3, "fused": bf // n ** 3}, "dtype": "f64",
             "case": "seeded phases (crust, fault, pluton, immersed, 5 % air rows), T 300-900 K, P 0.1-300 MPa, "
                     "face velocities; all twelve VTK fields"}
 

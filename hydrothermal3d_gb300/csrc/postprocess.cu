@@ -22,7 +22,19 @@ struct PostIn {
 
 // Air cells (phase 1) get NaN, except Velocity!'s Y/Z components and
 // EffectiveHeatCapacity!, which the reference leaves untouched there.
-__global__ void k_post(PostOut o, PostIn a, ht3d_post_params p, int nx, int ny, int nz) {
+// Permeability! depends on the row j only: kF of the ny cell-centre depths,
+// evaluated once per row (an FP64 exponential costs the same warp issue
+// slots whatever the number of active lanes)
+__global__ void k_perm_rows(double* __restrict__ kf, ht3d_post_params p, int ny) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= ny) return;
+    const double y = p.ymin + (double)j * p.dy + p.dy / 2;
+    kf[j] = law_kF(y * p.scale_L, p.delta * p.scale_L);
+}
+
+// kf_rows: the table of k_perm_rows when o.perm is set
+__global__ void k_post(PostOut o, PostIn a, ht3d_post_params p, const double* __restrict__ kf_rows, int nx, int ny,
+                       int nz) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
@@ -62,26 +74,29 @@ __global__ void k_post(PostOut o, PostIn a, ht3d_post_params p, int nx, int ny, 
         if (o.Pe) o.Pe[c] = nan;
         return;
     }
+    if (o.perm) {
+        double v = kf_rows[j];
+        if (ph == 2.0) v *= p.k_fact;
+        o.perm[c] = v;
+    }
+    // every read below is of an input that post_launch checked for the
+    // outputs requested: Tc for any T-dependent field, Pc for density/Peclet
+    if (!(o.keff || o.Pe || o.Ceff || o.rhof || o.mu)) return;
     const double T = a.Tc[e] * p.scale_T;
+    // FluidDensity! and Peclet! evaluate rho_f at the same (T - 273.15, P):
+    // once here serves both (the ALU, not HBM, bounds this kernel in FP64)
+    const double rho = (o.rhof || o.Pe) ? law_rhof_C(T - 273.15, a.Pc[e] * p.scale_sigma) : 0.0;
+    if (o.rhof) o.rhof[c] = rho;
     if (o.keff || o.Pe) {
         const double keff = ((1.0 - law_phi(ph, p.phi0)) * law_kTs(T) + law_phi(ph, p.phi0) * law_kTf(T));
         if (o.keff) o.keff[c] = keff;
         if (o.Pe) {
             const double V = sqrt(vx * vx + vy * vy + vz * vz);
-            const double Pp = a.Pc[e] * p.scale_sigma;
-            const double rho = law_rhof_C(T - 273.15, Pp);
             const double C = law_Cf(T);
             o.Pe[c] = p.scale_L * rho * C * V / keff;
         }
     }
     if (o.Ceff) o.Ceff[c] = law_Cs(T);
-    if (o.perm) {
-        const double y = p.ymin + (double)j * p.dy + p.dy / 2;
-        double v = law_kF(y * p.scale_L, p.delta * p.scale_L);
-        if (ph == 2.0) v *= p.k_fact;
-        o.perm[c] = v;
-    }
-    if (o.rhof) o.rhof[c] = law_rhof_C(T - 273.15, a.Pc[e] * p.scale_sigma);
     if (o.mu) o.mu[c] = law_muf(T);
 }
 
@@ -104,8 +119,13 @@ int post_launch(ht3d_ctx* ctx, const PostOut& o, const PostIn& a, const ht3d_pos
     HT3D_REQUIRE(!needP || a.Pc, "null argument");
     HT3D_REQUIRE(!needV || all_nonnull(a.Vx, a.Vy, a.Vz), "null argument");
     HT3D_REQUIRE(!(o.Vx || o.Vy || o.Vz) || all_nonnull(o.Vx, o.Vy, o.Vz), "velocity needs all three outputs");
+    double* kf_rows = nullptr;
+    if (o.perm) {
+        kf_rows = (double*)ht3d_scratch(ctx, SLOT_AUX1, sizeof(double) * ny);
+        HT3D_LAUNCH(ctx, k_perm_rows, (ny + 127) / 128, 128, 0, kf_rows, p, ny);
+    }
     dim3 b(32, 8, 1), g((nx + 31) / 32, (ny + 7) / 8, nz);
-    HT3D_LAUNCH(ctx, k_post, g, b, 0, o, a, p, nx, ny, nz);
+    HT3D_LAUNCH(ctx, k_post, g, b, 0, o, a, p, kf_rows, nx, ny, nz);
     return HT3D_OK;
 }
 

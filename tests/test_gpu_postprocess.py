@@ -23,7 +23,8 @@ def _same(name, got, ref):
     if name in LIBM:
         assert np.array_equal(np.isnan(got), np.isnan(ref)), name
         m = ~np.isnan(ref)
-        assert rel_err(got[m], ref[m]) <= 1e-13, name
+        if m.any():  # a grid of air cells holds only NaN
+            assert rel_err(got[m], ref[m]) <= 1e-13, name
     else:
         assert np.array_equal(got, ref, equal_nan=True), name
 
