@@ -19,17 +19,20 @@
 // FP64 kernel folds D into X, recomputes the true FP64 residual
 // (defect correction), evaluates the norms and Rayleigh-quotient sums in FP64,
 // performs that iteration's update into D, and refreshes Rin.  The DYREL
-// momentum F0 is stored in FP32 and carried across checks, so the iteration
-// follows the FP64 one up to FP32 rounding within a check window while the
-// stop test always sees the FP64 residual.
+// momentum is not stored: F0 = (Dprev - D) / dtau_prev follows from the
+// correction before the last update, which the iteration streams instead of
+// reading and writing F0 (seven fields per iteration instead of eight).  It is
+// carried across checks (Dprev = 0 after a fold), so the iteration follows
+// the FP64 one up to FP32 rounding within a check window while the stop test
+// always sees the FP64 residual.
 // ---------------------------------------------------------------------------
 namespace {
 
 // ---------------------------------------------------------------------------
 // Padded FP32 layout of the mixed solver's inner fields.
 //
-// Element (i, j, k) of every FP32 field (correction D, FP32 residual Rin,
-// momentum F0, F, face conductivities) sits at i + PX*(j + PY*k) with
+// Element (i, j, k) of every FP32 field (corrections D and Dprev, FP32
+// residual Rin, F, face conductivities) sits at i + PX*(j + PY*k) with
 // PX = nx+1 rounded up to 32 (128-byte rows), PY = ny+1 and nz+1 planes.  One
 // index therefore addresses a cell, its west x-face, its south y-face and its
 // bottom z-face; the east/north/front faces are +1, +PX, +PX*PY.  There is no
@@ -71,9 +74,37 @@ __device__ __forceinline__ float c4(const float4& v, int m) {
     return m == 0 ? v.x : (m == 1 ? v.y : (m == 2 ? v.z : v.w));
 }
 
+// Scalars of the FP32 iterations of the mixed solver, converted on the host.
+// The DYREL update F0' = h1 F0 + h2 F, x' = x - dtau F0' runs without a stored
+// momentum: F0 = (xprev - x) / dtau_prev is implied by the correction before
+// the last update (dtau_prev the dtau of that update), so
+//     x' = x + mom (x - xprev) - dh2 F,   mom = h1 dtau / dtau_prev,  dh2 = dtau h2
+// and an iteration streams the previous correction instead of reading and
+// writing F0.  mom = h1 except on the first iteration after a parameter update.
+struct MixScal {
+    float mom, dh2;             // inner update
+    float h1, h2, dtau;         // the FP64 check / refresh iteration's own update
+    float dtau_prev;            // dtau of the update that produced the current correction
+    float cX, _dx, _dy, _dz;
+};
+inline MixScal mix_scal(const DyrelScal& s, double dtau_prev) {
+    MixScal m;
+    m.mom = (float)(s.h1 * s.dtau / dtau_prev);
+    m.dh2 = (float)(s.dtau * s.h2);
+    m.h1 = (float)s.h1;
+    m.h2 = (float)s.h2;
+    m.dtau = (float)s.dtau;
+    m.dtau_prev = (float)dtau_prev;
+    m.cX = (float)s.cX;
+    m._dx = (float)s._dx;
+    m._dy = (float)s._dy;
+    m._dz = (float)s._dz;
+    return m;
+}
+
 // One cell of the FP32 inner iteration (the single place its arithmetic is
 // written, so every kernel that updates a cell rounds alike):
-//     F = (R + cX x + div q(x)) / diag,  F0' = h1 F0 + h2 F,  x' = x - dtau F0'
+//     F = (R + cX x + div q(x)) / diag,  x' = x + mom (x - xprev) - dh2 F
 // with q = -k dx on the six faces and diag = sum of k/dx^2 over them + cX.
 // Every operation is an explicit round-to-nearest intrinsic: the compiler may
 // neither contract nor reassociate them, so the value of a cell does not depend
@@ -81,9 +112,8 @@ __device__ __forceinline__ float c4(const float4& v, int m) {
 // four cells of a quad, k_mixed_inner2 does not).
 __device__ __forceinline__ void mixed_cell(float xc, float xw, float xe, float xs, float xn, float xb, float xf,
                                            float kW, float kE, float kS, float kN, float kB, float kF, float r,
-                                           float f0old, float h1, float h2, float dtau, float cX, float _dx, float _dy,
-                                           float _dz, float _dx2, float _dy2, float _dz2, float& f, float& f0,
-                                           float& xnew) {
+                                           float xprev, float mom, float dh2, float cX, float _dx, float _dy,
+                                           float _dz, float _dx2, float _dy2, float _dz2, float& f, float& xnew) {
     const float qW = -__fmul_rn(kW, __fmul_rn(_dx, __fsub_rn(xc, xw)));
     const float qE = -__fmul_rn(kE, __fmul_rn(_dx, __fsub_rn(xe, xc)));
     const float qS = -__fmul_rn(kS, __fmul_rn(_dy, __fsub_rn(xc, xs)));
@@ -98,8 +128,7 @@ __device__ __forceinline__ void mixed_cell(float xc, float xw, float xe, float x
     diag = __fmaf_rn(__fadd_rn(kS, kN), _dy2, diag);
     diag = __fmaf_rn(__fadd_rn(kB, kF), _dz2, diag);
     f = __fdividef(fu, diag);
-    f0 = __fmaf_rn(h1, f0old, __fmul_rn(h2, f));
-    xnew = __fmaf_rn(-dtau, f0, xc);
+    xnew = __fmaf_rn(mom, __fsub_rn(xc, xprev), __fmaf_rn(-dh2, f, xc));
 }
 
 // FP32 inner iteration of the mixed solver on the padded layout, for the
@@ -110,16 +139,19 @@ __device__ __forceinline__ void mixed_cell(float xc, float xw, float xe, float x
 // diagonal (the Gershgorin D of the operator, sum of k/dx^2 over the six
 // faces + cX) is recomputed from the face conductivities already in
 // registers instead of being streamed.
-//     F = (Rin + cX D + div q(D)) / diag ;  F0 = h1 F0 + h2 F ;  D -= dtau F0
+//     F = (Rin + cX D + div q(D)) / diag ;  D' = D + mom (D - Dprev) - dh2 F
+// Dio holds Dprev on entry (read at the thread's own cells only, so the
+// update can overwrite it in place); prev0 means Dprev = 0 (the correction
+// was just folded into the FP64 solution) and skips its load.  Seven fields
+// stream per iteration: D (with its neighbour rows), Dprev/D', Rin, kx, ky, kz.
 // All 32 lanes of the warp must call it.  Lanes past the grid (j >= ny, or
 // live == false) take part with in-bounds loads and store nothing.
 template <bool STOREF>
-__device__ __forceinline__ void mixed_quad(const float* __restrict__ Din, float* __restrict__ Dout,
+__device__ __forceinline__ void mixed_quad(const float* __restrict__ Din, float* __restrict__ Dio,
                                            const float* __restrict__ Rin, const float* __restrict__ kx,
                                            const float* __restrict__ ky, const float* __restrict__ kz,
-                                           float* __restrict__ F0, float* __restrict__ F, const DyrelScalT<float>& s,
-                                           const BC6<float>& bc, const Pad& p, int t, int k, int lane,
-                                           bool live = true) {
+                                           float* __restrict__ F, const MixScal& s, bool prev0, const BC6<float>& bc,
+                                           const Pad& p, int t, int k, int lane, bool live = true) {
     const int q = t % p.nq;
     int j = t / p.nq;
     const bool act = live && j < p.ny;
@@ -142,15 +174,15 @@ __device__ __forceinline__ void mixed_quad(const float* __restrict__ Din, float*
     const float4 kzB = *reinterpret_cast<const float4*>(kz + base);
     const float4 kzF = *reinterpret_cast<const float4*>(kz + base + p.plane);
     const float4 r4 = *reinterpret_cast<const float4*>(Rin + base);
-    const float4 f04 = *reinterpret_cast<const float4*>(F0 + base);
+    const float4 dp4 = prev0 ? make_float4(0.f, 0.f, 0.f, 0.f) : *reinterpret_cast<const float4*>(Dio + base);
     // west neighbour of cell i0, east neighbour of cell i0+3, east face of cell i0+3
     float dW = 0.f, dE = 0.f, kE3 = 0.f;
     if (i0 > 0) dW = lane > 0 ? dW_sh : Din[base - 1];
     if (i0 + 4 < p.nx) dE = lane < 31 ? dE_sh : Din[base + 4];
     if (i0 + 3 < p.nx) kE3 = (lane < 31 && q < p.nq - 1) ? kE_sh : kx[base + 4];
-    const float h1 = s.h1, h2 = s.h2, dtau = s.dtau, cX = s.cX, _dx = s._dx, _dy = s._dy, _dz = s._dz;
+    const float mom = s.mom, dh2 = s.dh2, cX = s.cX, _dx = s._dx, _dy = s._dy, _dz = s._dz;
     const float _dx2 = __fmul_rn(_dx, _dx), _dy2 = __fmul_rn(_dy, _dy), _dz2 = __fmul_rn(_dz, _dz);
-    float outD[4], outF0[4], outF[4];
+    float outD[4], outF[4];
 #pragma unroll
     for (int m = 0; m < 4; ++m) {
         const int i = i0 + m;
@@ -163,29 +195,27 @@ __device__ __forceinline__ void mixed_quad(const float* __restrict__ Din, float*
         const float xf = front ? c4(dF, m) : ghost(bc, 5, xc);
         const float kW = c4(kx4, m), kE = m == 3 ? kE3 : c4(kx4, m + 1);
         const float kS = c4(kyS, m), kN = c4(kyN, m), kB = c4(kzB, m), kF = c4(kzF, m);
-        float f, f0, xn1;
-        mixed_cell(xc, xw, xe, xs, xn, xb, xf, kW, kE, kS, kN, kB, kF, c4(r4, m), c4(f04, m), h1, h2, dtau, cX, _dx, _dy,
-                   _dz, _dx2, _dy2, _dz2, f, f0, xn1);
+        float f, xn1;
+        mixed_cell(xc, xw, xe, xs, xn, xb, xf, kW, kE, kS, kN, kB, kF, c4(r4, m), c4(dp4, m), mom, dh2, cX, _dx, _dy,
+                   _dz, _dx2, _dy2, _dz2, f, xn1);
         const bool valid = i < p.nx;
-        outF0[m] = valid ? f0 : 0.f;
         outD[m] = valid ? xn1 : 0.f;
         outF[m] = valid ? f : 0.f;
     }
     if (!act) return;
-    *reinterpret_cast<float4*>(F0 + base) = make_float4(outF0[0], outF0[1], outF0[2], outF0[3]);
-    *reinterpret_cast<float4*>(Dout + base) = make_float4(outD[0], outD[1], outD[2], outD[3]);
+    *reinterpret_cast<float4*>(Dio + base) = make_float4(outD[0], outD[1], outD[2], outD[3]);
     if (STOREF) *reinterpret_cast<float4*>(F + base) = make_float4(outF[0], outF[1], outF[2], outF[3]);
 }
 
 // One instance: thread t of plane k = blockIdx.y handles quad t of the plane.
 template <bool STOREF>
-__global__ void __launch_bounds__(256, 4) k_mixed_inner(const float* __restrict__ Din, float* __restrict__ Dout,
+__global__ void __launch_bounds__(256, 4) k_mixed_inner(const float* __restrict__ Din, float* __restrict__ Dio,
                                                         const float* __restrict__ Rin, const float* __restrict__ kx,
                                                         const float* __restrict__ ky, const float* __restrict__ kz,
-                                                        float* __restrict__ F0, float* __restrict__ F,
-                                                        DyrelScalT<float> s, BC6<float> bc, Pad p) {
-    mixed_quad<STOREF>(Din, Dout, Rin, kx, ky, kz, F0, F, s, bc, p, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y,
-                       threadIdx.x & 31);
+                                                        float* __restrict__ F, MixScal s, int prev0, BC6<float> bc,
+                                                        Pad p) {
+    mixed_quad<STOREF>(Din, Dio, Rin, kx, ky, kz, F, s, prev0 != 0, bc, p, blockIdx.x * blockDim.x + threadIdx.x,
+                       blockIdx.y, threadIdx.x & 31);
 }
 
 // ---------------------------------------------------------------------------
@@ -197,11 +227,13 @@ __global__ void __launch_bounds__(256, 4) k_mixed_inner(const float* __restrict_
 //      (register), p-1 (shared), p (register).
 // Halo cells (one ring in x and y, one plane before and after the chunk) are
 // computed by both neighbouring CTAs.  Every field is read once per pass and
-// D, F0 are written once: half the traffic of two single iterations.  F0 is
-// ping-ponged (the halo reads neighbouring cells' F0).  Both iterations use
+// D', D'' are written once each (the next pass needs both: D'' and its
+// previous correction D'); both go to buffers the pass does not read, since
+// the halo reads neighbouring cells' D and Dprev.  Iteration B's Dprev is
+// iteration A's input D, already in registers.  Both iterations use
 // mixed_cell, so the result is bit-identical to two k_mixed_inner launches.
 //
-// The inputs of plane p (D over the tile plus one ring, kx, ky, kz, Rin, F0)
+// The inputs of plane p (D over the tile plus one ring, kx, ky, kz, Rin, Dprev)
 // are brought into shared memory by TMA tensor copies (one thread issues six
 // 3-D box loads per plane, completing on the plane's mbarrier) two planes
 // ahead, in a ring of TB_STAGES planes.  Boxes are TB_BW floats wide and start
@@ -221,16 +253,16 @@ struct __align__(128) TbStage {
     float pad1[(128 - ((TB_Y + 1) * TB_BW * 4) % 128) % 128 / 4];
     float kz[TB_Y][TB_BW];
     float R[TB_Y][TB_BW];
-    float F0[TB_Y][TB_BW];
+    float Dp[TB_Y][TB_BW];      // previous correction
 };
 constexpr unsigned kTbStageBytes = 4u * TB_BW * ((TB_Y + 2) + 5 * TB_Y + 1);  // bytes the six boxes deliver
 static_assert(offsetof(TbStage, kx) % 128 == 0 && offsetof(TbStage, ky) % 128 == 0 &&
                   offsetof(TbStage, kz) % 128 == 0 && offsetof(TbStage, R) % 128 == 0 &&
-                  offsetof(TbStage, F0) % 128 == 0 && sizeof(TbStage) % 128 == 0,
+                  offsetof(TbStage, Dp) % 128 == 0 && sizeof(TbStage) % 128 == 0,
               "TMA destinations must be 128-byte aligned");
 
 struct TbMaps {  // tensor maps of one pass (by value, in the constant bank)
-    CUtensorMap D, kx, ky, kz, R, F0;
+    CUtensorMap D, kx, ky, kz, R, Dp;
 };
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -263,9 +295,9 @@ __device__ __forceinline__ void tma_load3(void* dst, const CUtensorMap* map, int
 
 template <bool STOREF>
 __global__ void __launch_bounds__(TB_X* TB_Y, 2) k_mixed_inner2(const __grid_constant__ TbMaps maps,
-                                                                const float* __restrict__ Din, float* __restrict__ Dout,
-                                                                float* __restrict__ F0out, float* __restrict__ F,
-                                                                DyrelScalT<float> s, BC6<float> bc, Pad p, int zchunk,
+                                                                const float* __restrict__ Din, float* __restrict__ D1out,
+                                                                float* __restrict__ D2out, float* __restrict__ F,
+                                                                MixScal s, BC6<float> bc, Pad p, int zchunk,
                                                                 int* __restrict__ err) {
     extern __shared__ unsigned char tb_raw[];
     unsigned char* base = tb_raw + ((128 - (smem_u32(tb_raw) & 127)) & 127);
@@ -283,7 +315,7 @@ __global__ void __launch_bounds__(TB_X* TB_Y, 2) k_mixed_inner2(const __grid_con
     const int k0 = blockIdx.z * zchunk, k1 = min(p.nz, k0 + zchunk);
     const int pa0 = max(k0 - 1, 0);
     const int plast = min(k1 + 1, p.nz);  // last staged plane (plane nz: its bottom z-faces)
-    const float h1 = s.h1, h2 = s.h2, dtau = s.dtau, cX = s.cX, _dx = s._dx, _dy = s._dy, _dz = s._dz;
+    const float mom = s.mom, dh2 = s.dh2, cX = s.cX, _dx = s._dx, _dy = s._dy, _dz = s._dz;
     const float _dx2 = __fmul_rn(_dx, _dx), _dy2 = __fmul_rn(_dy, _dy), _dz2 = __fmul_rn(_dz, _dz);
     // this thread's element offsets inside a stage's tiles (fixed over planes)
     const int oD = (ty + 1) * TB_BW + tx + (x0 - xD);  // D centre
@@ -298,7 +330,7 @@ __global__ void __launch_bounds__(TB_X* TB_Y, 2) k_mixed_inner2(const __grid_con
         tma_load3(&S.ky[0][0], &maps.ky, xK, y0, k, b);
         tma_load3(&S.kz[0][0], &maps.kz, xK, y0, k, b);
         tma_load3(&S.R[0][0], &maps.R, xK, y0, k, b);
-        tma_load3(&S.F0[0][0], &maps.F0, xK, y0, k, b);
+        tma_load3(&S.Dp[0][0], &maps.Dp, xK, y0, k, b);
     };
     if (tid == 0) {
         abort_flag = 0;
@@ -319,12 +351,12 @@ __global__ void __launch_bounds__(TB_X* TB_Y, 2) k_mixed_inner2(const __grid_con
     float* dpr = dpbuf + ((pa0 + 1) & 1) * TB_Y * TB_X + oP;  // plane pl - 1, read by B
     // running global addresses of this column for B's plane q = pl - 1
     const long long colo = gi + (long long)p.PX * gj;
-    float* outD = Dout + colo + p.plane * (long long)(pa0 - 1);
-    float* outF0 = F0out + colo + p.plane * (long long)(pa0 - 1);
+    float* outD1 = D1out + colo + p.plane * (long long)(pa0 - 1);
+    float* outD2 = D2out + colo + p.plane * (long long)(pa0 - 1);
     float* outF = F + colo + p.plane * (long long)(pa0 - 1);
     float dm1 = (pa0 > 0 && in) ? Din[p.plane * (pa0 - 1) + colo] : 0.f;  // D(p-1)
     float dpm = 0.f, dpc = 0.f;
-    float cW = 0.f, cE = 0.f, cS = 0.f, cN = 0.f, cB = 0.f, cF = 0.f, cr = 0.f, cf0 = 0.f;
+    float cW = 0.f, cE = 0.f, cS = 0.f, cN = 0.f, cB = 0.f, cF = 0.f, cr = 0.f, cd0 = 0.f;
     for (int pl = pa0; pl <= k1; ++pl) {
         if (pl + 2 <= plast) {
             if (tid == 0) {
@@ -352,7 +384,7 @@ __global__ void __launch_bounds__(TB_X* TB_Y, 2) k_mixed_inner2(const __grid_con
             __syncthreads();
             return;
         }
-        float da = 0.f, aW = 0.f, aE = 0.f, aS = 0.f, aN = 0.f, aB = 0.f, aF = 0.f, ar = 0.f, af0 = 0.f;
+        float da = 0.f, aW = 0.f, aE = 0.f, aS = 0.f, aN = 0.f, aB = 0.f, aF = 0.f, ar = 0.f, ad0 = 0.f;
         if (pl < p.nz) {
             const float* d0 = &S0->D[0][0] + oD;
             const float* k0p = &S0->kx[0][0] + oK;
@@ -364,7 +396,7 @@ __global__ void __launch_bounds__(TB_X* TB_Y, 2) k_mixed_inner2(const __grid_con
             aB = (&S0->kz[0][0])[oK];
             aF = (&S1->kz[0][0])[oK];
             ar = (&S0->R[0][0])[oK];
-            const float f0o = (&S0->F0[0][0])[oK];
+            const float xp = (&S0->Dp[0][0])[oK];
             const float xc = d0[0];
             const float xw = gW ? ghost(bc, 0, xc) : d0[-1];
             const float xe = gE ? ghost(bc, 1, xc) : d0[1];
@@ -373,8 +405,9 @@ __global__ void __launch_bounds__(TB_X* TB_Y, 2) k_mixed_inner2(const __grid_con
             const float xb = (pl == 0) ? ghost(bc, 4, xc) : dm1;
             const float xf = (pl == p.nz - 1) ? ghost(bc, 5, xc) : (&S1->D[0][0])[oD];
             float f;
-            mixed_cell(xc, xw, xe, xs, xn, xb, xf, aW, aE, aS, aN, aB, aF, ar, f0o, h1, h2, dtau, cX, _dx, _dy, _dz,
-                       _dx2, _dy2, _dz2, f, af0, da);
+            mixed_cell(xc, xw, xe, xs, xn, xb, xf, aW, aE, aS, aN, aB, aF, ar, xp, mom, dh2, cX, _dx, _dy, _dz, _dx2,
+                       _dy2, _dz2, f, da);
+            ad0 = xc;  // iteration B's previous correction at this cell
             dm1 = xc;
             *dpw = da;
         }
@@ -388,19 +421,19 @@ __global__ void __launch_bounds__(TB_X* TB_Y, 2) k_mixed_inner2(const __grid_con
             const float xn = gN ? ghost(bc, 3, xc) : dpr[TB_X];
             const float xb = (q == 0) ? ghost(bc, 4, xc) : dpm;
             const float xf = (q == p.nz - 1) ? ghost(bc, 5, xc) : da;
-            float f, f0, xn1;
-            mixed_cell(xc, xw, xe, xs, xn, xb, xf, cW, cE, cS, cN, cB, cF, cr, cf0, h1, h2, dtau, cX, _dx, _dy, _dz,
-                       _dx2, _dy2, _dz2, f, f0, xn1);
-            *outD = xn1;
-            *outF0 = f0;
+            float f, xn1;
+            mixed_cell(xc, xw, xe, xs, xn, xb, xf, cW, cE, cS, cN, cB, cF, cr, cd0, mom, dh2, cX, _dx, _dy, _dz, _dx2,
+                       _dy2, _dz2, f, xn1);
+            *outD1 = xc;
+            *outD2 = xn1;
             if (STOREF) *outF = f;
         }
-        outD += p.plane;
-        outF0 += p.plane;
+        outD1 += p.plane;
+        outD2 += p.plane;
         outF += p.plane;
         dpm = dpc;
         dpc = da;
-        cW = aW; cE = aE; cS = aS; cN = aN; cB = aB; cF = aF; cr = ar; cf0 = af0;
+        cW = aW; cE = aE; cS = aS; cN = aN; cB = aB; cF = aF; cr = ar; cd0 = ad0;
         const TbStage* t = S0;
         S0 = S1;
         S1 = S2;
@@ -453,15 +486,14 @@ bool tb_map(CUtensorMap* m, const float* field, const Pad& P, unsigned rows) {
 // its first field load.
 // ---------------------------------------------------------------------------
 struct EnsInner {
-    float* D[2];  // correction ping-pong: read D[parity], write D[parity ^ 1]
+    float* D[2];  // correction ping-pong: read D[parity], Dprev / write D[parity ^ 1]
     const float* Rin;
-    float* F0;
     float* F;
     const float* kx;
     const float* ky;
     const float* kz;
     Pad P;
-    DyrelScalT<float> s;
+    MixScal s;
     BC6<float> bc;
 };
 constexpr int kEnsMaxPerLaunch = 120;
@@ -475,7 +507,7 @@ struct EnsLaunch {
 static_assert(sizeof(EnsLaunch) <= 32000, "batched launch parameters exceed the 32 KB kernel parameter space");
 
 template <bool STOREF, int BS>
-__global__ void __launch_bounds__(BS) k_ens_inner(const __grid_constant__ EnsLaunch L, int parity) {
+__global__ void __launch_bounds__(BS) k_ens_inner(const __grid_constant__ EnsLaunch L, int parity, int prev0) {
     // member of this block: binary search of the block offsets
     int lo = 0, hi = L.n;
     while (hi - lo > 1) {
@@ -491,24 +523,26 @@ __global__ void __launch_bounds__(BS) k_ens_inner(const __grid_constant__ EnsLau
     const int t = (int)(tg - (long long)k * pq);
     const bool live = k < e.P.nz;
     if (!live) k = e.P.nz - 1;
-    mixed_quad<STOREF>(e.D[parity], e.D[parity ^ 1], e.Rin, e.kx, e.ky, e.kz, e.F0, e.F, e.s, e.bc, e.P, t, k,
+    mixed_quad<STOREF>(e.D[parity], e.D[parity ^ 1], e.Rin, e.kx, e.ky, e.kz, e.F, e.s, prev0 != 0, e.bc, e.P, t, k,
                        threadIdx.x & 31, live);
 }
 
 // FP64 check / refresh iteration of the mixed solver (see above).  FP64
 // fields in the reference layout, FP32 fields in the padded layout.  The fold
-// X + D and the residual are FP64; the quantities stored in FP32 (F, F0, the
-// next correction D) are formed in FP32 with the inner iteration's rounding
-// rules, and the Rayleigh-quotient terms are summed per thread in FP32 (they
-// only estimate lambda_min).  CHECK = false (a refresh between the
+// X + D and the residual are FP64; the quantities stored in FP32 (F, the
+// momentum F0 = (Dprev - D) / dtau_prev, the next correction) are formed in
+// FP32, and the Rayleigh-quotient terms are summed per thread in FP32 (they
+// only estimate lambda_min).  Dio holds Dprev on entry (prev0: Dprev = 0) and
+// receives the next correction -dtau F0', whose own previous correction is 0
+// (D has been folded into X).  CHECK = false (a refresh between the
 // reference's checks) skips the check sums and the FP64 F.
 template <bool CHECK>
 __global__ void __launch_bounds__(TX* TY) k_mixed_check(
-    const double* __restrict__ Xin, double* __restrict__ Xout, const float* __restrict__ Din, float* __restrict__ Dout,
+    const double* __restrict__ Xin, double* __restrict__ Xout, const float* __restrict__ Din, float* __restrict__ Dio,
     const double* __restrict__ R, const double* __restrict__ kx, const double* __restrict__ ky,
-    const double* __restrict__ kz, const double* __restrict__ invPC, float* __restrict__ F0,
-    float* __restrict__ F32, double* __restrict__ F64, float* __restrict__ Rin, DyrelScal s, DyrelScalT<float> s32,
-    BC6<double> bc, Pad p, int zchunk, double* __restrict__ partials) {
+    const double* __restrict__ kz, const double* __restrict__ invPC, float* __restrict__ F32,
+    double* __restrict__ F64, float* __restrict__ Rin, DyrelScal s, MixScal s32, int prev0, BC6<double> bc, Pad p,
+    int zchunk, double* __restrict__ partials) {
     const int nx = p.nx, ny = p.ny, nz = p.nz;
     const int i = blockIdx.x * TX + threadIdx.x;
     const int j = blockIdx.y * TY + threadIdx.y;
@@ -549,7 +583,9 @@ __global__ void __launch_bounds__(TX* TY) k_mixed_check(
             const double fu = R[c] + s.cX * xc + s._dx * (qE - qW) + s._dy * (qN - qS) + s._dz * (qF - qB);
             const double f = fu * invPC[c];
             const float f32 = (float)f;
-            const float f0 = __fmaf_rn(s32.h1, F0[pc], __fmul_rn(s32.h2, f32));
+            const float dprev = prev0 ? 0.f : Dio[pc];
+            const float f0old = __fdiv_rn(__fsub_rn(dprev, dcol[pe]), s32.dtau_prev);
+            const float f0 = __fmaf_rn(s32.h1, f0old, __fmul_rn(s32.h2, f32));
             const float d = __fmul_rn(s32.dtau, f0);
             if (CHECK) {
                 acc[0] += fabs(fu);
@@ -557,10 +593,9 @@ __global__ void __launch_bounds__(TX* TY) k_mixed_check(
                 rq_den = __fmaf_rn(d, d, rq_den);
                 F64[c] = f;
             }
-            F0[pc] = f0;
             F32[pc] = f32;
             Rin[pc] = (float)fu;
-            Dout[pc] = -d;
+            Dio[pc] = -d;
             ocol[e] = xc;
             if (i == 0) ocol[e - 1] = xw;
             if (i == nx - 1) ocol[e + 1] = xe;
@@ -611,6 +646,19 @@ __global__ void k_mixed_fold(double* __restrict__ X, const float* __restrict__ D
     if (j == ny - 1) X[e + n1] = ghost(bc, 3, x);
     if (k == 0) X[e - pl] = ghost(bc, 4, x);
     if (k == nz - 1) X[e + pl] = ghost(bc, 5, x);
+}
+
+// The momentum after the last update, F0 = (Dprev - D) / dtau_prev (Dprev
+// null: the correction was just folded, Dprev = 0), into a reference cell array.
+__global__ void k_unpack_f0(double* __restrict__ dst, const float* __restrict__ D, const float* __restrict__ Dprev,
+                            float dtau_prev, Pad p) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= p.nx || j >= p.ny || k >= p.nz) return;
+    const long long pe = i + (long long)p.PX * j + p.plane * k;
+    const float dp = Dprev ? Dprev[pe] : 0.f;
+    dst[i + (long long)p.nx * (j + (long long)p.ny * k)] = (double)__fdiv_rn(__fsub_rn(dp, D[pe]), dtau_prev);
 }
 
 // Live timing of the inner-iteration runs (HT3D_TUNE_TIME_INNER): an event
@@ -667,10 +715,12 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
     const size_t pbytes = sizeof(float) * (size_t)P.size;
     double* invPC = (double*)ht3d_scratch(ctx, SLOT_PC, sizeof(double) * n);
     double* X2 = (double*)ht3d_scratch(ctx, SLOT_X2, sizeof(double) * nex);
-    float* Da = (float*)ht3d_scratch(ctx, SLOT_F32_X, pbytes);
-    float* Db = (float*)ht3d_scratch(ctx, SLOT_F32_X2, pbytes);
-    float* F0a = (float*)ht3d_scratch(ctx, SLOT_F32_F0, pbytes);
-    float* F0b = (float*)ht3d_scratch(ctx, SLOT_F32_F0B, pbytes);
+    // correction buffers: the current D and its previous correction, plus two
+    // more for the two-iteration passes (which write neither buffer they read)
+    const bool want_pairs = ctx->mixed_temporal != 0;
+    float* Dbuf[4] = {(float*)ht3d_scratch(ctx, SLOT_F32_X, pbytes), (float*)ht3d_scratch(ctx, SLOT_F32_X2, pbytes),
+                      want_pairs ? (float*)ht3d_scratch(ctx, SLOT_F32_D3, pbytes) : nullptr,
+                      want_pairs ? (float*)ht3d_scratch(ctx, SLOT_F32_D4, pbytes) : nullptr};
     float* Fs = (float*)ht3d_scratch(ctx, SLOT_F32_F, pbytes);
     float* Rin = (float*)ht3d_scratch(ctx, SLOT_F32_R, pbytes);
     float* kx32 = (float*)ht3d_scratch(ctx, SLOT_F32_KX, pbytes);
@@ -693,8 +743,8 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
     HT3D_LAUNCH(ctx, k_dyrel_setup_fast, gc, b2, 0, kx, ky, kz, cX, 1.0 / (dx * dx), 1.0 / (dy * dy), 1.0 / (dz * dz),
                 nx, ny, nz, invPC, parts);
     HT3D_LAUNCH(ctx, (k_reduce_partials<RED_MAX, 1>), 1, 1024, 0, parts, (int)(gc.x * gc.y * gc.z), dres);
-    for (float* a : {Da, Db, F0a, F0b, Fs, Rin, kx32, ky32, kz32})
-        HT3D_CUDA(cudaMemsetAsync(a, 0, pbytes, ctx->stream));
+    for (float* a : {Dbuf[0], Dbuf[1], Dbuf[2], Dbuf[3], Fs, Rin, kx32, ky32, kz32})
+        if (a) HT3D_CUDA(cudaMemsetAsync(a, 0, pbytes, ctx->stream));
     HT3D_LAUNCH(ctx, k_pack, dim3((nx + 1 + 31) / 32, (ny + 7) / 8, nz), b2, 0, kx32, kx, nx + 1, ny, nz, P);
     HT3D_LAUNCH(ctx, k_pack, dim3((nx + 31) / 32, (ny + 1 + 7) / 8, nz), b2, 0, ky32, ky, nx, ny + 1, nz, P);
     HT3D_LAUNCH(ctx, k_pack, dim3((nx + 31) / 32, (ny + 7) / 8, nz + 1), b2, 0, kz32, kz, nx, ny, nz + 1, P);
@@ -709,22 +759,19 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
     sc._dz = 1.0 / dz;
     const dim3 ib(256), ig((unsigned)(((long long)P.nq * ny + 255) / 256), (unsigned)nz);
     // two iterations per pass (k_mixed_inner2) inside runs of inner iterations
-    bool pairs = ctx->mixed_temporal != 0;
+    bool pairs = want_pairs;
     int zc = ctx->mixed_temporal >= 2 ? ctx->mixed_temporal : 0;
     const int tiles = ((nx + TB_X - 3) / (TB_X - 2)) * ((ny + TB_Y - 3) / (TB_Y - 2));
     if (!zc) zc = (int)std::min<long long>(64, std::max<long long>(8, (long long)nz * tiles / (8LL * ctx->num_sms)));
     const dim3 tb(TB_X, TB_Y), tg((nx + TB_X - 3) / (TB_X - 2), (ny + TB_Y - 3) / (TB_Y - 2), (nz + zc - 1) / zc);
-    TbMaps mapsA, mapsB;  // passes reading (Da, F0a) and (Db, F0b)
+    TbMaps mk;                       // conductivity and residual maps
+    CUtensorMap mapD[4], mapP[4];    // each correction buffer as a pass's D (with its ring) and as its Dprev
     int* derr = nullptr;
     if (pairs) {
-        pairs = tb_map(&mapsA.D, Da, P, TB_Y + 2) && tb_map(&mapsB.D, Db, P, TB_Y + 2) &&
-                tb_map(&mapsA.F0, F0a, P, TB_Y) && tb_map(&mapsB.F0, F0b, P, TB_Y) &&
-                tb_map(&mapsA.kx, kx32, P, TB_Y) && tb_map(&mapsA.ky, ky32, P, TB_Y + 1) &&
-                tb_map(&mapsA.kz, kz32, P, TB_Y) && tb_map(&mapsA.R, Rin, P, TB_Y);
-        mapsB.kx = mapsA.kx;
-        mapsB.ky = mapsA.ky;
-        mapsB.kz = mapsA.kz;
-        mapsB.R = mapsA.R;
+        pairs = tb_map(&mk.kx, kx32, P, TB_Y) && tb_map(&mk.ky, ky32, P, TB_Y + 1) && tb_map(&mk.kz, kz32, P, TB_Y) &&
+                tb_map(&mk.R, Rin, P, TB_Y);
+        for (int q = 0; q < 4 && pairs; ++q)
+            pairs = tb_map(&mapD[q], Dbuf[q], P, TB_Y + 2) && tb_map(&mapP[q], Dbuf[q], P, TB_Y);
     }
     if (pairs) {
         static_assert(kTbSmem <= 227 * 1024, "staging ring exceeds the shared memory of a CTA");
@@ -736,10 +783,9 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
     InnerTimer timer(ctx);
     double* xcur = X;
     double* xnxt = X2;
-    float* dcur = Da;
-    float* dnxt = Db;
-    float* f0cur = F0a;  // current FP32 momentum (k_mixed_inner2 writes the other buffer)
-    float* f0nxt = F0b;
+    int cur = 0, prv = 1;            // Dbuf indices of D and of its previous correction
+    bool prev0 = true;               // the previous correction is 0 (start, or D just folded into X)
+    double dtau_prev = S.dtau;       // dtau of the update that produced D
     DyrelCheck C;
     int it_done = 0;
     bool last_fp64 = false;  // the last iteration ran the FP64 kernel (check or refresh)
@@ -759,18 +805,19 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
         sc.h1 = S.h1;
         sc.h2 = S.h2;
         sc.dtau = S.dtau;
+        const MixScal s32 = mix_scal(sc, dtau_prev);
         if (chk || refresh) {
             timer.end();
-            const DyrelScalT<float> s32(sc);
             if (chk)
-                HT3D_LAUNCH(ctx, k_mixed_check<true>, LC.grid, LC.block, 0, xcur, xnxt, dcur, dnxt, R, kx, ky, kz, invPC,
-                            f0cur, Fs, F, Rin, sc, s32, bc, P, LC.zchunk, parts);
+                HT3D_LAUNCH(ctx, k_mixed_check<true>, LC.grid, LC.block, 0, xcur, xnxt, Dbuf[cur], Dbuf[prv], R, kx, ky,
+                            kz, invPC, Fs, F, Rin, sc, s32, prev0 ? 1 : 0, bc, P, LC.zchunk, parts);
             else
-                HT3D_LAUNCH(ctx, k_mixed_check<false>, LC.grid, LC.block, 0, xcur, xnxt, dcur, dnxt, R, kx, ky, kz,
-                            invPC, f0cur, Fs, F, Rin, sc, s32, bc, P, LC.zchunk, parts);
+                HT3D_LAUNCH(ctx, k_mixed_check<false>, LC.grid, LC.block, 0, xcur, xnxt, Dbuf[cur], Dbuf[prv], R, kx,
+                            ky, kz, invPC, Fs, F, Rin, sc, s32, prev0 ? 1 : 0, bc, P, LC.zchunk, parts);
             std::swap(xcur, xnxt);
+            std::swap(cur, prv);  // the new correction sits in the former Dprev buffer
+            prev0 = true;
         } else {
-            const DyrelScalT<float> s32(sc);
             timer.begin();
             // this run of inner iterations ends at run_end; a run that ends the
             // solve keeps its last iteration single (the final fold needs the
@@ -779,32 +826,38 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
             while (run_end < nmax && !is_fp64(run_end + 1)) ++run_end;
             const int pair_end = run_end == nmax ? run_end - 1 : run_end;
             const int left = pair_end - iter + 1;
-            if (pairs && left >= 2 && left % 2 == 0) {
+            // a pass starts only on a steady iteration (Dprev stored, mom = h1)
+            if (pairs && !prev0 && dtau_prev == sc.dtau && left >= 2 && left % 2 == 0) {
                 const bool storef2 = iter + 1 == nmax || is_check(iter + 2, prm->nitout);
-                // D alternates every iteration, F0 only on passes: pick their maps separately
-                TbMaps mp = mapsA;
-                mp.D = dcur == Da ? mapsA.D : mapsB.D;
-                mp.F0 = f0cur == F0a ? mapsA.F0 : mapsB.F0;
+                int o1 = -1, o2 = -1;  // the two buffers the pass does not read
+                for (int q = 0; q < 4; ++q)
+                    if (q != cur && q != prv) (o1 < 0 ? o1 : o2) = q;
+                TbMaps mp = mk;
+                mp.D = mapD[cur];
+                mp.Dp = mapP[prv];
                 if (storef2)
-                    HT3D_LAUNCH(ctx, k_mixed_inner2<true>, tg, tb, kTbSmem, mp, dcur, dnxt, f0nxt, Fs, s32, bch, P, zc,
-                                derr);
+                    HT3D_LAUNCH(ctx, k_mixed_inner2<true>, tg, tb, kTbSmem, mp, Dbuf[cur], Dbuf[o1], Dbuf[o2], Fs, s32,
+                                bch, P, zc, derr);
                 else
-                    HT3D_LAUNCH(ctx, k_mixed_inner2<false>, tg, tb, kTbSmem, mp, dcur, dnxt, f0nxt, Fs, s32, bch, P, zc,
-                                derr);
-                std::swap(f0cur, f0nxt);
+                    HT3D_LAUNCH(ctx, k_mixed_inner2<false>, tg, tb, kTbSmem, mp, Dbuf[cur], Dbuf[o1], Dbuf[o2], Fs,
+                                s32, bch, P, zc, derr);
+                prv = o1;
+                cur = o2;
                 timer.count(2);
                 ++iter;  // the pass did iterations iter and iter + 1
             } else {
                 if (storef)
-                    HT3D_LAUNCH(ctx, k_mixed_inner<true>, ig, ib, 0, dcur, dnxt, Rin, kx32, ky32, kz32, f0cur, Fs, s32,
-                                bch, P);
+                    HT3D_LAUNCH(ctx, k_mixed_inner<true>, ig, ib, 0, Dbuf[cur], Dbuf[prv], Rin, kx32, ky32, kz32, Fs,
+                                s32, prev0 ? 1 : 0, bch, P);
                 else
-                    HT3D_LAUNCH(ctx, k_mixed_inner<false>, ig, ib, 0, dcur, dnxt, Rin, kx32, ky32, kz32, f0cur, Fs, s32,
-                                bch, P);
+                    HT3D_LAUNCH(ctx, k_mixed_inner<false>, ig, ib, 0, Dbuf[cur], Dbuf[prv], Rin, kx32, ky32, kz32, Fs,
+                                s32, prev0 ? 1 : 0, bch, P);
+                std::swap(cur, prv);
                 timer.count();
             }
+            prev0 = false;
         }
-        std::swap(dcur, dnxt);
+        dtau_prev = sc.dtau;
         it_done = iter;
         last_fp64 = chk || refresh;
         last_chk = chk;
@@ -818,12 +871,12 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
     }
     timer.end();
     // final fold of the correction into the FP64 solution
-    HT3D_LAUNCH(ctx, k_mixed_fold, gc, b2, 0, xcur, dcur, last_fp64 ? nullptr : dnxt, bc, P);
+    HT3D_LAUNCH(ctx, k_mixed_fold, gc, b2, 0, xcur, Dbuf[cur], last_fp64 ? nullptr : Dbuf[prv], bc, P);
     if (xcur != X) {
         dim3 g((nx + 2 + 31) / 32, (ny + 2 + 7) / 8, nz + 2);
         HT3D_LAUNCH(ctx, k_copy_ex_faces<double>, g, b2, 0, X, xcur, nx, ny, nz);
     }
-    HT3D_LAUNCH(ctx, k_unpack, gc, b2, 0, F0, f0cur, P);
+    HT3D_LAUNCH(ctx, k_unpack_f0, gc, b2, 0, F0, Dbuf[cur], prev0 ? nullptr : Dbuf[prv], (float)dtau_prev, P);
     if (!last_chk) HT3D_LAUNCH(ctx, k_unpack, gc, b2, 0, F, Fs, P);
     if (derr) {  // a bounded wait of k_mixed_inner2 gave up
         int herr = 0;
@@ -863,16 +916,16 @@ constexpr int kEnsGraphIters = 16;
 constexpr int kEnsTuneRounds = 2;  // timed launches per block size
 
 template <bool STOREF>
-void ens_launch_raw(cudaStream_t st, int cfg, const EnsLaunch& L, int parity) {
+void ens_launch_raw(cudaStream_t st, int cfg, const EnsLaunch& L, int parity, int prev0) {
     const unsigned g = (unsigned)L.nblk;
-    if (cfg == 0) k_ens_inner<STOREF, 64><<<g, 64, 0, st>>>(L, parity);
-    else if (cfg == 1) k_ens_inner<STOREF, 128><<<g, 128, 0, st>>>(L, parity);
-    else k_ens_inner<STOREF, 256><<<g, 256, 0, st>>>(L, parity);
+    if (cfg == 0) k_ens_inner<STOREF, 64><<<g, 64, 0, st>>>(L, parity, prev0);
+    else if (cfg == 1) k_ens_inner<STOREF, 128><<<g, 128, 0, st>>>(L, parity, prev0);
+    else k_ens_inner<STOREF, 256><<<g, 256, 0, st>>>(L, parity, prev0);
 }
 
 template <bool STOREF>
-int ens_launch_all(cudaStream_t st, int cfg, const std::vector<EnsLaunch>& groups, int parity) {
-    for (const EnsLaunch& L : groups) ens_launch_raw<STOREF>(st, cfg, L, parity);
+int ens_launch_all(cudaStream_t st, int cfg, const std::vector<EnsLaunch>& groups, int parity, int prev0) {
+    for (const EnsLaunch& L : groups) ens_launch_raw<STOREF>(st, cfg, L, parity, prev0);
     return (int)groups.size();
 }
 
@@ -881,11 +934,12 @@ struct EnsHost {
     IterLaunch LC;
     double* invPC;
     double* X2;
-    float* f32[8];  // Da, Db, F0, F, Rin, kx, ky, kz
+    float* f32[7];  // Da, Db, F, Rin, kx, ky, kz
     double* xcur;
     double* xnxt;
     DyrelState S;
     DyrelScal sc;
+    double dtau_prev;  // dtau of the update that produced the current correction
     BC6<double> bc;
     BC6<float> bch;
     bool used, active, last_fp64, last_chk;
@@ -912,7 +966,7 @@ bool ens_capture(ht3d_ctx* ctx, unsigned long long sig, int cfg, const std::vect
             cudaGetLastError();
             return false;
         }
-        for (int g = 0; g < kEnsGraphIters; ++g) ens_launch_all<false>(ctx->stream, cfg, groups, (p + g) & 1);
+        for (int g = 0; g < kEnsGraphIters; ++g) ens_launch_all<false>(ctx->stream, cfg, groups, (p + g) & 1, 0);
         cudaGraph_t graph = nullptr;
         const cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
         if (e != cudaSuccess || !graph) {
@@ -1016,9 +1070,9 @@ void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
         HT3D_LAUNCH(ctx, (k_reduce_partials<RED_MAX, 1>), 1, 1024, 0, parts, (int)(gc.x * gc.y * gc.z), dres + q);
         const size_t pbytes = sizeof(float) * (size_t)h.P.size;
         for (float* a : h.f32) HT3D_CUDA(cudaMemsetAsync(a, 0, pbytes, ctx->stream));
-        HT3D_LAUNCH(ctx, k_pack, dim3((nx + 1 + 31) / 32, (ny + 7) / 8, nz), b2, 0, h.f32[5], I.kx, nx + 1, ny, nz, h.P);
-        HT3D_LAUNCH(ctx, k_pack, dim3((nx + 31) / 32, (ny + 1 + 7) / 8, nz), b2, 0, h.f32[6], I.ky, nx, ny + 1, nz, h.P);
-        HT3D_LAUNCH(ctx, k_pack, dim3((nx + 31) / 32, (ny + 7) / 8, nz + 1), b2, 0, h.f32[7], I.kz, nx, ny, nz + 1, h.P);
+        HT3D_LAUNCH(ctx, k_pack, dim3((nx + 1 + 31) / 32, (ny + 7) / 8, nz), b2, 0, h.f32[4], I.kx, nx + 1, ny, nz, h.P);
+        HT3D_LAUNCH(ctx, k_pack, dim3((nx + 31) / 32, (ny + 1 + 7) / 8, nz), b2, 0, h.f32[5], I.ky, nx, ny + 1, nz, h.P);
+        HT3D_LAUNCH(ctx, k_pack, dim3((nx + 31) / 32, (ny + 7) / 8, nz + 1), b2, 0, h.f32[6], I.kz, nx, ny, nz + 1, h.P);
     }
     HT3D_CUDA(cudaMemcpyAsync(hres, dres, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
     HT3D_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -1034,6 +1088,7 @@ void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
         h.sc.h1 = h.S.h1;
         h.sc.h2 = h.S.h2;
         h.sc.dtau = h.S.dtau;
+        h.dtau_prev = h.S.dtau;
         h.xcur = I.X;
         h.xnxt = h.X2;
         h.active = true;
@@ -1074,14 +1129,13 @@ void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
                 EnsInner& e = G.rec[m];
                 e.D[0] = h.f32[0];
                 e.D[1] = h.f32[1];
-                e.F0 = h.f32[2];
-                e.F = h.f32[3];
-                e.Rin = h.f32[4];
-                e.kx = h.f32[5];
-                e.ky = h.f32[6];
-                e.kz = h.f32[7];
+                e.F = h.f32[2];
+                e.Rin = h.f32[3];
+                e.kx = h.f32[4];
+                e.ky = h.f32[5];
+                e.kz = h.f32[6];
                 e.P = h.P;
-                e.s = DyrelScalT<float>(h.sc);
+                e.s = mix_scal(h.sc, h.dtau_prev);
                 e.bc = h.bch;
             }
         }
@@ -1111,6 +1165,7 @@ void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
     auto is_storef = [&](int it) { return !is_fp64(it) && (it == nitmax || is_check(it + 1, nitout)); };
     InnerTimer timer(ctx);
     int nactive = nused;
+    int prev0 = 1;  // the previous corrections are 0 (start, or D just folded): same for every member
     for (int iter = 1; iter <= nitmax && nactive > 0; ++iter) {
         const int parity = (iter - 1) & 1;  // correction buffer of every instance still iterating
         const bool chk = is_check(iter, nitout);
@@ -1123,15 +1178,16 @@ void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
                 h.sc.h2 = h.S.h2;
                 h.sc.dtau = h.S.dtau;
                 const EnsSolveInst& I = in[q];
-                const DyrelScalT<float> s32(h.sc);
+                const MixScal s32 = mix_scal(h.sc, h.dtau_prev);
                 if (chk)
                     HT3D_LAUNCH(ctx, k_mixed_check<true>, h.LC.grid, h.LC.block, 0, h.xcur, h.xnxt, h.f32[parity],
-                                h.f32[parity ^ 1], I.R, I.kx, I.ky, I.kz, h.invPC, h.f32[2], h.f32[3], I.F, h.f32[4],
-                                h.sc, s32, h.bc, h.P, h.LC.zchunk, parts);
+                                h.f32[parity ^ 1], I.R, I.kx, I.ky, I.kz, h.invPC, h.f32[2], I.F, h.f32[3], h.sc, s32,
+                                prev0, h.bc, h.P, h.LC.zchunk, parts);
                 else
                     HT3D_LAUNCH(ctx, k_mixed_check<false>, h.LC.grid, h.LC.block, 0, h.xcur, h.xnxt, h.f32[parity],
-                                h.f32[parity ^ 1], I.R, I.kx, I.ky, I.kz, h.invPC, h.f32[2], h.f32[3], I.F, h.f32[4],
-                                h.sc, s32, h.bc, h.P, h.LC.zchunk, parts);
+                                h.f32[parity ^ 1], I.R, I.kx, I.ky, I.kz, h.invPC, h.f32[2], I.F, h.f32[3], h.sc, s32,
+                                prev0, h.bc, h.P, h.LC.zchunk, parts);
+                h.dtau_prev = h.sc.dtau;
                 std::swap(h.xcur, h.xnxt);
                 h.it_done = iter;
                 h.last_fp64 = true;
@@ -1140,11 +1196,12 @@ void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
                     HT3D_LAUNCH(ctx, (k_reduce_partials<RED_SUM, 3>), 1, 1024, 0, parts, (int)h.LC.nblocks,
                                 dres + 3 * q);
             }
+            prev0 = 1;
         } else {
             timer.begin();
             const bool storef = is_storef(iter);
             int window = 1;
-            if (!storef && !tuning && graphs) {
+            if (!storef && !tuning && graphs && !prev0) {
                 window = 0;
                 while (window < kEnsGraphIters && iter + window <= nitmax && !is_fp64(iter + window) &&
                        !is_storef(iter + window))
@@ -1167,8 +1224,8 @@ void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
                     c = tune_n % 3;
                     HT3D_CUDA(cudaEventRecord(ctx->tune_events[2 * tune_n], ctx->stream));
                 }
-                const int nl = storef ? ens_launch_all<true>(ctx->stream, c, groups[c], parity)
-                                      : ens_launch_all<false>(ctx->stream, c, groups[c], parity);
+                const int nl = storef ? ens_launch_all<true>(ctx->stream, c, groups[c], parity, prev0)
+                                      : ens_launch_all<false>(ctx->stream, c, groups[c], parity, prev0);
                 ctx->launches += nl;
                 timer.count();
                 if (timed) {
@@ -1195,12 +1252,19 @@ void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
                     }
                 }
             }
+            // the records hold mom = h1 dtau / dtau_prev: rebuild them when
+            // that was the first iteration after a parameter update
+            bool stale = false;
             for (int q = 0; q < n; ++q)
                 if (H[q].active) {
                     H[q].it_done = iter + window - 1;
                     H[q].last_fp64 = false;
                     H[q].last_chk = false;
+                    stale = stale || H[q].dtau_prev != H[q].sc.dtau;
+                    H[q].dtau_prev = H[q].sc.dtau;
                 }
+            prev0 = 0;
+            if (stale) build_groups();
             iter += window - 1;
         }
         if (chk) {
@@ -1237,8 +1301,9 @@ void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
             dim3 g((nx + 2 + 31) / 32, (ny + 2 + 7) / 8, nz + 2);
             HT3D_LAUNCH(ctx, k_copy_ex_faces<double>, g, b2, 0, I.X, h.xcur, nx, ny, nz);
         }
-        HT3D_LAUNCH(ctx, k_unpack, gc, b2, 0, I.F0, h.f32[2], h.P);
-        if (!h.last_chk) HT3D_LAUNCH(ctx, k_unpack, gc, b2, 0, I.F, h.f32[3], h.P);
+        HT3D_LAUNCH(ctx, k_unpack_f0, gc, b2, 0, I.F0, h.f32[dc], h.last_fp64 ? nullptr : h.f32[dc ^ 1],
+                    (float)h.dtau_prev, h.P);
+        if (!h.last_chk) HT3D_LAUNCH(ctx, k_unpack, gc, b2, 0, I.F, h.f32[2], h.P);
         h.C.fill(I.st, h.S, h.it_done);
         in[q].status = h.C.status;
     }

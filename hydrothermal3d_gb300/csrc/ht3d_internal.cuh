@@ -24,8 +24,8 @@ enum ScratchSlot {
     SLOT_PC,            // Jacobi diagonal / inverse diagonal
     SLOT_G,             // Gershgorin ratios
     SLOT_SNAP,          // pre-launch snapshot for in-place boundary kernels
-    SLOT_F32_X, SLOT_F32_X2, SLOT_F32_F0, SLOT_F32_R, SLOT_F32_PC, SLOT_F32_KX, SLOT_F32_KY, SLOT_F32_KZ,
-    SLOT_F32_F, SLOT_F32_F0B,
+    SLOT_F32_X, SLOT_F32_X2, SLOT_F32_D3, SLOT_F32_R, SLOT_F32_PC, SLOT_F32_KX, SLOT_F32_KY, SLOT_F32_KZ,
+    SLOT_F32_F, SLOT_F32_D4,
     SLOT_STEP_R, SLOT_STEP_F, SLOT_STEP_F0, SLOT_STEP_TY, SLOT_STEP_KX, SLOT_STEP_KY, SLOT_STEP_KZ,
     SLOT_WENO_T0, SLOT_WENO_T1, SLOT_WENO_T2, SLOT_WENO_V,
     SLOT_AUX0, SLOT_AUX1, SLOT_AUX2, SLOT_AUX3,
