@@ -442,8 +442,9 @@ def roofline(ctx, stream, n, inner, step_ms, iters=20):
            "share_of_timed_region": inner_ms / step_ms if step_ms else None,
            "timing": "CUDA events on the ctx stream around every run of consecutive inner launches inside the "
                      "timed steps (HT3D_TUNE_TIME_INNER)",
-           "note": "the kernel streams 8 of the 9 algorithmic fields (the Jacobi diagonal is recomputed), so "
-                   "achieved can exceed the DRAM rate by up to 9/8; traffic is the measured DRAM bytes"}
+           "note": "the kernel streams 7 of the 9 algorithmic fields (the Jacobi diagonal is recomputed, the DYREL "
+                   "momentum is implied by the previous correction), so achieved can exceed the DRAM rate by up to "
+                   "9/7; traffic is the measured DRAM bytes"}
     X64c = ht.zeros(n + 2, n + 2, n + 2).uniform_(0, 1)
     R64c = ht.zeros(n, n, n).uniform_(-1, 1)
     k64c = [ht.ones(n + 1, n, n), ht.ones(n, n + 1, n), ht.ones(n, n, n + 1)]
