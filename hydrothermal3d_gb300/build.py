@@ -58,11 +58,17 @@ def _compile(nvcc, src, extra):
 
 def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     """Compile and link libht3d.so; returns its path."""
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _deps_mtime():
+    if not force and not os.environ.get("HT3D_NVCC_FLAGS") and os.path.exists(LIB) and \
+            os.path.getmtime(LIB) >= _deps_mtime():
         return LIB
     nvcc = _nvcc()
     os.makedirs(OBJ, exist_ok=True)
     extra = ["-Xptxas", "-v"] if verbose_ptxas else []
+    # HT3D_NVCC_FLAGS: extra nvcc flags for every translation unit (e.g. -D
+    # switches for experiments or -G for debugging); a rebuild is forced
+    env_flags = os.environ.get("HT3D_NVCC_FLAGS", "").split()
+    if env_flags:
+        extra += env_flags
     srcs = _sources()
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         results = list(ex.map(lambda s: _compile(nvcc, s, extra), srcs))
