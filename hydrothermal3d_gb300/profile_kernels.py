@@ -9,7 +9,9 @@ dyrel_f32 (FP32 pseudo-iteration on the reference layout),
 dyrel_f64 (plain FP64 pseudo-iteration), mixed_solve (a mixed-form DYREL
 solve of --iters pseudo-iterations: two FP64 checks, then the padded FP32
 inner kernel k_mixed_inner), weno_f64 / weno_mixed (one fused WENO5
-advection), post (one fused pass of the twelve output diagnostics, k_post).
+advection), post (one fused pass of the twelve output diagnostics, k_post),
+dim_step (one dimensional v18 time step, it = 0, with --iters pseudo-iterations
+per solve: k_dim_iter thermal then Darcy).
 Prints the average time per launch measured with CUDA events.
 """
 import argparse
@@ -25,7 +27,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--kernel", default="dyrel_f32",
                     choices=["dyrel_f32", "dyrel_f64", "mixed_solve", "weno_f64", "weno_mixed", "weno_f32",
-                             "ensemble", "post"])
+                             "ensemble", "post", "dim_step"])
     ap.add_argument("--members", type=int, default=16, help="ensemble members (--kernel ensemble)")
     ap.add_argument("--n", type=int, default=255)
     ap.add_argument("--iters", type=int, default=5)
@@ -117,6 +119,25 @@ def main():
         t = e0.elapsed_time(e1) / 1e3 / a.iters
         print(json.dumps({"kernel": "k_post", "n": n, "us_per_pass": t * 1e6,
                           "alg_GBs": post.bytes_fused(n, n, n) / t / 1e9}))
+    elif a.kernel == "dim_step":
+        from hydrothermal3d_gb300 import api, v18
+        nit = max(2, a.iters)
+        b = v18.box(n, n, n, seed=2, nitmax=nit, nitout=max(1, nit // 2))
+        p = b["params"]
+        p.it = 0
+        T, P = ht.from_numpy(b["T"]), ht.from_numpy(b["P"])
+        args = (ht.from_numpy(b["phc"]), ht.from_numpy(b["phv"]), ht.from_numpy(b["wN"]), ht.from_numpy(b["kmul"]))
+        V = [ht.zeros(n + 1, n, n), ht.zeros(n, n + 1, n), ht.zeros(n, n, n + 1)]
+        torch.cuda.synchronize()  # inputs were built on torch's stream
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            gt, gd = api.step_v18(ctx, T, P, *args, *V, p)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1e3
+        bt, bd = v18.bytes_per_iteration(n, n, n)
+        print(json.dumps({"kernel": "k_dim_iter (v18 step)", "n": n, "iters": [gt.iters, gd.iters], "ms_per_step": t * 1e3,
+                          "alg_GBs_iterations": (gt.iters * bt + gd.iters * bd) / t / 1e9}))
     elif a.kernel == "weno_f32":
         from hydrothermal3d_gb300 import api, sweep
         V = [v.float().permute(2, 1, 0).contiguous().permute(2, 1, 0) for v in sweep.curl_velocity(n, n, n, seed=6)]
