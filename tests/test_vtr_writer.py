@@ -65,3 +65,18 @@ def test_rejects_bad_arguments(tmp_path):
     with pytest.raises(api.Ht3dError) as e:
         api.write_vtr(tmp_path / "no_such_dir" / "a", x, x, x, {"T": np.zeros((2, 2, 2))})
     assert e.value.status == abi.ERR_IO
+
+
+def test_vector_field_across_interleave_chunks(tmp_path):
+    """More points than one interleave chunk (65536): components stay aligned."""
+    nx, ny, nz = 50, 41, 37  # 75850 points
+    rng = np.random.default_rng(3)
+    V = tuple(np.asfortranarray(rng.standard_normal((nx, ny, nz))) for _ in range(3))
+    out = api.write_vtr(tmp_path / "big.vtr", np.arange(nx, dtype=float), np.arange(ny, dtype=float),
+                        np.arange(nz, dtype=float), {"Velocity": V, "Peclet": V[0] * 2})
+    assert out.endswith("big.vtr") and not out.endswith(".vtr.vtr")
+    n, f = read_vtr(out)
+    assert n == (nx, ny, nz)
+    for a, b in zip(f["Velocity"], V):
+        assert np.array_equal(a, b)
+    assert np.array_equal(f["Peclet"], V[0] * 2)
