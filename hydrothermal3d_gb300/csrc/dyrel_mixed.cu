@@ -105,7 +105,8 @@ inline MixScal mix_scal(const DyrelScal& s, double dtau_prev) {
 // One cell of the FP32 inner iteration (the single place its arithmetic is
 // written, so every kernel that updates a cell rounds alike):
 //     F = (R + cX x + div q(x)) / diag,  x' = x + mom (x - xprev) - dh2 F
-// with q = -k dx on the six faces and diag = sum of k/dx^2 over them + cX.
+// with q = -k dx on the six faces and diag = sum of k/dx^2 over them + cX;
+// div q is evaluated per axis as dx^2 (k_in (x - x_in) - k_out (x_out - x)).
 // Every operation is an explicit round-to-nearest intrinsic: the compiler may
 // neither contract nor reassociate them, so the value of a cell does not depend
 // on the kernel it is inlined into (k_mixed_inner shares fluxes between the
@@ -114,16 +115,14 @@ __device__ __forceinline__ void mixed_cell(float xc, float xw, float xe, float x
                                            float kW, float kE, float kS, float kN, float kB, float kF, float r,
                                            float xprev, float mom, float dh2, float cX, float _dx, float _dy,
                                            float _dz, float _dx2, float _dy2, float _dz2, float& f, float& xnew) {
-    const float qW = -__fmul_rn(kW, __fmul_rn(_dx, __fsub_rn(xc, xw)));
-    const float qE = -__fmul_rn(kE, __fmul_rn(_dx, __fsub_rn(xe, xc)));
-    const float qS = -__fmul_rn(kS, __fmul_rn(_dy, __fsub_rn(xc, xs)));
-    const float qN = -__fmul_rn(kN, __fmul_rn(_dy, __fsub_rn(xn, xc)));
-    const float qB = -__fmul_rn(kB, __fmul_rn(_dz, __fsub_rn(xc, xb)));
-    const float qF = -__fmul_rn(kF, __fmul_rn(_dz, __fsub_rn(xf, xc)));
+    // dx (qE - qW) with q = -k dx (x_out - x_in) is dx^2 (kW (xc - xw) - kE (xe - xc))
+    const float gx = __fmaf_rn(kW, __fsub_rn(xc, xw), -__fmul_rn(kE, __fsub_rn(xe, xc)));
+    const float gy = __fmaf_rn(kS, __fsub_rn(xc, xs), -__fmul_rn(kN, __fsub_rn(xn, xc)));
+    const float gz = __fmaf_rn(kB, __fsub_rn(xc, xb), -__fmul_rn(kF, __fsub_rn(xf, xc)));
     float fu = __fmaf_rn(cX, xc, r);
-    fu = __fmaf_rn(_dx, __fsub_rn(qE, qW), fu);
-    fu = __fmaf_rn(_dy, __fsub_rn(qN, qS), fu);
-    fu = __fmaf_rn(_dz, __fsub_rn(qF, qB), fu);
+    fu = __fmaf_rn(_dx2, gx, fu);
+    fu = __fmaf_rn(_dy2, gy, fu);
+    fu = __fmaf_rn(_dz2, gz, fu);
     float diag = __fmaf_rn(__fadd_rn(kW, kE), _dx2, cX);
     diag = __fmaf_rn(__fadd_rn(kS, kN), _dy2, diag);
     diag = __fmaf_rn(__fadd_rn(kB, kF), _dz2, diag);
