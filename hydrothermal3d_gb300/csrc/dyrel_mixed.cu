@@ -526,10 +526,11 @@ __global__ void __launch_bounds__(BS) k_ens_inner(const __grid_constant__ EnsLau
     }
     const EnsInner& e = L.rec[lo];
     // the member's quads in (quad, row, plane) order, BS per block across planes
-    const long long tg = (long long)(blockIdx.x - L.block0[lo]) * BS + threadIdx.x;
-    const int pq = L.quads[lo];  // quads per plane
+    // (fewer than 2^30 quads per member: 32-bit unsigned arithmetic)
+    const unsigned tg = (unsigned)(blockIdx.x - L.block0[lo]) * BS + threadIdx.x;
+    const unsigned pq = (unsigned)L.quads[lo];  // quads per plane
     int k = (int)(tg / pq);
-    const int t = (int)(tg - (long long)k * pq);
+    const int t = (int)(tg - (unsigned)k * pq);
     const bool live = k < e.P.nz;
     if (!live) k = e.P.nz - 1;
     mixed_quad<STOREF>(e.D[parity], e.D[parity ^ 1], e.Rin, e.kx, e.ky, e.kz, e.F, e.s, prev0 != 0, e.bc, e.P, t, k,
