@@ -31,8 +31,10 @@ struct File {
 bool write_all(FILE* f, const void* p, size_t n) { return n == 0 || std::fwrite(p, 1, n, f) == n; }
 bool read_all(FILE* f, void* p, size_t n) { return n == 0 || std::fread(p, 1, n, f) == n; }
 
+// a field name is written into an XML attribute: non-empty, at most 200
+// bytes, none of the characters that would need escaping
 bool valid_name(const char* s) {
-    if (!s || !*s) return false;
+    if (!s || !*s || std::strlen(s) > 200) return false;
     for (; *s; ++s)
         if (*s == '"' || *s == '<' || *s == '>' || *s == '&' || (unsigned char)*s < 0x20) return false;
     return true;

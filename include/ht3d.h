@@ -575,8 +575,9 @@ int ht3d_Nusselt(ht3d_ctx* ctx, const double* qy, double Lx, double Lz, int nx, 
    field order (a 3-component field gives its X, Y, Z arrays, interleaved in
    the file like WriteVTK's tuple).  VTK XML, Float64, one appended raw block
    (UInt64 headers, little-endian).  ".vtr" is appended to path unless present.
-   Host-only: needs no context or GPU.  HT3D_ERR_IO if the file cannot be
-   written. */
+   Field names: 1-200 bytes, none of " < > & or control characters
+   (HT3D_ERR_ARG otherwise).  Host-only: needs no context or GPU.  HT3D_ERR_IO
+   if the file cannot be written. */
 int ht3d_write_vtr(const char* path, const double* x, const double* y, const double* z, int nx, int ny, int nz,
                    int nfields, const char* const* names, const int* ncomp, const double* const* data);
 

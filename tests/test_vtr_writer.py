@@ -62,6 +62,9 @@ def test_rejects_bad_arguments(tmp_path):
     with pytest.raises(api.Ht3dError) as e:  # quote in a name would break the XML
         api.write_vtr(tmp_path / "a", x, x, x, {'T"x': np.zeros((2, 2, 2))})
     assert e.value.status == abi.ERR_ARG
+    with pytest.raises(api.Ht3dError) as e:  # longer than an XML attribute the writer accepts
+        api.write_vtr(tmp_path / "a", x, x, x, {"T" * 201: np.zeros((2, 2, 2))})
+    assert e.value.status == abi.ERR_ARG
     with pytest.raises(api.Ht3dError) as e:
         api.write_vtr(tmp_path / "no_such_dir" / "a", x, x, x, {"T": np.zeros((2, 2, 2))})
     assert e.value.status == abi.ERR_IO
