@@ -114,3 +114,67 @@ def test_dyrel_parameters(orc):
     assert st.h1 == (2 - c * dtau) / (2 + c * dtau) and st.h2 == 2 * dtau / (2 + c * dtau)
     # uniform k, Neumann: G/D = 2 (sum |offdiag| = diag)
     assert abs(lmax - 2.0) <= 1e-14
+
+
+def test_weno5_mass_of_a_translated_blob(orc):
+    """Advective-form WENO5 conserves the blob's mass to truncation error
+    (Gaussian of the TestAdvection.jl set-up, uniform V, walls far away); the
+    reference's v2 stencil quirk loses more than the fixed stencil."""
+    ncx = ncy = 122
+    ncz = 3
+    dx = dy = 2.0 / ncx
+    dz = 1.0 / ncz
+    xce = np.linspace(-1 - dx / 2, 1 + dx / 2, ncx + 2)
+    yce = np.linspace(-1 - dy / 2, 1 + dy / 2, ncy + 2)
+    base = (5 * np.exp(-((xce[:, None] + 0.5) ** 2) / 0.01 - ((yce[None, :] + 0.5) ** 2) / 0.01) + 1.0)[:, :, None]
+    Vx = np.ones((ncx + 1, ncy, ncz), order="F")
+    Vy = np.ones((ncx, ncy + 1, ncz), order="F")
+    Vz = np.zeros((ncx, ncy, ncz + 1), order="F")
+    dt = 0.5 * min(dx, dy, dz)
+    drift = {}
+    for variant in (abi.WENO_V2_REF, abi.WENO_V2_FIXED):
+        T = np.asfortranarray(np.broadcast_to(base, (ncx + 2, ncy + 2, ncz + 2)).copy())
+        m0 = (T[1:-1, 1:-1, 1:-1] - 1).sum()
+        for _ in range(50):
+            orc.call("AdvectWithWeno5_v2", T, Vx, Vy, Vz, dt, 1 / dx, 1 / dy, 1 / dz, orc.int6(0, 0, 1, 1, 0, 0),
+                     orc.dbl6(0, 0, 1.0, 1.0, 0, 0), ctypes.c_int(1 if variant == abi.WENO_V2_REF else 0), ncx,
+                     ncy, ncz)
+        drift[variant] = abs((T[1:-1, 1:-1, 1:-1] - 1).sum() - m0) / m0
+    assert drift[abi.WENO_V2_FIXED] < 5e-3
+    assert drift[abi.WENO_V2_FIXED] < drift[abi.WENO_V2_REF] < 1e-2
+
+
+def test_geotherm_column_matches_1d_solve(orc):
+    """Steady DYREL solve with y-varying k and source: x/z-invariant and equal
+    to the exact 1-D solve of the same discrete operator."""
+    from kat_cases import GEO_N, GEO_BC, geotherm_case, geotherm_exact, geotherm_params
+    nx, ny, nz = GEO_N
+    c = geotherm_case()
+    X = np.zeros((nx + 2, ny + 2, nz + 2), order="F")
+    F, F0 = orc.zeros(nx, ny, nz), orc.zeros(nx, ny, nz)
+    s, st = orc.dyrel_solve_dimless(X, c["R"], c["kx"], c["ky"], c["kz"], 0.0, *c["d"], *GEO_BC, geotherm_params(),
+                                    F, F0)
+    assert s == 0
+    col = X[1:-1, 1:-1, 1:-1]
+    assert np.ptp(col, axis=(0, 2)).max() == 0.0
+    Tex = geotherm_exact(c)
+    assert np.abs(col - Tex[None, :, None]).max() <= 1e-12 * np.abs(Tex).max()
+
+
+def test_hrl_onset_growth_factor(orc):
+    """Horton-Rogers-Lapwood onset: below Ra = 4 pi^2 the mode decays, above
+    it grows, each step by the linear factor (1 + dt Ra/2)/(1 + 2 pi^2 dt)."""
+    from kat_cases import ONSET_N, ONSET_STEPS, onset_case, onset_factor
+    n = ONSET_N
+    for Ra in (20.0, 80.0):
+        T, P, ktv, kfv, p, amplitude = onset_case(Ra)
+        V = [np.zeros(s, order="F") for s in ((n + 1, n, n), (n, n + 1, n), (n, n, n + 1))]
+        a = [amplitude(T[1:-1, 1:-1, 1:-1])]
+        for _ in range(ONSET_STEPS):
+            s, _, _ = orc.step_hrl(T, P, ktv, kfv, *V, p)
+            assert s == 0
+            a.append(amplitude(T[1:-1, 1:-1, 1:-1]))
+        ratios = np.array(a[1:]) / np.array(a[:-1])
+        G = onset_factor(Ra)
+        assert np.all(np.abs(ratios - G) <= 5e-3 * G), (Ra, ratios, G)
+        assert (a[-1] < a[0]) if Ra < 4 * np.pi ** 2 else (a[-1] > a[0])
