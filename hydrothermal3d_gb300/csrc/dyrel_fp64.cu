@@ -8,6 +8,7 @@ int ht3d_dyrel_solve_fp64(ht3d_ctx* ctx, double* X, const double* R, const doubl
                           const double* kz, double cX, double dx, double dy, double dz, const int* bc_type6,
                           const double* bc_val6, const ht3d_dyrel_params* prm, int n_iter_fixed, double* F, double* F0,
                           ht3d_dyrel_stats* st, int nx, int ny, int nz) {
+    NvtxRange range("ht3d DYREL solve (FP64)");
     const long long n = (long long)nx * ny * nz;
     const long long nex = (long long)(nx + 2) * (ny + 2) * (nz + 2);
     double* PC = (double*)ht3d_scratch(ctx, SLOT_PC, sizeof(double) * n);

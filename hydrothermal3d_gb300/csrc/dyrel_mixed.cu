@@ -718,6 +718,7 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
                            const double* kz, double cX, double dx, double dy, double dz, const int* bc_type6,
                            const double* bc_val6, const ht3d_dyrel_params* prm, int n_iter_fixed, double* F,
                            double* F0, ht3d_dyrel_stats* st, int nx, int ny, int nz) {
+    NvtxRange range("ht3d DYREL solve (mixed)");
     const long long n = (long long)nx * ny * nz;
     const long long nex = (long long)(nx + 2) * (ny + 2) * (nz + 2);
     const Pad P = make_pad(nx, ny, nz);
@@ -998,6 +999,7 @@ bool ens_capture(ht3d_ctx* ctx, unsigned long long sig, int cfg, const std::vect
 }  // namespace
 
 void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
+    NvtxRange range("ht3d batched DYREL solve");
     std::vector<EnsHost> H(n);
     int nitout = 0, nitmax = 0, nused = 0;
     for (int q = 0; q < n; ++q) {

@@ -26,6 +26,7 @@ T* carve(char* base, size_t& off, size_t count) {
 
 extern "C" int ht3d_ensemble_step(ht3d_ctx* ctx, ht3d_instance* m, int n, int precision) {
     return ht3d_guard(ctx, [&]() {
+        NvtxRange range("ht3d ensemble_step");
         HT3D_REQUIRE(m && n > 0, "no members");
         HT3D_REQUIRE(precision == HT3D_FP64 || precision == HT3D_MIXED, "unknown precision");
         for (int q = 0; q < n; ++q) {

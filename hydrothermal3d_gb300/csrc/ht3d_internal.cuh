@@ -8,6 +8,8 @@
 #include <vector>
 #include <stdexcept>
 
+#include <nvtx3/nvToolsExt.h>  // header-only NVTX v3: named ranges for timeline profilers
+
 #include "../../include/ht3d.h"
 
 // ---------------------------------------------------------------------------
@@ -64,6 +66,15 @@ struct ht3d_ctx {
     void* slot_ptr[SLOT_COUNT] = {};
     size_t slot_bytes[SLOT_COUNT] = {};
     double* h_result = nullptr;  // pinned, 64 doubles
+};
+
+// Named host range around a solver phase ("ht3d step_hrl", "ht3d thermal
+// solve", ...), visible in timeline profilers; free when none is attached.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
 };
 
 struct ht3d_error : public std::runtime_error {

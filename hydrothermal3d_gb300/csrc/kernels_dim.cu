@@ -717,6 +717,7 @@ extern "C" int ht3d_step_v18(ht3d_ctx* ctx, double* Tc_ex, double* Pc_ex, const 
                              ht3d_v18_params* p, ht3d_dyrel_stats* st_T, ht3d_dyrel_stats* st_P, int nx, int ny,
                              int nz) {
     return ht3d_guard(ctx, [&]() {
+        NvtxRange range("ht3d step_v18");
         ht3d_check_dims(nx, ny, nz, 3);
         HT3D_REQUIRE(Tc_ex && Pc_ex && phc_ex && phv && wN && Vx && Vy && Vz && p, "null argument");
         HT3D_REQUIRE(p->dt > 0.0, "dt must be positive");

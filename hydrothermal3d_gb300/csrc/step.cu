@@ -21,6 +21,7 @@ void ht3d_weno5_advect_impl(ht3d_ctx* ctx, double* Tc_ex, const double* Vx, cons
 int ht3d_step_hrl_impl(ht3d_ctx* ctx, double* Tc_ex, double* Pc_ex, const double* ktv, const double* kfv, double* Vx,
                        double* Vy, double* Vz, ht3d_hrl_params* p, ht3d_dyrel_stats* st_thermal,
                        ht3d_dyrel_stats* st_darcy, int precision, int nx, int ny, int nz) {
+    NvtxRange range("ht3d step_hrl");
     ht3d_check_dims(nx, ny, nz, 1);
     HT3D_REQUIRE(Tc_ex && Pc_ex && ktv && kfv && Vx && Vy && Vz && p, "null argument");
     HT3D_REQUIRE(precision == HT3D_FP64 || precision == HT3D_MIXED, "unknown precision");

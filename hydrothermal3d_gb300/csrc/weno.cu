@@ -216,6 +216,7 @@ void weno_all(ht3d_ctx* ctx, double* T, double* T1, const double* const* V, doub
 void ht3d_weno5_advect_impl(ht3d_ctx* ctx, double* Tc_ex, const double* Vx, const double* Vy, const double* Vz,
                             double dt, double _dx, double _dy, double _dz, const int* bc_type6, const double* bc_val6,
                             int variant, int precision, int nx, int ny, int nz) {
+    NvtxRange range("ht3d WENO5 advection");
     ht3d_check_dims(nx, ny, nz, 3);
     HT3D_REQUIRE(variant >= HT3D_WENO_V1 && variant <= HT3D_WENO_V2_FIXED, "unknown WENO variant");
     HT3D_REQUIRE(precision == HT3D_FP64 || precision == HT3D_MIXED, "unknown precision");
