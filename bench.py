@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--ens-members", type=int, default=64)
     ap.add_argument("--ens-steps", type=int, default=20)
     ap.add_argument("--skip-ensemble", action="store_true")
+    ap.add_argument("--mixed-refresh", type=int, default=0,
+                    help="FP64 refresh cadence of the mixed form in inner iterations (0 = library default)")
     ap.add_argument("--post-n", type=int, default=255, help="cells per axis of the output-diagnostics pass (0 = skip)")
     ap.add_argument("--sweep-n", type=int, default=511, help="cells per axis of the standalone WENO5 sweep (0 = skip)")
     ap.add_argument("--c63-steps", type=int, default=10,
@@ -67,6 +69,8 @@ def workload_config(a, extra=None):
          "cells": a.n ** 3, "Ra": 1000.0, "dyrel_tol": 1e-8, "nitout": a.nitout,
          "l2_policy": "inputs larger than L2 (each 255^3 FP64 field is 133 MB > 129 MB L2)",
          "parallelism": f"replicas x{a.gpus}"}
+    if getattr(a, "mixed_refresh", 0):
+        c["mixed_refresh"] = a.mixed_refresh
     if extra:
         c.update(extra)
     return c
@@ -288,6 +292,8 @@ def run_ours(a):
     torch.cuda.set_device(dev)
     stream = torch.cuda.Stream()
     ctx = ht.Context(device=dev, stream=stream.cuda_stream)
+    if a.mixed_refresh:
+        ctx.set_tuning(abi.TUNE_MIXED_REFRESH, a.mixed_refresh)
     n = a.n
     N = n ** 3
     T0, P0, ktv, kfv = hrl.initial_fields(n, n, n, seed=1)
