@@ -13,6 +13,7 @@ TUNE_TIME_INNER = 3
 TUNE_ENS_BLOCK = 4
 TUNE_ENS_GRAPH = 5
 TUNE_TEMPORAL = 6
+TUNE_WAIT_TEST = 7
 DYREL_ZMARCH, DYREL_CELL = 1, 2
 
 

@@ -181,6 +181,11 @@ int ht3d_ctx_set_tuning(ht3d_ctx* ctx, int key, int value) {
         ctx->mixed_temporal = value;
         return HT3D_OK;
     }
+    if (key == HT3D_TUNE_WAIT_TEST) {
+        if (value < 0 || value > 1 << 20) return HT3D_ERR_ARG;
+        ctx->wait_test = value;
+        return HT3D_OK;
+    }
     if (key == HT3D_TUNE_TIME_INNER) {
         if (value != 0 && value != 1) return HT3D_ERR_ARG;
         ctx->time_inner = value;

@@ -290,8 +290,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
         : "memory");
     return ok != 0;
 }
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
-    for (unsigned it = 0; it < kTbWaitLimit; ++it)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, unsigned limit = kTbWaitLimit) {
+    for (unsigned it = 0; it < limit; ++it)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -307,7 +307,8 @@ __global__ void __launch_bounds__(TB_X* TB_Y, 2) k_mixed_inner2(const __grid_con
                                                                 const float* __restrict__ Din, float* __restrict__ D1out,
                                                                 float* __restrict__ D2out, float* __restrict__ F,
                                                                 MixScal s, BC6<float> bc, Pad p, int zchunk,
-                                                                int* __restrict__ err) {
+                                                                int* __restrict__ err, int skip_plane,
+                                                                unsigned detect_limit) {
     extern __shared__ unsigned char tb_raw[];
     unsigned char* base = tb_raw + ((128 - (smem_u32(tb_raw) & 127)) & 127);
     TbStage* st = reinterpret_cast<TbStage*>(base);
@@ -330,7 +331,10 @@ __global__ void __launch_bounds__(TB_X* TB_Y, 2) k_mixed_inner2(const __grid_con
     const int oD = (ty + 1) * TB_BW + tx + (x0 - xD);  // D centre
     const int oK = ty * TB_BW + tx + (x0 - xK);        // faces / cell fields
     const int oP = ty * TB_X + tx;                      // D' planes
+    // skip_plane >= 0 (HT3D_TUNE_WAIT_TEST only): that plane's copies are never
+    // issued, so its wait runs out and the error path below is exercised
     auto issue = [&](int k) {  // thread 0: the six boxes of plane k into slot k % TB_STAGES
+        if (k == skip_plane) return;
         TbStage& S = st[k % TB_STAGES];
         uint64_t* b = &bar[k % TB_STAGES];
         mbar_expect_tx(b, kTbStageBytes);
@@ -379,16 +383,19 @@ __global__ void __launch_bounds__(TB_X* TB_Y, 2) k_mixed_inner2(const __grid_con
         // slot); thread 0 polls the barriers, the CTA barrier then releases (and
         // orders the copied data for) every other thread
         if (tid == 0) {
-            bool ok = mbar_wait_bounded(&bar[pl % TB_STAGES], ((pl - pa0) / TB_STAGES) & 1);
+            bool ok = mbar_wait_bounded(&bar[pl % TB_STAGES], ((pl - pa0) / TB_STAGES) & 1, detect_limit);
             if (pl + 1 <= plast)
-                ok = ok && mbar_wait_bounded(&bar[(pl + 1) % TB_STAGES], ((pl + 1 - pa0) / TB_STAGES) & 1);
+                ok = ok && mbar_wait_bounded(&bar[(pl + 1) % TB_STAGES], ((pl + 1 - pa0) / TB_STAGES) & 1,
+                                             detect_limit);
             if (!ok) abort_flag = 1;
         }
         __syncthreads();
         if (abort_flag) {
             if (tid == 0) {
                 atomicExch(err, HT3D_ERR_TIMEOUT);
-                for (int q = pl; q <= issued; ++q) mbar_wait_bounded(&bar[q % TB_STAGES], ((q - pa0) / TB_STAGES) & 1);
+                // every copy issued must land before the CTA's shared memory is released
+                for (int q = pl; q <= issued; ++q)
+                    if (q != skip_plane) mbar_wait_bounded(&bar[q % TB_STAGES], ((q - pa0) / TB_STAGES) & 1);
             }
             __syncthreads();
             return;
@@ -846,12 +853,16 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
                 TbMaps mp = mk;
                 mp.D = mapD[cur];
                 mp.Dp = mapP[prv];
+                // HT3D_TUNE_WAIT_TEST: this pass skips one plane's copies and detects with a short limit
+                const int skip = ctx->wait_test > 0 ? ctx->wait_test - 1 : -1;
+                const unsigned lim = ctx->wait_test > 0 ? (1u << 12) : kTbWaitLimit;
+                ctx->wait_test = 0;
                 if (storef2)
                     HT3D_LAUNCH(ctx, k_mixed_inner2<true>, tg, tb, kTbSmem, mp, Dbuf[cur], Dbuf[o1], Dbuf[o2], Fs, s32,
-                                bch, P, zc, derr);
+                                bch, P, zc, derr, skip, lim);
                 else
                     HT3D_LAUNCH(ctx, k_mixed_inner2<false>, tg, tb, kTbSmem, mp, Dbuf[cur], Dbuf[o1], Dbuf[o2], Fs,
-                                s32, bch, P, zc, derr);
+                                s32, bch, P, zc, derr, skip, lim);
                 prv = o1;
                 cur = o2;
                 timer.count(2);
@@ -893,7 +904,7 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
         int herr = 0;
         HT3D_CUDA(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
         HT3D_CUDA(cudaStreamSynchronize(ctx->stream));
-        if (herr && C.status == HT3D_OK) C.status = herr;
+        if (herr) C.status = herr;  // the root cause: later NaN checks follow from the aborted pass
     }
     timer.collect();
     C.fill(st, S, it_done);

@@ -78,8 +78,13 @@ extern "C" {
                                        blocking, z-chunk chosen per grid), >= 2 = the same
                                        with that many planes per chunk; bit-identical
                                        results (on GB300 the two-iteration pass, TMA-staged,
-                                       is still instruction-issue bound and slower: 95
-                                       vs 86 us per iteration at 255^3)                  */
+                                       is still instruction-issue bound and slower: 94
+                                       vs 76 us per iteration at 255^3)                  */
+#define HT3D_TUNE_WAIT_TEST 7       /* test hook of the bounded waits: v > 0 makes the next
+                                       two-iteration pass (HT3D_TUNE_TEMPORAL) skip the
+                                       copies of plane v - 1 and give up after 4096 polls;
+                                       the solve returns HT3D_ERR_TIMEOUT and the context
+                                       stays usable.  Reset after that pass.             */
 
 typedef struct ht3d_ctx ht3d_ctx;
 

@@ -269,3 +269,39 @@ def test_mixed_temporal_blocking_is_bit_identical(ctx, n, niter, refresh, zchunk
     np.testing.assert_array_equal(a[1], b[1])
     np.testing.assert_array_equal(a[2], b[2])
     assert a[3:] == b[3:]
+
+
+def test_bounded_wait_runs_out_and_context_recovers(ctx):
+    """HT3D_TUNE_WAIT_TEST: the first two-iteration pass never issues the copies
+    of plane 1, its bounded mbarrier wait gives up, the CTA waits for the copies
+    it did issue and returns, and the solve reports HT3D_ERR_TIMEOUT.  The same
+    context then solves normally: bit-identical to the per-iteration kernel."""
+    n = (30, 14, 9)
+    nx, ny, nz = n
+    X, R, k = problem(n, seed=43)
+    types, vals = BCS["mixedbc"]
+    prm = abi.DyrelParams.reference(nitout=10)
+    d = (1.0 / nx, 0.9 / ny, 1.2 / nz)
+
+    def solve():
+        Xd, Fd, F0d = ht.from_numpy(X), ht.zeros(nx, ny, nz), ht.zeros(nx, ny, nz)
+        api.dyrel_solve_dimless(ctx, Xd, ht.from_numpy(R), *[ht.from_numpy(a) for a in k], 30.0, *d, types, vals,
+                                prm, Fd, F0d, abi.MIXED, n_iter_fixed=9)
+        return ht.to_numpy(Xd), ht.to_numpy(Fd), ht.to_numpy(F0d)
+
+    try:
+        ctx.set_tuning(abi.TUNE_TEMPORAL, 1)
+        ctx.set_tuning(abi.TUNE_WAIT_TEST, 2)
+        with pytest.raises(api.Ht3dError) as e:
+            solve()
+        assert e.value.status == abi.ERR_TIMEOUT
+        paired = solve()  # the hook is spent: a normal solve on the same context
+        ctx.set_tuning(abi.TUNE_TEMPORAL, 0)
+        single = solve()
+    finally:
+        ctx.set_tuning(abi.TUNE_WAIT_TEST, 0)
+        ctx.set_tuning(abi.TUNE_TEMPORAL, 0)
+    m = no_edges_mask(X.shape)
+    np.testing.assert_array_equal(paired[0][m], single[0][m])
+    np.testing.assert_array_equal(paired[1], single[1])
+    np.testing.assert_array_equal(paired[2], single[2])
