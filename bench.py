@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--skip-ensemble", action="store_true")
     ap.add_argument("--mixed-refresh", type=int, default=0,
                     help="FP64 refresh cadence of the mixed form in inner iterations (0 = library default)")
+    ap.add_argument("--nu-steps", type=int, default=60,
+                    help="time steps of the 63^3 Nusselt time series, FP64 vs mixed (0 = skip)")
     ap.add_argument("--post-n", type=int, default=255, help="cells per axis of the output-diagnostics pass (0 = skip)")
     ap.add_argument("--sweep-n", type=int, default=511, help="cells per axis of the standalone WENO5 sweep (0 = skip)")
     ap.add_argument("--c63-steps", type=int, default=10,
@@ -385,6 +387,8 @@ def run_ours(a):
         out["config_63"] = c63_bench(ctx, stream, a.c63_steps)
     if a.post_n:
         out["diagnostics"] = post_bench(ctx, stream, a.post_n)
+    if a.nu_steps and rank == 0:
+        out["nusselt_63"] = nusselt_bench(ctx, stream, a.nu_steps)
 
     if rank == 0:
         v, cores, desc, _ = cpu_sample(n, a.cpu_seconds, threads=os.cpu_count())
@@ -723,6 +727,36 @@ def post_bench(ctx, stream, n, reps=5):
             "single_field_ms": per_field, "alg_bytes_per_cell": {"separate": bs // n ** 3, "fused": bf // n ** 3}, "dtype": "f64",
             "case": "seeded phases (crust, fault, pluton, immersed, 5 % air rows), T 300-900 K, P 0.1-300 MPa, "
                     "face velocities; all twelve VTK fields"}
+
+
+def nusselt_bench(ctx, stream, steps, n=63):
+    """Nusselt-number time series of the HRL run at n^3 through the time-loop
+    driver, plain FP64 and mixed form from the same initial state: the mixed
+    form must track the FP64 physics over many steps."""
+    import torch
+    import hydrothermal3d_gb300 as ht
+    from hydrothermal3d_gb300 import abi, driver, hrl
+    out = {"n": n, "steps": steps}
+    series = {}
+    with torch.cuda.stream(stream):
+        for name, prec in (("fp64", abi.FP64), ("mixed", abi.MIXED)):
+            T0, P0, ktv, kfv = hrl.initial_fields(n, n, n, seed=1)
+            T, P, ktd, kfd = (ht.from_numpy(x) for x in (T0, P0, ktv, kfv))
+            V = (ht.zeros(n + 1, n, n), ht.zeros(n, n + 1, n), ht.zeros(n, n, n + 1))
+            p = hrl.params(n, n, n)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            recs = driver.run_hrl(ctx, T, P, ktd, kfd, V, p, steps, prec)
+            out[name + "_seconds"] = time.perf_counter() - t0
+            series[name] = [(r["time"], r["Nu"]) for r in recs]
+    nu64 = [nu for _, nu in series["fp64"]]
+    numx = [nu for _, nu in series["mixed"]]
+    out["Nu_fp64_every_10_steps"] = nu64[9::10]
+    out["Nu_mixed_every_10_steps"] = numx[9::10]
+    out["time_every_10_steps"] = [t for t, _ in series["fp64"]][9::10]
+    out["max_abs_Nu_difference"] = max(abs(x - y) for x, y in zip(nu64, numx))
+    out["note"] = "Nu of T after each step (driver.py); both runs from the seed-1 initial condition"
+    return out
 
 
 def fault_bench(ctx, stream, a):
