@@ -64,3 +64,27 @@ def test_fault_slab_case():
     assert abs(float(torch.log10(kfv[:8]).std()) - 0.25) < 0.08
     inner = T[1:-1, 1:-1, 1:-1]
     assert float(inner.max()) <= 1.0 + 1e-3 and float(inner.min()) >= -1e-3
+
+
+def test_bench_command_line():
+    """bench.py parses its default and documented options without a GPU."""
+    import importlib.util
+    import os
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec = importlib.util.spec_from_file_location("bench_cli", os.path.join(root, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    argv = sys.argv
+    try:
+        sys.argv = ["bench.py"]
+        a = bench.parse()
+        assert (a.gpus, a.impl, a.n) == (1, "ours", 255) and a.warmup >= 3
+        sys.argv = ["bench.py", "--impl", "reference", "--steps", "2", "--warmup", "3", "--mixed-refresh", "1024",
+                    "--nu-steps", "0", "--post-n", "0", "--fault-steps", "20"]
+        a = bench.parse()
+        assert a.impl == "reference" and a.mixed_refresh == 1024 and a.fault_steps == 20
+        c = bench.workload_config(a)
+        assert c["cells"] == 255 ** 3 and c["mixed_refresh"] == 1024
+    finally:
+        sys.argv = argv
