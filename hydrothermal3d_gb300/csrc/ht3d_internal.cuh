@@ -132,10 +132,43 @@ static inline bool all_nonnull(P... p) {
         (ctx)->launches++;                                                     \
     } while (0)
 
+// Phase codes (-1 immersed, 0 crust, 1 air, 2 fault, 3 pluton) are small
+// integers stored as doubles.  Equality with a nonzero code is tested on the
+// bit pattern: the same truth value as the FP64 comparison for every input,
+// NaN included (a nonzero finite value has one representation), as an integer
+// compare instead of an instruction on the FP64 pipe.
+__device__ __forceinline__ bool ph_eq(double p, double code) {
+    return __double_as_longlong(p) == __double_as_longlong(code);
+}
+__device__ __forceinline__ bool ph_abs_eq(double p, double code) {  // fabs(p) == code, code > 0
+    return (__double_as_longlong(p) & 0x7fffffffffffffffLL) == __double_as_longlong(code);
+}
+
 static inline dim3 grid3(long long n1, long long n2, long long n3, dim3 b) {
     return dim3((unsigned)((n1 + b.x - 1) / b.x), (unsigned)((n2 + b.y - 1) / b.y), (unsigned)((n3 + b.z - 1) / b.z));
 }
 static const dim3 kBlock3(32, 8, 1);
+
+// Launch shape of the light per-cell kernels (a few loads and stores per
+// cell): each kBlock3 block covers kZPer consecutive k planes of its 32 x 8
+// tile, one (i, j) column per thread.  A 255^3 launch is then 8 k blocks
+// instead of 65 k; scheduling 65 k one-cell blocks alone took about 60 us.
+constexpr int kZPer = 8;
+static inline dim3 grid3z(long long n1, long long n2, long long n3) {
+    return dim3((unsigned)((n1 + 31) / 32), (unsigned)((n2 + 7) / 8), (unsigned)((n3 + kZPer - 1) / kZPer));
+}
+// Calls f(i, j, k) for this thread's cells of an n1 x n2 x n3 box (grid3z
+// launch with kBlock3 blocks); a `return` in f skips one cell.
+template <class F>
+__device__ __forceinline__ void for_cells_z(int n1, int n2, int n3, F&& f) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= n1 || j >= n2) return;
+    const int k0 = blockIdx.z * kZPer;
+#pragma unroll
+    for (int kk = 0; kk < kZPer; ++kk)
+        if (k0 + kk < n3) f(i, j, k0 + kk);
+}
 
 // Largest element count any array of an n^3 problem may have (n+6)^3 must fit
 // 32-bit index arithmetic.

@@ -54,7 +54,7 @@ __global__ void k_hydro_conductivity(double* kfv, const double* __restrict__ Tce
     if (mode == 1) out = rk_mu / sc_t;
     else if (mode == 2) out = (kF / law_muf(Tv)) / (sc_L * sc_L / sc_eta);
     else if (mode == 3) out = kF / (sc_L * sc_L);
-    if (phv[v] == 2.0) out *= k_fact;
+    if (ph_eq(phv[v], 2.0)) out *= k_fact;
     kfv[v] = out;
 }
 
@@ -69,7 +69,7 @@ __global__ void k_fluid_density(double* rfv, const double* __restrict__ Tce, con
     Pv *= sc_s;
     const int v = VXI(i, j, k);
     double r = law_rhof_C(Tv - 273.15, Pv) / sc_rho;
-    if (phv[v] == 1.0) r = 0.000 / sc_rho;
+    if (ph_eq(phv[v], 1.0)) r = 0.000 / sc_rho;
     rfv[v] = r;
 }
 
@@ -108,7 +108,7 @@ __global__ void k_rhoC_eff(double* rC, const double* __restrict__ T, const doubl
     if (i >= nx || j >= ny || k >= nz) return;
     const int e = EXI(i + 1, j + 1, k + 1);
     const double ph = phc[e];
-    if (fabs(ph) != 1.0) {
+    if (!ph_abs_eq(ph, 1.0)) {
         const double Tsca = T[e] * sT, Psca = P[e] * ss;
         const double r_eff = law_phi(ph, phii) * law_rhof_C(Tsca - 273.15, Psca) + (1.0 - law_phi(ph, phii)) * law_rhos(Tsca);
         const double Ceff = law_phi(ph, phii) * law_Cf(Tsca) + (1.0 - law_phi(ph, phii)) * law_Cs(Tsca);
@@ -126,9 +126,9 @@ __global__ void k_res_temperature(double* F, const double* __restrict__ T, const
     if (i >= nx || j >= ny || k >= nz) return;
     const int e = EXI(i + 1, j + 1, k + 1), c = CI(i, j, k);
     const double ph = phc[e];
-    if (fabs(ph) != 1.0) {
+    if (!ph_abs_eq(ph, 1.0)) {
         double Q = 0.;
-        if (ph == 3.0) Q = Qt;
+        if (ph_eq(ph, 3.0)) Q = Qt;
         double f = transient * rC[c] * _dt * (T[e] - T0[c]);
         f += (qx[ix3(i + 1, j, k, nx + 1, ny)] - qx[ix3(i, j, k, nx + 1, ny)]) * _dx;
         f += (qy[ix3(i, j + 1, k, nx, ny + 1)] - qy[ix3(i, j, k, nx, ny + 1)]) * _dy;
@@ -140,36 +140,59 @@ __global__ void k_res_temperature(double* F, const double* __restrict__ T, const
         F[c] = 0.;
     }
 }
-// SetTemperatureBCs! (:183-205) / SetPressureBCs! (:291-314), out of place:
-// S is the pre-launch snapshot, X the array written (snapshot semantics).
-template <int PRESSURE>
-__global__ void k_dim_bcs(double* X, const double* __restrict__ S, const double* __restrict__ ky,
-                          const double* __restrict__ wN, const double* __restrict__ ph, double qyS, double _dy,
-                          double VN, int nx, int ny, int nz) {
-    GIDX;
+// SetTemperatureBCs! (:183-205) / SetPressureBCs! (:291-314) in place, with
+// snapshot semantics (every rule reads cells as they were before the call;
+// a later rule of one cell overrides an earlier one) in two passes over the
+// phase array: MODE bit 1 clear evaluates the new value of each written cell
+// from X, which this pass does not modify, into B; MODE bit 1 set stores B
+// into X for the same cells.  MODE bit 0: pressure (1) or temperature (0).
+template <int MODE>
+__global__ void k_dim_bcs(double* X, double* B, const double* __restrict__ ky, const double* __restrict__ wN,
+                          const double* __restrict__ ph, double qyS, double _dy, double VN, int nx, int ny, int nz) {
+    constexpr int PRESSURE = MODE & 1, APPLY = MODE >> 1;
     const int n1 = nx + 2, n2 = ny + 2, n3 = nz + 2;
-    if (i >= n1 || j >= n2 || k >= n3) return;
-    const int e = EXI(i, j, k);
-    double v = S[e];
-    bool w = false;
-    const double p = ph[e];
-    if (p == 1.0) { v = VN; w = true; }
-    const int kmaxx = PRESSURE ? n3 - 2 : n3 - 1;  // x-rule z range differs between the two kernels
-    if (i == 0 && j >= 1 && j <= n2 - 2 && k >= 1 && k <= kmaxx) { v = S[EXI(1, j, k)]; w = true; }
-    if (i == n1 - 1 && j >= 1 && j <= n2 - 2 && k >= 1 && k <= kmaxx) { v = S[EXI(n1 - 2, j, k)]; w = true; }
-    if (j == 0 && i >= 1 && i <= n1 - 2 && k >= 1 && k <= n3 - 2) {
-        if (PRESSURE) v = S[EXI(i, 1, k)];
-        else v = qyS / _dy / ky[ix3(i - 1, 0, k - 1, nx, ny + 1)] + S[EXI(i, 1, k)];
-        w = true;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= n1 || j >= n2) return;
+    const int k0 = blockIdx.z * kZPer;  // grid3z launch: kZPer planes of one (i, j) column
+    double pv[kZPer];                   // the column's phase codes, loaded before any rule runs
+#pragma unroll
+    for (int kk = 0; kk < kZPer; ++kk) pv[kk] = k0 + kk < n3 ? ph[EXI(i, j, k0 + kk)] : 0.0;
+#pragma unroll
+    for (int kk = 0; kk < kZPer; ++kk) {
+        const int k = k0 + kk;
+        if (k >= n3) break;
+        const int e = EXI(i, j, k);
+        const double p = pv[kk];
+        const int kmaxx = PRESSURE ? n3 - 2 : n3 - 1;  // x-rule z range differs between the two kernels
+        const bool xl = i == 0 && j >= 1 && j <= n2 - 2 && k >= 1 && k <= kmaxx;
+        const bool xr = i == n1 - 1 && j >= 1 && j <= n2 - 2 && k >= 1 && k <= kmaxx;
+        const bool ys = j == 0 && i >= 1 && i <= n1 - 2 && k >= 1 && k <= n3 - 2;
+        const bool imm = ph_eq(p, -1.0) && j >= 1;
+        const bool zb = k == 0 && i >= 1 && i <= n1 - 2 && j >= 1 && j <= n2 - 2;
+        const bool zf = k == n3 - 1 && i >= 1 && i <= n1 - 2 && j >= 1 && j <= n2 - 2;
+        const bool air = ph_eq(p, 1.0);
+        if (!(air || xl || xr || ys || imm || zb || zf)) continue;
+        if (APPLY) {
+            X[e] = B[e];
+            continue;
+        }
+        double v = 0.0;
+        if (air) v = VN;
+        if (xl) v = X[EXI(1, j, k)];
+        if (xr) v = X[EXI(n1 - 2, j, k)];
+        if (ys) {
+            if (PRESSURE) v = X[EXI(i, 1, k)];
+            else v = qyS / _dy / ky[ix3(i - 1, 0, k - 1, nx, ny + 1)] + X[EXI(i, 1, k)];
+        }
+        if (imm) {
+            const double wn = wN[i + (nx + 2) * k];
+            v = (VN - (1.0 - wn) * X[EXI(i, j - 1, k)]) / wn;
+        }
+        if (zb) v = X[EXI(i, j, 1)];
+        if (zf) v = X[EXI(i, j, n3 - 2)];
+        B[e] = v;
     }
-    if (p == -1.0 && j >= 1) {
-        const double wn = wN[i + (nx + 2) * k];
-        v = (VN - (1.0 - wn) * S[EXI(i, j - 1, k)]) / wn;
-        w = true;
-    }
-    if (k == 0 && i >= 1 && i <= n1 - 2 && j >= 1 && j <= n2 - 2) { v = S[EXI(i, j, 1)]; w = true; }
-    if (k == n3 - 1 && i >= 1 && i <= n1 - 2 && j >= 1 && j <= n2 - 2) { v = S[EXI(i, j, n3 - 2)]; w = true; }
-    if (w) X[e] = v;
 }
 // ϕρf (:225-235), ϕρf_old (:237-247, cell inputs), ϕdρdP! (:249-259)
 __global__ void k_phi_rhof(double* out, const double* __restrict__ T, const double* __restrict__ P,
@@ -178,7 +201,7 @@ __global__ void k_phi_rhof(double* out, const double* __restrict__ T, const doub
     GIDX;
     if (i >= nx || j >= ny || k >= nz) return;
     const double ph = phc[EXI(i + 1, j + 1, k + 1)];
-    if (ph != 1.0) {
+    if (!ph_eq(ph, 1.0)) {
         const int s = cell_in ? CI(i, j, k) : EXI(i + 1, j + 1, k + 1);
         const double Tc = T[s] * sT - 273.15;
         const double Pc = P[s] * ss;
@@ -216,7 +239,7 @@ __global__ void k_res_pressure(double* F, const double* __restrict__ phc, const 
     if (i >= nx || j >= ny || k >= nz) return;
     const int c = CI(i, j, k);
     const double ph = phc[EXI(i + 1, j + 1, k + 1)];
-    if (fabs(ph) != 1.0) {
+    if (!ph_abs_eq(ph, 1.0)) {
         double f = transient * _dt * (prf[c] - prf0[c]);
         f += (qx[ix3(i + 1, j, k, nx + 1, ny)] - qx[ix3(i, j, k, nx + 1, ny)]) * _dx;
         f += (qy[ix3(i, j + 1, k, nx, ny + 1)] - qy[ix3(i, j, k, nx, ny + 1)]) * _dy;
@@ -352,14 +375,15 @@ static int dim_bcs(ht3d_ctx* ctx, int pressure, double* X, const double* ky, con
     DIMS;
     HT3D_REQUIRE(X && wN && phc && (pressure || ky), "null argument");
     const long long nex = (long long)(nx + 2) * (ny + 2) * (nz + 2);
-    double* snap = (double*)ht3d_scratch(ctx, SLOT_SNAP, sizeof(double) * nex);
-    HT3D_CUDA(cudaMemcpyAsync(snap, X, sizeof(double) * nex, cudaMemcpyDeviceToDevice, ctx->stream));
-    if (pressure)
-        HT3D_LAUNCH(ctx, k_dim_bcs<1>, G3(nx + 2, ny + 2, nz + 2), kBlock3, 0, X, snap, ky, wN, phc, qyS, _dy, VN, nx,
-                    ny, nz);
-    else
-        HT3D_LAUNCH(ctx, k_dim_bcs<0>, G3(nx + 2, ny + 2, nz + 2), kBlock3, 0, X, snap, ky, wN, phc, qyS, _dy, VN, nx,
-                    ny, nz);
+    double* B = (double*)ht3d_scratch(ctx, SLOT_SNAP, sizeof(double) * nex);
+    const dim3 g = grid3z(nx + 2, ny + 2, nz + 2);
+    if (pressure) {
+        HT3D_LAUNCH(ctx, k_dim_bcs<1>, g, kBlock3, 0, X, B, ky, wN, phc, qyS, _dy, VN, nx, ny, nz);
+        HT3D_LAUNCH(ctx, k_dim_bcs<3>, g, kBlock3, 0, X, B, ky, wN, phc, qyS, _dy, VN, nx, ny, nz);
+    } else {
+        HT3D_LAUNCH(ctx, k_dim_bcs<0>, g, kBlock3, 0, X, B, ky, wN, phc, qyS, _dy, VN, nx, ny, nz);
+        HT3D_LAUNCH(ctx, k_dim_bcs<2>, g, kBlock3, 0, X, B, ky, wN, phc, qyS, _dy, VN, nx, ny, nz);
+    }
     return HT3D_OK;
 }
 
@@ -626,7 +650,7 @@ __global__ void __launch_bounds__(CX_* CY_* CZ_) k_dim_iter(DimIterArgs A, DimSc
 
 __global__ void k_pluton(double* T, const double* __restrict__ phc, double Tp, long long n) {
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
-        if (phc[t] == 3.0) T[t] = Tp;
+        if (ph_eq(phc[t], 3.0)) T[t] = Tp;
 }
 __global__ void k_phase8(signed char* out, const double* __restrict__ phc, long long n) {
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
@@ -639,9 +663,7 @@ __global__ void k_av_xza(double* out, const double* __restrict__ rfv, int nx, in
         (rfv[VXI(i, j, k)] + rfv[VXI(i + 1, j, k)] + rfv[VXI(i, j, k + 1)] + rfv[VXI(i + 1, j, k + 1)]) * 0.25;
 }
 __global__ void k_inn_copy(double* A, const double* __restrict__ B, int nx, int ny, int nz) {
-    GIDX;
-    if (i >= nx || j >= ny || k >= nz) return;
-    A[CI(i, j, k)] = B[EXI(i + 1, j + 1, k + 1)];
+    for_cells_z(nx, ny, nz, [&](int i, int j, int k) { A[CI(i, j, k)] = B[EXI(i + 1, j + 1, k + 1)]; });
 }
 __global__ void k_gersh(double* G, double* D, const double* __restrict__ rC, const double* __restrict__ kx,
                         const double* __restrict__ ky, const double* __restrict__ kz, double transient, double dt,
@@ -750,8 +772,8 @@ extern "C" int ht3d_step_v18(ht3d_ctx* ctx, double* Tc_ex, double* Pc_ex, const 
         const unsigned g1 = (unsigned)std::max<long long>(1, std::min<long long>((nex + 255) / 256, ctx->num_sms * 16LL));
         if (p->it == 1) HT3D_LAUNCH(ctx, k_pluton, g1, 256, 0, Tc_ex, phc_ex, p->T_pluton, nex);
         HT3D_LAUNCH(ctx, k_phase8, g1, 256, 0, W.ph, phc_ex, nex);
-        HT3D_LAUNCH(ctx, k_inn_copy, gc, kBlock3, 0, W.T0, Tc_ex, nx, ny, nz);
-        HT3D_LAUNCH(ctx, k_inn_copy, gc, kBlock3, 0, W.P0, Pc_ex, nx, ny, nz);
+        HT3D_LAUNCH(ctx, k_inn_copy, grid3z(nx, ny, nz), kBlock3, 0, W.T0, Tc_ex, nx, ny, nz);
+        HT3D_LAUNCH(ctx, k_inn_copy, grid3z(nx, ny, nz), kBlock3, 0, W.P0, Pc_ex, nx, ny, nz);
         HT3D_CUDA(cudaMemsetAsync(W.rC, 0, sizeof(double) * n, ctx->stream));
         DimScal s{};
         s._dx = _dx; s._dy = _dy; s._dz = _dz; s._dt = _dt; s.transient = transient; s.Qt = p->Qt; s.g = p->g;

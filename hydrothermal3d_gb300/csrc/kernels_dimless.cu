@@ -113,11 +113,11 @@ __global__ void k_residual(double* F, double* T, const double* __restrict__ R, c
 template <int MODE>
 __global__ void k_update(double* F0, double* X, const double* __restrict__ F, double a, double b, double dtau, int nx,
                          int ny, int nz) {
-    GIDX;
-    if (i >= nx || j >= ny || k >= nz) return;
-    const double f0 = MODE == 0 ? CX(F, i, j, k) + a * CX(F0, i, j, k) : a * CX(F0, i, j, k) + b * CX(F, i, j, k);
-    CX(F0, i, j, k) = f0;
-    EX(X, i + 1, j + 1, k + 1) = EX(X, i + 1, j + 1, k + 1) - dtau * f0;
+    for_cells_z(nx, ny, nz, [&](int i, int j, int k) {
+        const double f0 = MODE == 0 ? CX(F, i, j, k) + a * CX(F0, i, j, k) : a * CX(F0, i, j, k) + b * CX(F, i, j, k);
+        CX(F0, i, j, k) = f0;
+        EX(X, i + 1, j + 1, k + 1) = EX(X, i + 1, j + 1, k + 1) - dtau * f0;
+    });
 }
 
 // Six-face ghost rules of the dimensionless BC kernels, with snapshot
@@ -125,7 +125,9 @@ __global__ void k_update(double* F0, double* X, const double* __restrict__ F, do
 // later rules of one ghost overwrite earlier ones).  The launch is split in
 // three phases so no thread reads a cell another thread of the same launch
 // writes: corners (read edge ghosts), then edges (read face ghosts), then
-// face ghosts (read inner cells).
+// face ghosts (read inner cells).  Each phase runs over the ghost shell only:
+// thread t walks the planes x-, x+, y-, y+, z-, z+ in turn, and a cell on
+// several planes (an edge or a corner) belongs to the first of them.
 struct FaceBC {
     int type[6];
     double val[6];
@@ -134,9 +136,32 @@ __device__ __forceinline__ double bc_rule(const FaceBC& bc, int f, double inner)
     return bc.type[f] == HT3D_BC_DIRICHLET ? 2.0 * bc.val[f] - inner : inner;
 }
 __global__ void k_face_bc(double* X, FaceBC bc, int phase, int nx, int ny, int nz) {
-    GIDX;
     const int n1 = nx + 2, n2 = ny + 2, n3 = nz + 2;
-    if (i >= n1 || j >= n2 || k >= n3) return;
+    const long long px = (long long)n2 * n3, py = (long long)n1 * n3, pz = (long long)n1 * n2;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int i, j, k;
+    if (t < 2 * px) {
+        i = t < px ? 0 : n1 - 1;
+        const long long r = t % px;
+        j = (int)(r % n2);
+        k = (int)(r / n2);
+    } else if (t < 2 * (px + py)) {
+        t -= 2 * px;
+        j = t < py ? 0 : n2 - 1;
+        const long long r = t % py;
+        i = (int)(r % n1);
+        k = (int)(r / n1);
+        if (i == 0 || i == n1 - 1) return;  // on an x plane
+    } else if (t < 2 * (px + py + pz)) {
+        t -= 2 * (px + py);
+        k = t < pz ? 0 : n3 - 1;
+        const long long r = t % pz;
+        i = (int)(r % n1);
+        j = (int)(r / n1);
+        if (i == 0 || i == n1 - 1 || j == 0 || j == n2 - 1) return;  // on an x or y plane
+    } else {
+        return;
+    }
     const int nb = (i == 0 || i == n1 - 1) + (j == 0 || j == n2 - 1) + (k == 0 || k == n3 - 1);
     if (nb == 0 || (3 - nb) != phase) return;  // phase 0: corners (nb=3), 1: edges, 2: faces
     double v = 0.0;
@@ -150,9 +175,13 @@ __global__ void k_face_bc(double* X, FaceBC bc, int phase, int nx, int ny, int n
     if (set) X[ix3(i, j, k, n1, n2)] = v;
 }
 
+// one thread per (i, k) column zeroes the south (j = 0) and north (j = ny) faces
 __global__ void k_kill_ns(double* Ty, int nx, int ny, int nz) {
-    GIDX;
-    if (i < nx && k < nz && (j == 0 || j == ny)) FY(Ty, i, j, k) = 0.0;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)nx * nz) return;
+    const int i = (int)(t % nx), k = (int)(t / nx);
+    FY(Ty, i, 0, k) = 0.0;
+    FY(Ty, i, ny, k) = 0.0;
 }
 
 __global__ void k_reset2(double* A, double* B, long long n) {
@@ -172,10 +201,10 @@ __global__ void k_mul(double* a, const double* __restrict__ b, const double* __r
 // dir 0: A(n^3) = inn(B), 1: inn(A) = B(n^3)
 template <int DIR>
 __global__ void k_cpy_inn(double* A, const double* __restrict__ B, int nx, int ny, int nz) {
-    GIDX;
-    if (i >= nx || j >= ny || k >= nz) return;
-    if (DIR == 0) CX(A, i, j, k) = EX(B, i + 1, j + 1, k + 1);
-    else EX(A, i + 1, j + 1, k + 1) = CX(B, i, j, k);
+    for_cells_z(nx, ny, nz, [&](int i, int j, int k) {
+        if (DIR == 0) CX(A, i, j, k) = EX(B, i + 1, j + 1, k + 1);
+        else EX(A, i + 1, j + 1, k + 1) = CX(B, i, j, k);
+    });
 }
 
 // GershgorinPoisson!  Dimensional/kernels_HT3D_dimensional.jl:207-221
@@ -201,10 +230,10 @@ __global__ void k_gershgorin(double* G, double* D, const double* __restrict__ rC
 
 __global__ void k_swap_dyrel(double* Xc, double* Yc, const double* __restrict__ X0, const double* __restrict__ Y0,
                              int nx, int ny, int nz) {
-    GIDX;
-    if (i >= nx || j >= ny || k >= nz) return;
-    CX(Xc, i, j, k) = EX(X0, i + 1, j + 1, k + 1);
-    CX(Yc, i, j, k) = CX(Y0, i, j, k);
+    for_cells_z(nx, ny, nz, [&](int i, int j, int k) {
+        CX(Xc, i, j, k) = EX(X0, i + 1, j + 1, k + 1);
+        CX(Yc, i, j, k) = CX(Y0, i, j, k);
+    });
 }
 
 template <int DEN>
@@ -229,8 +258,9 @@ void ht3d_launch_face_bc(ht3d_ctx* ctx, double* X, const int* type6, const doubl
         bc.type[f] = type6[f];
         bc.val[f] = val6[f];
     }
-    dim3 g = grid3(nx + 2, ny + 2, nz + 2, kBlock3);
-    for (int ph = 0; ph < 3; ++ph) HT3D_LAUNCH(ctx, k_face_bc, g, kBlock3, 0, X, bc, ph, nx, ny, nz);
+    const long long n1 = nx + 2, n2 = ny + 2, n3 = nz + 2, shell = 2 * (n2 * n3 + n1 * n3 + n1 * n2);
+    const unsigned blocks = (unsigned)((shell + 255) / 256);
+    for (int ph = 0; ph < 3; ++ph) HT3D_LAUNCH(ctx, k_face_bc, dim3(blocks), dim3(256), 0, X, bc, ph, nx, ny, nz);
 }
 
 extern "C" {
@@ -332,7 +362,7 @@ int ht3d_UpdateP(ht3d_ctx* ctx, double* F0, double* P, const double* F, double d
     return ht3d_guard(ctx, [&]() {
         HT3D_REQUIRE(all_nonnull(F0, P, F), "null argument");
         DIMS_OK(1);
-        HT3D_LAUNCH(ctx, k_update<0>, G3(nx, ny, nz), kBlock3, 0, F0, P, F, dampx, 0.0, dtau, nx, ny, nz);
+        HT3D_LAUNCH(ctx, k_update<0>, grid3z(nx, ny, nz), kBlock3, 0, F0, P, F, dampx, 0.0, dtau, nx, ny, nz);
         return HT3D_OK;
     });
 }
@@ -342,7 +372,7 @@ int ht3d_DYRELUpdate(ht3d_ctx* ctx, double* F0, double* X, const double* F, doub
     return ht3d_guard(ctx, [&]() {
         HT3D_REQUIRE(all_nonnull(F0, X, F), "null argument");
         DIMS_OK(1);
-        HT3D_LAUNCH(ctx, k_update<1>, G3(nx, ny, nz), kBlock3, 0, F0, X, F, h1, h2, dtau, nx, ny, nz);
+        HT3D_LAUNCH(ctx, k_update<1>, grid3z(nx, ny, nz), kBlock3, 0, F0, X, F, h1, h2, dtau, nx, ny, nz);
         return HT3D_OK;
     });
 }
@@ -366,7 +396,8 @@ int ht3d_KillNorthSouthFluxes(ht3d_ctx* ctx, double* Ty, int nx, int ny, int nz)
     return ht3d_guard(ctx, [&]() {
         HT3D_REQUIRE(all_nonnull(Ty), "null argument");
         DIMS_OK(1);
-        HT3D_LAUNCH(ctx, k_kill_ns, G3(nx, ny + 1, nz), kBlock3, 0, Ty, nx, ny, nz);
+        const long long cols = (long long)nx * nz;
+        HT3D_LAUNCH(ctx, k_kill_ns, dim3((unsigned)((cols + 255) / 256)), dim3(256), 0, Ty, nx, ny, nz);
         return HT3D_OK;
     });
 }
@@ -384,7 +415,7 @@ int ht3d_Cpy_inn_to_all(ht3d_ctx* ctx, double* A, const double* B_ex, int nx, in
     return ht3d_guard(ctx, [&]() {
         HT3D_REQUIRE(all_nonnull(A, B_ex), "null argument");
         DIMS_OK(1);
-        HT3D_LAUNCH(ctx, k_cpy_inn<0>, G3(nx, ny, nz), kBlock3, 0, A, B_ex, nx, ny, nz);
+        HT3D_LAUNCH(ctx, k_cpy_inn<0>, grid3z(nx, ny, nz), kBlock3, 0, A, B_ex, nx, ny, nz);
         return HT3D_OK;
     });
 }
@@ -393,7 +424,7 @@ int ht3d_Cpy_all_to_inn(ht3d_ctx* ctx, double* A_ex, const double* B, int nx, in
     return ht3d_guard(ctx, [&]() {
         HT3D_REQUIRE(all_nonnull(A_ex, B), "null argument");
         DIMS_OK(1);
-        HT3D_LAUNCH(ctx, k_cpy_inn<1>, G3(nx, ny, nz), kBlock3, 0, A_ex, B, nx, ny, nz);
+        HT3D_LAUNCH(ctx, k_cpy_inn<1>, grid3z(nx, ny, nz), kBlock3, 0, A_ex, B, nx, ny, nz);
         return HT3D_OK;
     });
 }
@@ -445,7 +476,7 @@ int ht3d_SwapDYREL(ht3d_ctx* ctx, double* Xc, double* Yc, const double* X0c_ex, 
     return ht3d_guard(ctx, [&]() {
         HT3D_REQUIRE(all_nonnull(Xc, Yc, X0c_ex, Y0c), "null argument");
         DIMS_OK(1);
-        HT3D_LAUNCH(ctx, k_swap_dyrel, G3(nx, ny, nz), kBlock3, 0, Xc, Yc, X0c_ex, Y0c, nx, ny, nz);
+        HT3D_LAUNCH(ctx, k_swap_dyrel, grid3z(nx, ny, nz), kBlock3, 0, Xc, Yc, X0c_ex, Y0c, nx, ny, nz);
         return HT3D_OK;
     });
 }

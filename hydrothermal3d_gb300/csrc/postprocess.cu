@@ -42,7 +42,7 @@ __global__ void k_post(PostOut o, PostIn a, ht3d_post_params p, const double* __
     const long long c = (long long)i + (long long)nx * ((long long)j + (long long)ny * k);
     const long long e = (long long)(i + 1) + (long long)(nx + 2) * ((long long)(j + 1) + (long long)(ny + 2) * (k + 1));
     const double ph = a.phc[e];
-    const bool air = ph == 1.0;
+    const bool air = ph_eq(ph, 1.0);
     const double nan = __longlong_as_double(0x7ff8000000000000LL);
     if (o.phase) o.phase[c] = air ? nan : ph;
     if (o.P) o.P[c] = air ? nan : a.Pc[e] * p.scale_sigma;
@@ -76,7 +76,7 @@ __global__ void k_post(PostOut o, PostIn a, ht3d_post_params p, const double* __
     }
     if (o.perm) {
         double v = kf_rows[j];
-        if (ph == 2.0) v *= p.k_fact;
+        if (ph_eq(ph, 2.0)) v *= p.k_fact;
         o.perm[c] = v;
     }
     // every read below is of an input that post_launch checked for the

@@ -152,15 +152,18 @@ __global__ void k_advect_v1(double* Fc, const double* __restrict__ Vxp, const do
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
         Fc[t] = Fc[t] - dt * (Vxp[t] * dm[t] + Vxm[t] * dp[t]);
 }
-__global__ void k_timeavg_v1(double* Fc, const double* __restrict__ Fold, double order, long long n) {
+// TimeAveraging!: Fc = (1/order) Fc + (1 - 1/order) Fold.  The two weights
+// a = 1/order and b = 1 - a are formed once on the host (IEEE division and
+// subtraction, the same bits as per cell) and passed in.
+__global__ void k_timeavg_v1(double* Fc, const double* __restrict__ Fold, double a, double b, long long n) {
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
-        Fc[t] = (1.0 / order) * Fc[t] + (1.0 - 1.0 / order) * Fold[t];
+        Fc[t] = a * Fc[t] + b * Fold[t];
 }
-__global__ void k_timeavg_v2(double* Fc, const double* __restrict__ Fold, double order, int nx, int ny, int nz) {
-    GIDX;
-    if (i >= nx || j >= ny || k >= nz) return;
-    const long long e = ix3(i + 1, j + 1, k + 1, nx + 2, ny + 2);
-    Fc[e] = (1.0 / order) * Fc[e] + (1.0 - 1.0 / order) * Fold[ix3(i, j, k, nx, ny)];
+__global__ void k_timeavg_v2(double* Fc, const double* __restrict__ Fold, double a, double b, int nx, int ny, int nz) {
+    for_cells_z(nx, ny, nz, [&](int i, int j, int k) {
+        const long long e = ix3(i + 1, j + 1, k + 1, nx + 2, ny + 2);
+        Fc[e] = a * Fc[e] + b * Fold[ix3(i, j, k, nx, ny)];
+    });
 }
 
 // Advect! v2 (tools/Weno5_Routines_v2.jl:55-212), reference arithmetic
@@ -308,7 +311,8 @@ int ht3d_TimeAveraging_v1(ht3d_ctx* ctx, double* Fc, const double* Fold, double 
     return ht3d_guard(ctx, [&]() {
         HT3D_REQUIRE(all_nonnull(Fc, Fold), "null argument");
         HT3D_REQUIRE(n >= 0, "negative size");
-        if (n) HT3D_LAUNCH(ctx, k_timeavg_v1, g1(ctx, n), 256, 0, Fc, Fold, order, n);
+        const double a = 1.0 / order, b = 1.0 - a;
+        if (n) HT3D_LAUNCH(ctx, k_timeavg_v1, g1(ctx, n), 256, 0, Fc, Fold, a, b, n);
         return HT3D_OK;
     });
 }
@@ -330,7 +334,8 @@ int ht3d_TimeAveraging_v2(ht3d_ctx* ctx, double* Fc_ex, const double* Fold, doub
     return ht3d_guard(ctx, [&]() {
         HT3D_REQUIRE(all_nonnull(Fc_ex, Fold), "null argument");
         ht3d_check_dims(nx, ny, nz, 1);
-        HT3D_LAUNCH(ctx, k_timeavg_v2, G3(nx, ny, nz), kBlock3, 0, Fc_ex, Fold, order, nx, ny, nz);
+        const double a = 1.0 / order, b = 1.0 - a;
+        HT3D_LAUNCH(ctx, k_timeavg_v2, grid3z(nx, ny, nz), kBlock3, 0, Fc_ex, Fold, a, b, nx, ny, nz);
         return HT3D_OK;
     });
 }

@@ -120,6 +120,34 @@ def test_boundary_kernels_snapshot_semantics(ctx, orc):
     np.testing.assert_array_equal(ht.to_numpy(Pd), Po)
 
 
+def test_boundary_kernels_read_cells_they_overwrite(ctx, orc):
+    """Rules that read a cell the same call overwrites (an air cell next to a
+    face ghost, an immersed cell above another immersed or air cell) must see
+    its value from before the call, as the oracle's explicit snapshot does."""
+    b = setup()
+    p = b["params"]
+    nx, ny, nz = (s - 2 for s in b["T"].shape)
+    phc = b["phc2"].copy(order="F")
+    phc[1, 3, 2] = phc[nx, 2, 3] = phc[2, 1, 3] = phc[3, 4, 1] = phc[4, 2, nz] = 1.0  # air read by x/y/z face rules
+    phc[4, 5, 4] = phc[4, 6, 4] = -1.0  # immersed above immersed
+    phc[5, 3, 5], phc[5, 4, 5] = 1.0, -1.0  # immersed above air
+    rng = np.random.default_rng(19)
+    ky = np.asfortranarray(rng.uniform(0.5, 2, (nx, ny + 1, nz)))
+    T = b["T"] + np.asfortranarray(rng.uniform(-0.01, 0.01, b["T"].shape))
+    To, Td = T.copy(order="F"), ht.from_numpy(T)
+    orc.call("SetTemperatureBCs_dim", To, ky, b["wN2"], phc, p.qyS, 1 / p.dy, p.Ttop, nx, ny, nz)
+    api.SetTemperatureBCs(ctx, Td, ht.from_numpy(ky), ht.from_numpy(b["wN2"]), ht.from_numpy(phc), p.qyS,
+                          1 / p.dy, 1.0, p.Tbot, p.Ttop)
+    np.testing.assert_array_equal(ht.to_numpy(Td), To)
+    P = b["P"] * (1 + np.asfortranarray(rng.uniform(-0.01, 0.01, b["P"].shape)))
+    Po, Pd = P.copy(order="F"), ht.from_numpy(P)
+    orc.call("SetPressureBCs_dim", Po, b["wN2"], phc, p.Ptop, nx, ny, nz)
+    api.SetPressureBCs_dim(ctx, Pd, ht.from_numpy(b["wN2"]), ht.from_numpy(phc), p.Pbot, p.Ptop)
+    np.testing.assert_array_equal(ht.to_numpy(Pd), Po)
+    # the x ghost (0, 3, 2) takes the pre-call value of the air cell (1, 3, 2), which the call resets to Ptop
+    assert Po[0, 3, 2] == P[1, 3, 2] and Po[1, 3, 2] == p.Ptop != P[1, 3, 2]
+
+
 def test_flux_and_residual_kernels(ctx, orc):
     b = setup()
     p = b["params"]

@@ -220,7 +220,7 @@ def test_weno_v1_pieces_and_copies(ctx, orc, n):
     api.Advect_v1(ctx, Fd, dev(Vp), dev(dm), dev(Vm), dev(dp), 0.013)
     assert rel_err(host(Fd), Fo) <= TOL
     Fold = rnd(rng, nx, ny, nz)
-    for order in (1.0, 2.0):
+    for order in (1.0, 2.0, 3.0):  # 1/3 is inexact: the weights the host forms must match per-cell ones
         Fo, Fd = F.copy(order="F"), dev(F)
         orc.call("TimeAveraging_v1", Fo, Fold, order, N)
         api.TimeAveraging_v1(ctx, Fd, dev(Fold), order)
