@@ -6,10 +6,11 @@
 //    in one appended raw block (UInt64 size headers).
 //  * ht3d_breakpoint_write / _read: the restart state of
 //    Dimensional/HydroThermal3D_v18.jl:384-395 and :579-588 (Tc_ex, Pc_ex,
-//    time, dt).  The reference stores it in HDF5, which this build has no
-//    library for; the library writes the same four items to a raw binary file
+//    time, dt).  The reference stores it in HDF5; with no HDF5 library to
+//    link, the library writes the same four items to a raw binary file
 //    (layout in include/ht3d.h) straight from device memory.
-// Host code only; both machines are little-endian, which the VTK header states.
+// Host code only; it writes little-endian data (x86-64 and AArch64 hosts),
+// which the VTK header states.
 #include <algorithm>
 #include <cstdio>
 #include <cstring>

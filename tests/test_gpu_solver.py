@@ -4,7 +4,7 @@ time step) against the oracle, FP64 and mixed precision.
 Tolerances (relative, max-norm over the compared cells):
   FP64 form  : <= 1e-12 (the plain form's contract; FMA contraction and one
                reciprocal differ from the oracle by rounding only)
-  mixed form : <= 1e-6 in T after a full step (BASELINE target), solver
+  mixed form : <= 1e-6 in T after a full step (its accuracy target), solver
                outputs within the DYREL tolerance.
 Edge and corner ghost cells are excluded (the reference writes them with a
 race; no consumer on the dimensionless path reads them)."""
