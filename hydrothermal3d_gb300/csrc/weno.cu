@@ -50,10 +50,10 @@ __global__ void __launch_bounds__(256) k_weno_stage(const double* __restrict__ s
         // x[o] holds X[I+o-3]
         const double m1 = h * (x[1] - x[0]), m2 = h * (x[2] - x[1]), m3 = h * (x[3] - x[2]), m4 = h * (x[4] - x[3]);
         const double m5 = QUIRK ? h * (x[5] - x[2]) : h * (x[5] - x[4]);
-        const double dFm = weno5_ref(m1, m2, m3, m4, m5);
+        const double dFm = upwind_active(Vp) ? weno5_ref(m1, m2, m3, m4, m5) : 0.0;
         const double p1 = h * (x[6] - x[5]), p2 = h * (x[5] - x[4]), p3 = h * (x[4] - x[3]), p4 = h * (x[3] - x[2]);
         const double p5 = h * (x[2] - x[1]);
-        const double dFp = weno5_ref(p1, p2, p3, p4, p5);
+        const double dFp = upwind_active(Vm) ? weno5_ref(p1, p2, p3, p4, p5) : 0.0;
         rhs = Vp * dFm + Vm * dFp;
     } else {
         const float hf = (float)h;
@@ -61,6 +61,9 @@ __global__ void __launch_bounds__(256) k_weno_stage(const double* __restrict__ s
 #pragma unroll
         for (int o = 0; o < 6; ++o) d[o] = hf * (float)(x[o + 1] - x[o]);  // d[o] = h*(X[I+o-2]-X[I+o-3])
         const float m5 = QUIRK ? hf * (float)(x[5] - x[2]) : d[4];
+        // both derivatives always: this form is bound by the FP64 conversions
+        // above, and skipping a zero-factor derivative made it slower (37.7 to
+        // 40.2 ms per 511^3 sweep)
         const float dFm = weno5_f32(d[0], d[1], d[2], d[3], m5);
         const float dFp = weno5_f32(d[5], d[4], d[3], d[2], d[1]);
         rhs = (double)((float)Vp * dFm + (float)Vm * dFp);
@@ -183,10 +186,12 @@ __global__ void k_advect_v2(double* Fc, const double* __restrict__ X, const doub
     if (a >= 0.0) Vm = 0.0;
     if (b < 0.0) Vp = 0.0;
     if (b >= 0.0) Vp = b;
-    const double dFm = weno5_ref(h * (x(-2) - x(-3)), h * (x(-1) - x(-2)), h * (x(0) - x(-1)), h * (x(1) - x(0)),
-                                 quirk ? h * (x(2) - x(-1)) : h * (x(2) - x(1)));
-    const double dFp = weno5_ref(h * (x(3) - x(2)), h * (x(2) - x(1)), h * (x(1) - x(0)), h * (x(0) - x(-1)),
-                                 h * (x(-1) - x(-2)));
+    const double dFm = upwind_active(Vp) ? weno5_ref(h * (x(-2) - x(-3)), h * (x(-1) - x(-2)), h * (x(0) - x(-1)),
+                                                     h * (x(1) - x(0)), quirk ? h * (x(2) - x(-1)) : h * (x(2) - x(1)))
+                                         : 0.0;
+    const double dFp = upwind_active(Vm) ? weno5_ref(h * (x(3) - x(2)), h * (x(2) - x(1)), h * (x(1) - x(0)),
+                                                     h * (x(0) - x(-1)), h * (x(-1) - x(-2)))
+                                         : 0.0;
     const long long e = ix3(i + 1, j + 1, k + 1, nx + 2, ny + 2);
     Fc[e] = Fc[e] - dt * (Vp * dFm + Vm * dFp);
 }

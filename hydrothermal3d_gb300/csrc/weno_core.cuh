@@ -51,6 +51,17 @@ __device__ __forceinline__ float weno5_f32(float v1, float v2, float v3, float v
     return __fdividef(w1 * p1 + w2 * p2 + w3 * p3, w1 + w2 + w3);
 }
 
+// Upwinding multiplies each one-sided WENO5 derivative by a velocity factor
+// that is exactly zero wherever the flow through that face has the other
+// sign.  A derivative whose factor is zero is skipped (taken as 0): the
+// product it would have added is a zero, so for finite fields the update
+// T - dt*(Vp*dFm + Vm*dFp) keeps its value (at most the sign of a zero
+// result differs), and where a warp's flow has one sign only one of the two
+// reconstructions is evaluated.  The test reads the bit pattern (x != 0 for
+// every input, NaN included), not an FP64 compare.
+__device__ __forceinline__ bool upwind_active(double v) { return (__double_as_longlong(v) << 1) != 0; }
+__device__ __forceinline__ bool upwind_active(float v) { return (__float_as_uint(v) << 1) != 0u; }
+
 struct WenoBC {
     int typeL, typeR;
     double valL, valR;

@@ -22,8 +22,8 @@ __device__ __forceinline__ float weno_point_f32(float x0, float x1, float x2, fl
     const float d0 = h * (x1 - x0), d1 = h * (x2 - x1), d2 = h * (x3 - x2), d3 = h * (x4 - x3), d4 = h * (x5 - x4),
                 d5 = h * (x6 - x5);
     const float m5 = QUIRK ? h * (x5 - x2) : d4;
-    const float dFm = weno5_f32(d0, d1, d2, d3, m5);
-    const float dFp = weno5_f32(d5, d4, d3, d2, d1);
+    const float dFm = upwind_active(Vp) ? weno5_f32(d0, d1, d2, d3, m5) : 0.0f;
+    const float dFp = upwind_active(Vm) ? weno5_f32(d5, d4, d3, d2, d1) : 0.0f;
     return x3 - dt * (Vp * dFm + Vm * dFp);
 }
 
