@@ -143,6 +143,15 @@ __device__ __forceinline__ bool ph_eq(double p, double code) {
 __device__ __forceinline__ bool ph_abs_eq(double p, double code) {  // fabs(p) == code, code > 0
     return (__double_as_longlong(p) & 0x7fffffffffffffffLL) == __double_as_longlong(code);
 }
+// The sign the FP64 comparisons x < 0.0 and x > 0.0 see: -1, +1, or 0 for
+// +-0 and NaN (both comparisons false), from the bit pattern with integer
+// operations instead of two compares on the FP64 pipe.
+__device__ __forceinline__ int cmp_sign(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned long long m = b & 0x7fffffffffffffffULL;
+    if (m == 0ULL || m > 0x7ff0000000000000ULL) return 0;
+    return (b >> 63) ? -1 : 1;
+}
 
 static inline dim3 grid3(long long n1, long long n2, long long n3, dim3 b) {
     return dim3((unsigned)((n1 + b.x - 1) / b.x), (unsigned)((n2 + b.y - 1) / b.y), (unsigned)((n3 + b.z - 1) / b.z));

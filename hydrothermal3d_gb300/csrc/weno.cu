@@ -79,17 +79,20 @@ __global__ void __launch_bounds__(256) k_weno_stage(const double* __restrict__ s
     const int j = blockIdx.y * blockDim.y + threadIdx.y; \
     const int k = blockIdx.z * blockDim.z + threadIdx.z
 
+// a zero (or NaN) face velocity leaves the output as it was, as in the reference
 __global__ void k_vplusminus(double* Vm, double* Vp, const double* __restrict__ V, int axis, int nx, int ny, int nz) {
-    GIDX;
-    if (i >= nx || j >= ny || k >= nz) return;
-    const int c = ix3(i, j, k, nx, ny);
-    const int v1 = axis == 0 ? ix3(i, j, k, nx + 1, ny) : (axis == 1 ? ix3(i, j, k, nx, ny + 1) : ix3(i, j, k, nx, ny));
-    const int v2 = axis == 0 ? v1 + 1 : (axis == 1 ? v1 + nx : v1 + nx * ny);
-    const double a = V[v1], b = V[v2];
-    if (a < 0.0) Vm[c] = a;
-    if (a > 0.0) Vm[c] = 0.0;
-    if (b < 0.0) Vp[c] = 0.0;
-    if (b > 0.0) Vp[c] = b;
+    for_cells_z(nx, ny, nz, [&](int i, int j, int k) {
+        const int c = ix3(i, j, k, nx, ny);
+        const int v1 =
+            axis == 0 ? ix3(i, j, k, nx + 1, ny) : (axis == 1 ? ix3(i, j, k, nx, ny + 1) : ix3(i, j, k, nx, ny));
+        const int v2 = axis == 0 ? v1 + 1 : (axis == 1 ? v1 + nx : v1 + nx * ny);
+        const double a = V[v1], b = V[v2];
+        const int sa = cmp_sign(a), sb = cmp_sign(b);
+        if (sa < 0) Vm[c] = a;
+        if (sa > 0) Vm[c] = 0.0;
+        if (sb < 0) Vp[c] = 0.0;
+        if (sb > 0) Vp[c] = b;
+    });
 }
 
 __global__ void k_dfdx(double* dF, const double* __restrict__ v1, const double* __restrict__ v2,
@@ -261,7 +264,7 @@ int ht3d_VPlusMinus(ht3d_ctx* ctx, double* Vm, double* Vp, const double* V, int 
         HT3D_REQUIRE(all_nonnull(Vm, Vp, V), "null argument");
         ht3d_check_dims(nx, ny, nz, 1);
         HT3D_REQUIRE(axis >= 0 && axis <= 2, "axis must be 0, 1 or 2");
-        HT3D_LAUNCH(ctx, k_vplusminus, G3(nx, ny, nz), kBlock3, 0, Vm, Vp, V, axis, nx, ny, nz);
+        HT3D_LAUNCH(ctx, k_vplusminus, grid3z(nx, ny, nz), kBlock3, 0, Vm, Vp, V, axis, nx, ny, nz);
         return HT3D_OK;
     });
 }

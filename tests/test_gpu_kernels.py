@@ -196,11 +196,18 @@ def test_weno_granular_v1_and_v2(ctx, orc, n):
         shape[axis] += 1
         V = rnd(rng, *shape)
         V.flat[::7] = 0.0
-        Vm, Vp = np.zeros((nx, ny, nz), order="F"), np.zeros((nx, ny, nz), order="F")
-        Vmd, Vpd = ht.zeros(nx, ny, nz), ht.zeros(nx, ny, nz)
+        # faces the comparisons V < 0 / V > 0 both reject (-0, NaN) or take (+-inf)
+        # leave / set the outputs; the outputs start at a sentinel so a skipped write shows
+        V.flat[3::11] = -0.0
+        V.flat[5::13] = np.nan
+        V.flat[2::17] = np.inf
+        V.flat[4::19] = -np.inf
+        Vm, Vp = np.full((nx, ny, nz), 7.0, order="F"), np.full((nx, ny, nz), 7.0, order="F")
+        Vmd, Vpd = dev(Vm), dev(Vp)
         orc.call("VPlusMinus", Vm, Vp, V, ctypes.c_int(axis), nx, ny, nz)
         api.VPlusMinus(ctx, Vmd, Vpd, dev(V), axis)
         assert np.array_equal(host(Vmd), Vm) and np.array_equal(host(Vpd), Vp)
+        V[~np.isfinite(V)] = 0.5  # the advection below wants finite velocities
         for quirk in (0, 1):
             To, Td = T.copy(order="F"), dev(T)
             orc.call("Advect_v2", To, X, V, ctypes.c_int(axis), 0.01, *h, ctypes.c_int(quirk), nx, ny, nz)
