@@ -1,14 +1,15 @@
 """Known-answer physics through the GPU solver and time step (cases in
 kat_cases.py): the y-column geotherm against the exact 1-D solve, and the
 Horton-Rogers-Lapwood onset growth factors, for the plain FP64 and the
-mixed form."""
+mixed form; the reference's crustal geotherm benchmark through the
+dimensional step."""
 import numpy as np
 import pytest
 
 import hydrothermal3d_gb300 as ht
 from hydrothermal3d_gb300 import api, abi
 from kat_cases import (GEO_N, GEO_BC, geotherm_case, geotherm_exact, geotherm_params, ONSET_N, ONSET_STEPS,
-                       onset_case, onset_factor)
+                       onset_case, onset_factor, GEO18_N, geotherm_v18_case, geotherm_v18_exact, geotherm_v18_ky)
 
 pytestmark = pytest.mark.gpu
 
@@ -54,3 +55,21 @@ def test_hrl_onset_growth_factor(ctx, orc, prec, Ra):
     ratios = a_gpu[1:] / a_gpu[:-1]
     G = onset_factor(Ra)
     assert np.all(np.abs(ratios - G) <= 5e-3 * G)
+
+
+def test_crustal_geotherm_benchmark_steady_state(ctx, orc):
+    """Dimensional/Benchmarks/Geotherm_1D_weights.jl through ht3d_step_v18
+    (it = 0, steady thermal solve): the profile marched down from the
+    surface with the basal flux through every rock face, to 1e-11."""
+    nx, ny, nz = GEO18_N
+    c = geotherm_v18_case()
+    ky = geotherm_v18_ky(orc, c)
+    T, P = ht.from_numpy(c["T"]), ht.from_numpy(c["P"])
+    V = [ht.zeros(nx + 1, ny, nz), ht.zeros(nx, ny + 1, nz), ht.zeros(nx, ny, nz + 1)]
+    gt, _ = api.step_v18(ctx, T, P, ht.from_numpy(c["phc"]), ht.from_numpy(c["phv"]), ht.from_numpy(c["wN"]), None,
+                         *V, c["params"])
+    assert gt.status == 0 and gt.converged
+    exact = geotherm_v18_exact(c, ky)
+    got = ht.to_numpy(T)[1:-1, 1:c["js"] + 2, 1:-1]
+    assert np.abs(got - exact).max() <= 1e-11 * np.abs(exact).max()
+

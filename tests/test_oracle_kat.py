@@ -178,3 +178,27 @@ def test_hrl_onset_growth_factor(orc):
         G = onset_factor(Ra)
         assert np.all(np.abs(ratios - G) <= 5e-3 * G), (Ra, ratios, G)
         assert (a[-1] < a[0]) if Ra < 4 * np.pi ** 2 else (a[-1] > a[0])
+
+
+def test_crustal_geotherm_benchmark_steady_state(orc):
+    """Dimensional/Benchmarks/Geotherm_1D_weights.jl: the dimensional step's
+    steady initialisation (it = 0) on the benchmark's column -- basal flux
+    qmoho, immersed surface cell with weight wN, air at Tsurf, conductivity
+    fixed from the initial 20 K/km profile -- equals the profile marched
+    down from the surface with the flux qmoho through every rock face."""
+    from kat_cases import GEO18_N, geotherm_v18_case, geotherm_v18_exact, geotherm_v18_ky
+    nx, ny, nz = GEO18_N
+    c = geotherm_v18_case()
+    assert 0.0 < c["wN_value"] < 1.0
+    ky = geotherm_v18_ky(orc, c)
+    assert np.ptp(ky, axis=(0, 2)).max() <= 1e-15 * ky.max()  # the smoothing keeps a linear k(T(y)) per column
+    T, P = c["T"].copy(order="F"), c["P"].copy(order="F")
+    V = [np.zeros(s, order="F") for s in ((nx + 1, ny, nz), (nx, ny + 1, nz), (nx, ny, nz + 1))]
+    s, st_t, _ = orc.step_v18(T, P, c["phc"], c["phv"], c["wN"], None, *V, c["params"])
+    assert s == 0 and st_t.converged
+    exact = geotherm_v18_exact(c, ky)
+    got = T[1:-1, 1:c["js"] + 2, 1:-1]
+    assert np.abs(got - exact).max() <= 1e-12 * np.abs(exact).max()
+    # the steady profile is not the initial one: the basal flux and the surface rule shaped it
+    T0 = c["T"][1:-1, 1:c["js"] + 2, 1:-1]
+    assert np.abs(exact - T0).max() >= 1e-3 * np.abs(exact).max()
