@@ -25,7 +25,7 @@ import numpy as np
 import torch
 
 import hydrothermal3d_gb300 as ht
-from hydrothermal3d_gb300 import api, abi, v18
+from hydrothermal3d_gb300 import api, v18
 
 
 def _numel(shape):
