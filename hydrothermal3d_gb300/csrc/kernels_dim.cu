@@ -475,7 +475,7 @@ int ht3d_Init_vel_dim(ht3d_ctx* ctx, double* Vx, double* Vy, double* Vz, const d
 int ht3d_material_law(ht3d_ctx* ctx, int which, const double* a, const double* b, double* out, long long n) {
     return ht3d_guard(ctx, [&]() {
         HT3D_REQUIRE(all_nonnull(a, out), "null argument");
-        HT3D_REQUIRE(which >= 0 && which <= 9 && a && out && n >= 0, "bad argument");
+        HT3D_REQUIRE(which >= 0 && which <= 11 && a && out && n >= 0, "bad argument");
         const unsigned g = (unsigned)std::max<long long>(1, std::min<long long>((n + 255) / 256, ctx->num_sms * 16LL));
         if (n) HT3D_LAUNCH(ctx, k_law_eval, g, 256, 0, out, a, b, which, n);
         return HT3D_OK;

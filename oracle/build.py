@@ -13,6 +13,8 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "ht3d_oracle.cpp")
+# the library's exponentials (shared so both sides evaluate the laws to the same bits)
+EXPO = os.path.join(os.path.dirname(HERE), "hydrothermal3d_gb300", "csrc", "expo.h")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libht3d_oracle.so")
 
@@ -21,7 +23,7 @@ CXXFLAGS = ["-O3", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-sha
 
 def build(force: bool = False) -> str:
     os.makedirs(OUT_DIR, exist_ok=True)
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(SRC), os.path.getmtime(EXPO)):
         return LIB
     cmd = ["g++", *CXXFLAGS, "-o", LIB + ".tmp", SRC]
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -39,6 +39,7 @@
 #include <vector>
 #include <algorithm>
 #include <omp.h>
+#include "../hydrothermal3d_gb300/csrc/expo.h"
 
 typedef long long i64;
 
@@ -495,8 +496,12 @@ static inline double drhodP_C(double T_C, double p) {
     return -7.372e-15 * T3 + 8.036e-21 * T2 * p + 7.485e-12 * T2 + 4.083e-26 * T_C * p2 - 3.586e-17 * T_C * p +
            4.547e-9 * T_C - 5.852e-32 * p3 + 4.353e-23 * p2 - 8.882e-15 * p + 7.424e-7;
 }
-static inline double mu_f(double T) { return 2.414e-5 * std::pow(10.0, 247.8 / (T - 140.)); }
-static inline double k_F(double y, double delta) { return 5e-16 * std::exp(y / delta); }
+// 10^x and e^x: the library's own exponentials (expo.h), so the oracle and the
+// device evaluate the laws to the same bits; expo.h is pinned against 40-digit
+// decimal arithmetic (below 1 ulp) by the CPU tests.  Julia evaluates
+// 10^x with pow and e^x with its own table method, both also below 1 ulp.
+static inline double mu_f(double T) { return 2.414e-5 * ht3d_exp10(247.8 / (T - 140.)); }
+static inline double k_F(double y, double delta) { return 5e-16 * ht3d_exp(y / delta); }
 static inline double phi_of(double phase, double phi0) { return phase == 2.0 ? 3 * phi0 : phi0; }
 
 double orc_law(int which, double a, double b) {
@@ -511,6 +516,8 @@ double orc_law(int which, double a, double b) {
         case 7: return mu_f(a);
         case 8: return k_F(a, b);
         case 9: return phi_of(a, b);
+        case 10: return ht3d_exp(a);
+        case 11: return ht3d_exp10(a);
     }
     return NAN;
 }

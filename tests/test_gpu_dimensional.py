@@ -1,8 +1,9 @@
 """GPU parity of the dimensional (v18) kernels and time step against the oracle.
 
-The material laws call pow/exp, whose last bit may differ between CUDA's and
-the host's math library; granular kernels are therefore compared at 1e-13
-(relative, max-norm), full solves at 1e-10."""
+The material laws' exponentials (10^x of the viscosity, e^x of the
+permeability) are the library's own (expo.h), compiled into the device code
+and into the oracle alike, so every kernel is compared bit for bit and a full
+time step to 1e-12 (relative, max-norm) with identical iteration counts."""
 import ctypes
 
 import numpy as np
@@ -13,7 +14,10 @@ from hydrothermal3d_gb300 import api, abi, v18
 from conftest import rel_err, no_edges_mask
 
 pytestmark = pytest.mark.gpu
-TOL = 1e-13
+
+
+def same(got, ref):
+    np.testing.assert_array_equal(got, ref)
 
 
 def setup(n=(9, 8, 7), seed=3):
@@ -36,15 +40,35 @@ def test_material_laws(ctx, orc):
     rng = np.random.default_rng(1)
     a = np.asfortranarray(rng.uniform(300, 900, (50, 1, 1)))
     b = np.asfortranarray(rng.uniform(1e5, 3e8, (50, 1, 1)))
-    for which in range(10):
+    for which in range(12):
         aa = a - 273.15 if which in (5, 6) else (np.asfortranarray(rng.uniform(-5, 0, a.shape)) if which == 8 else a)
         bb = b if which in (5, 6) else (np.full(a.shape, 3.0, order="F") if which == 8 else b)
         if which == 9:
             aa = np.asfortranarray(rng.integers(-1, 4, a.shape).astype(float))
             bb = np.full(a.shape, 0.01, order="F")
+        if which == 10:
+            aa = np.asfortranarray(rng.uniform(-740, 705, a.shape))
+        if which == 11:
+            aa = np.asfortranarray(rng.uniform(-320, 305, a.shape))
         got = ht.to_numpy(api.material_law(ctx, which, ht.from_numpy(aa), ht.from_numpy(bb)))
         ref = np.array([orc.law(which, x, y) for x, y in zip(aa.ravel(), bb.ravel())]).reshape(aa.shape)
-        assert rel_err(got, ref) <= TOL, which
+        same(got, ref)
+
+
+def test_exponentials_within_cuda_error_bounds(ctx):
+    """The library's e^x and 10^x against CUDA's exp and pow(10, x) (documented
+    at 1 and 2 ulp of the exact value): within 2 ulp of CUDA's, and equal to
+    CUDA's exp for most arguments (both are then correctly rounded)."""
+    import torch
+    rng = np.random.default_rng(2)
+    for which, lo, hi, fn in ((10, -700.0, 700.0, torch.exp), (11, -300.0, 300.0, lambda t: torch.pow(10.0, t))):
+        x = np.asfortranarray(rng.uniform(lo, hi, (4096, 1, 1)))
+        got = ht.to_numpy(api.material_law(ctx, which, ht.from_numpy(x)))
+        cuda = fn(ht.from_numpy(x)).cpu().numpy()
+        ulps = np.abs(got - cuda) / np.spacing(np.abs(cuda))
+        assert ulps.max() <= 2.0, (which, ulps.max())
+        if which == 10:
+            assert (ulps == 0).mean() > 0.9
 
 
 def test_property_kernels(ctx, orc):
@@ -56,7 +80,7 @@ def test_property_kernels(ctx, orc):
     kv, kvd = np.zeros((nx + 1, ny + 1, nz + 1), order="F"), ht.zeros(nx + 1, ny + 1, nz + 1)
     orc.call("ComputeThermalConductivity", kv, T, phv, p.phi_i, p.sc_kt, p.sc_T, nx, ny, nz)
     api.ComputeThermalConductivity(ctx, kvd, Td, phvd, p.phi_i, p.sc_kt, p.sc_T)
-    assert rel_err(ht.to_numpy(kvd), kv) <= TOL
+    same(ht.to_numpy(kvd), kv)
     import ctypes
     for mode in (1, 2, 3):
         for kmul in (None, b["kmul"]):
@@ -65,40 +89,40 @@ def test_property_kernels(ctx, orc):
             api.ComputeHydroConductivity(ctx, kvd, Td, Pd, phvd, p.ymin, p.dy, p.k_fact, 3000.0 / p.sc_L, p.sc_sigma,
                                          p.sc_T, p.sc_L, p.sc_t, p.sc_eta, mode,
                                          None if kmul is None else ht.from_numpy(kmul))
-            assert rel_err(ht.to_numpy(kvd), kv) <= TOL, mode
+            same(ht.to_numpy(kvd), kv)
     orc.call("ComputeFluidDensity", kv, T, P, phv, p.sc_sigma, p.sc_T, p.sc_rho, nx, ny, nz)
     api.ComputeFluidDensity(ctx, kvd, Td, Pd, phvd, p.sc_sigma, p.sc_T, p.sc_rho)
-    assert rel_err(ht.to_numpy(kvd), kv) <= TOL
+    same(ht.to_numpy(kvd), kv)
     c, cd = np.zeros((nx, ny, nz), order="F"), ht.zeros(nx, ny, nz)
     orc.call("SmoothConductivityV2C", c, kv, nx, ny, nz)
     api.SmoothConductivityV2C(ctx, cd, kvd)
-    assert rel_err(ht.to_numpy(cd), c) <= TOL
+    same(ht.to_numpy(cd), c)
     orc.call("SmoothConductivityC2V", kv, c, nx, ny, nz)
     api.SmoothConductivityC2V(ctx, kvd, cd)
-    assert rel_err(ht.to_numpy(kvd), kv) <= TOL
+    same(ht.to_numpy(kvd), kv)
     k = [np.zeros(s, order="F") for s in ((nx + 1, ny, nz), (nx, ny + 1, nz), (nx, ny, nz + 1))]
     kd = [ht.zeros(*a.shape) for a in k]
     orc.call("InitConductivity", *k, kv, nx, ny, nz)
     api.InitConductivity(ctx, *kd, kvd)
     for a, bb in zip(kd, k):
-        assert rel_err(ht.to_numpy(a), bb) <= TOL
+        same(ht.to_numpy(a), bb)
     rC, rCd = np.zeros((nx, ny, nz), order="F"), ht.zeros(nx, ny, nz)
     orc.call("ComputeRhoCeffective", rC, T, P, phc, p.phi_i, p.sc_T, p.sc_sigma, p.sc_C, p.sc_rho, nx, ny, nz)
     api.ComputeRhoCeffective(ctx, rCd, Td, Pd, phcd, p.phi_i, p.sc_T, p.sc_sigma, p.sc_C, p.sc_rho)
-    assert rel_err(ht.to_numpy(rCd), rC) <= TOL
+    same(ht.to_numpy(rCd), rC)
     Tc0 = np.asfortranarray(T[1:-1, 1:-1, 1:-1] * 0.995)
     Pc0 = np.asfortranarray(P[1:-1, 1:-1, 1:-1] * 1.003)
     o, od = np.zeros((nx, ny, nz), order="F"), ht.zeros(nx, ny, nz)
     orc.call("phi_rhof", o, Tc0, Pc0, phc, p.phi_i, p.sc_rho, p.sc_T, p.sc_sigma, ctypes.c_int(1), ctypes.c_int(0),
              nx, ny, nz)
     api.PhiRhofOld(ctx, od, ht.from_numpy(Tc0), ht.from_numpy(Pc0), phcd, p.phi_i, p.sc_rho, p.sc_T, p.sc_sigma)
-    assert rel_err(ht.to_numpy(od), o) <= TOL, "PhiRhofOld"
+    same(ht.to_numpy(od), o)
     for name, args, cell in (("PhiRhof", (T, P), 0), ("PhiDrhodP", (T, P), 0)):
         o, od = np.zeros((nx, ny, nz), order="F"), ht.zeros(nx, ny, nz)
         orc.call("phi_rhof", o, *args, phc, p.phi_i, p.sc_rho, p.sc_T, p.sc_sigma, ctypes.c_int(cell),
                  ctypes.c_int(1 if name == "PhiDrhodP" else 0), nx, ny, nz)
         getattr(api, name)(ctx, od, Td, Pd, phcd, p.phi_i, p.sc_rho, p.sc_T, p.sc_sigma)
-        assert rel_err(ht.to_numpy(od), o) <= TOL, name
+        same(ht.to_numpy(od), o)
 
 
 def test_boundary_kernels_snapshot_semantics(ctx, orc):
@@ -162,28 +186,32 @@ def test_flux_and_residual_kernels(ctx, orc):
     orc.call("ComputeDarcyFlux", *q, rfv, *k, b["P"], p.g, *h, nx, ny, nz)
     api.ComputeDarcyFlux(ctx, *qd, ht.from_numpy(rfv), *kd, ht.from_numpy(b["P"]), p.g, *h)
     for a, bb in zip(qd, q):
-        assert rel_err(ht.to_numpy(a), bb) <= TOL
+        same(ht.to_numpy(a), bb)
     F, Fd = np.zeros((nx, ny, nz), order="F"), ht.zeros(nx, ny, nz)
     prf, prf0, PC = (np.asfortranarray(rng.uniform(0.5, 1.5, (nx, ny, nz))) for _ in range(3))
     orc.call("ResidualFluidPressure", F, b["phc2"], prf, prf0, PC, *q, 1.0, 3.0, *h, nx, ny, nz)
     api.ResidualFluidPressure(ctx, Fd, ht.from_numpy(b["phc2"]), ht.from_numpy(prf), ht.from_numpy(prf0),
                               ht.from_numpy(PC), *qd, 1.0, 3.0, *h)
-    assert rel_err(ht.to_numpy(Fd), F) <= TOL
+    same(ht.to_numpy(Fd), F)
     T0 = np.asfortranarray(b["T"][1:-1, 1:-1, 1:-1] * 0.99)
     orc.call("ResidualTemperatureLinearised", F, b["T"], T0, prf, b["phc2"], PC, *q, 0.5, 1.0, 3.0, *h, nx, ny, nz)
     api.ResidualTemperatureLinearised(ctx, Fd, ht.from_numpy(b["T"]), ht.from_numpy(T0), ht.from_numpy(prf),
                                       ht.from_numpy(b["phc2"]), ht.from_numpy(PC), *qd, 0.5, 1.0, 3.0, *h)
-    assert rel_err(ht.to_numpy(Fd), F) <= TOL
+    same(ht.to_numpy(Fd), F)
     V = [np.zeros(a.shape, order="F") for a in k]
     Vd = [ht.zeros(*a.shape) for a in k]
     orc.call("Init_vel_dim", *V, *q, rfv, nx, ny, nz)
     api.Init_vel_dim(ctx, *Vd, *qd, ht.from_numpy(rfv))
     for a, bb in zip(Vd, V):
-        assert rel_err(ht.to_numpy(a), bb) <= TOL
+        same(ht.to_numpy(a), bb)
 
 
 @pytest.mark.parametrize("n", [(8, 9, 6), (24, 20, 12)])
 def test_step_v18_matches_oracle(ctx, orc, n):
+    """Three dimensional time steps (the steady initialisation, then transient
+    steps with pluton insertion and WENO5-v2 sub-steps): the same thermal and
+    Darcy iteration counts as the oracle, T, P and the Darcy velocities V
+    within 1e-12 relative max-norm."""
     b = setup(n)
     nx, ny, nz = n
     V = [np.zeros(s, order="F") for s in ((nx + 1, ny, nz), (nx, ny + 1, nz), (nx, ny, nz + 1))]
@@ -193,16 +221,19 @@ def test_step_v18_matches_oracle(ctx, orc, n):
     phc, phv, wN, kmul = b["phc"], b["phv"], b["wN"], b["kmul"]
     args_d = (ht.from_numpy(phc), ht.from_numpy(phv), ht.from_numpy(wN), ht.from_numpy(kmul))
     p_o, p_d = b["params"], v18.box(*n, seed=3, nitout=50, tol=1e-9)["params"]
+    inner = (slice(1, -1),) * 3
     for it in range(3):
         p_o.it = p_d.it = it
         s, st_t, st_p = orc.step_v18(T, P, phc, phv, wN, kmul, *V, p_o)
         assert s == 0
         gt, gp = api.step_v18(ctx, Td, Pd, *args_d, *Vd, p_d)
         assert gt.status == 0 and gp.status == 0
-        assert abs(gt.iters - st_t.iters) <= p_o.thermal_dyrel.nitout and abs(gp.iters - st_p.iters) <= p_o.darcy_dyrel.nitout
-        assert p_d.n_adv == p_o.n_adv
-        assert rel_err(ht.to_numpy(Td)[1:-1, 1:-1, 1:-1], T[1:-1, 1:-1, 1:-1]) <= 1e-10
-        assert rel_err(ht.to_numpy(Pd)[1:-1, 1:-1, 1:-1], P[1:-1, 1:-1, 1:-1]) <= 1e-10
+        assert (gt.iters, gp.iters) == (st_t.iters, st_p.iters), it
+        assert p_d.n_adv == p_o.n_adv and p_d.dt == p_o.dt
+        assert rel_err(ht.to_numpy(Td)[inner], T[inner]) <= 1e-12
+        assert rel_err(ht.to_numpy(Pd)[inner], P[inner]) <= 1e-12
+        for vd, v in zip(Vd, V):
+            assert rel_err(ht.to_numpy(vd), v) <= 1e-12
 
 
 @pytest.mark.parametrize("grid", [(250, 106, 3), (47, 31, 9)])

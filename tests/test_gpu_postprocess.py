@@ -2,31 +2,22 @@
 and the Nusselt number (Dimensionless/HydroThermal3D_Alban_v6.jl:345-348)
 against the oracle.
 
-Fields built from products, sums and sqrt are bit-identical; permeability and
-viscosity call exp/pow, whose last bit may differ between CUDA's and the
-host's math library, and are compared at 1e-13 (relative, max-norm) with
-identical NaN positions.  Air cells must hold NaN, or keep their previous
-value where the reference leaves them untouched."""
+Every field is bit-identical, permeability and viscosity included: their
+exponentials are the library's own (expo.h), compiled into the device code
+and the oracle alike.  Air cells must hold NaN, or keep their previous value
+where the reference leaves them untouched."""
 import numpy as np
 import pytest
 
 import hydrothermal3d_gb300 as ht
 from hydrothermal3d_gb300 import api, abi
-from conftest import rel_err
 from post_case import PARAMS, SENTINEL, case, oracle_fields
 
 pytestmark = pytest.mark.gpu
-LIBM = {"permeability", "viscosity"}
 
 
 def _same(name, got, ref):
-    if name in LIBM:
-        assert np.array_equal(np.isnan(got), np.isnan(ref)), name
-        m = ~np.isnan(ref)
-        if m.any():  # a grid of air cells holds only NaN
-            assert rel_err(got[m], ref[m]) <= 1e-13, name
-    else:
-        assert np.array_equal(got, ref, equal_nan=True), name
+    assert np.array_equal(got, ref, equal_nan=True), name
 
 
 def _dev(c):
