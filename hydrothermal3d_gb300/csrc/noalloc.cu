@@ -14,6 +14,7 @@
 // Compiled with -fmad=false like the plain FP64 solver: the result is
 // identical to ht3d_dyrel_iterate's.
 #include <mutex>
+#include <utility>
 
 #include "dyrel_common.cuh"
 
@@ -28,7 +29,9 @@ __device__ __align__(256) double g_noalloc_scratch[kNoallocMaxEx];
 
 // Device address of g_noalloc_scratch per device.  The symbol's name in host
 // code is only a host-side stand-in, so the address is queried once per
-// device with that device current.
+// device with that device current.  cudaDeviceReset unloads the module, and
+// the array may come back elsewhere: the cached address is then stale, so a
+// process that resets a device must not call this entry point on it again.
 double* g_scratch_ptr[kMaxDevices] = {};
 std::mutex g_setup_mutex;
 
@@ -50,6 +53,20 @@ int scratch_for_current_device(double** out) {
     return HT3D_OK;
 }
 
+// Launches through cudaLaunchKernel, whose return value is this launch's own
+// status: an error left on the thread by someone else's earlier launch is
+// neither reported as this call's nor cleared.
+template <typename... P>
+cudaError_t launch_exact(void (*kern)(P...), dim3 g, dim3 b, cudaStream_t st, P... args) {
+    void* ptrs[] = {(void*)&args...};
+    return cudaLaunchKernel((const void*)kern, g, b, ptrs, 0, st);
+}
+template <typename... P, typename... A>
+cudaError_t launch(void (*kern)(P...), dim3 g, dim3 b, cudaStream_t st, A... args) {
+    static_assert(sizeof...(P) == sizeof...(A), "argument count");
+    return launch_exact<P...>(kern, g, b, st, static_cast<P>(args)...);
+}
+
 }  // namespace
 
 extern "C" int ht3d_dyrel_iterate_noalloc(double* X_ex, const double* R, const double* kx, const double* ky,
@@ -66,6 +83,7 @@ extern "C" int ht3d_dyrel_iterate_noalloc(double* X_ex, const double* R, const d
         bc.dir[f] = bc_type6[f];
         bc.val2[f] = 2.0 * bc_val6[f];
     }
+    if (n_iter == 0) return HT3D_OK;  // nothing to do, nothing touched
     double* scratch = nullptr;
     const int s = scratch_for_current_device(&scratch);
     if (s != HT3D_OK) return s;
@@ -75,13 +93,14 @@ extern "C" int ht3d_dyrel_iterate_noalloc(double* X_ex, const double* R, const d
     double* cur = X_ex;
     double* nxt = scratch;
     for (int it = 0; it < n_iter; ++it) {
-        k_dyrel_cell<double, MODE_PLAIN><<<grd, blk, 0, st>>>(cur, nxt, R, kx, ky, kz, PC, F0, nullptr, sc, bc, nx, ny,
-                                                              nz, nullptr);
+        const cudaError_t e = launch(k_dyrel_cell<double, MODE_PLAIN>, grd, blk, st, cur, nxt, R, kx, ky, kz, PC, F0,
+                                     (double*)nullptr, sc, bc, nx, ny, nz, (double*)nullptr);
+        if (e != cudaSuccess) return HT3D_ERR_CUDA;
         std::swap(cur, nxt);
     }
     if (cur != X_ex) {
         const dim3 b(32, 8, 1), g((nx + 2 + 31) / 32, (ny + 2 + 7) / 8, nz + 2);
-        k_copy_ex_faces<double><<<g, b, 0, st>>>(X_ex, cur, nx, ny, nz);
+        if (launch(k_copy_ex_faces<double>, g, b, st, X_ex, cur, nx, ny, nz) != cudaSuccess) return HT3D_ERR_CUDA;
     }
-    return cudaGetLastError() == cudaSuccess ? HT3D_OK : HT3D_ERR_CUDA;
+    return HT3D_OK;
 }

@@ -322,7 +322,9 @@ int ht3d_Init_vel_dim(ht3d_ctx* ctx, double* Vx, double* Vy, double* Vz, const d
                       const double* qz, const double* rhofv, int nx, int ny, int nz);
 /* material laws (Dimensional/HydroThermal3D_v18.jl:29-39) evaluated elementwise:
    which 0 kTs(T), 1 kTf(T), 2 Cf(T), 3 Cs(T), 4 ρs(T), 5 ρf_C(T_C,p), 6 dρdP_C(T_C,p),
-   7 μf(T), 8 kF(y,δ), 9 ϕ(phase,ϕ0); b may be NULL for one-argument laws */
+   7 μf(T), 8 kF(y,δ), 9 ϕ(phase,ϕ0), 10 e^a and 11 10^a (the exponentials μf and kF use:
+   one implementation, below 1 ulp, whose bits are the same on every machine);
+   b may be NULL for one-argument laws */
 int ht3d_material_law(ht3d_ctx* ctx, int which, const double* a, const double* b, double* out, long long n);
 
 /* ------------------------------------------------------------------ */
@@ -421,7 +423,13 @@ int ht3d_dyrel_iterate_f32(ht3d_ctx* ctx, float* X_ex, const float* R, const flo
      (nx+2)(ny+2)(nz+2) > 1048576 are rejected with HT3D_ERR_SCRATCH.
    - Never calls cudaMalloc, cudaFree or any allocating routine.
    - The first call on a device looks up the array's device address with that
-     device current; make that first call before any stream capture.
+     device current; make that first call before any stream capture.  The
+     address is kept for the life of the process: after cudaDeviceReset on a
+     device, do not call this entry point on that device again.
+   - n_iter == 0 checks the arguments and returns HT3D_OK without touching
+     the device.
+   - A launch that fails returns HT3D_ERR_CUDA; errors left on the thread by
+     other launches are neither reported nor cleared.
    - Asynchronous: returns after queueing its kernels on `stream`.
    - All calls share the one array, whose contents persist between calls
      (nothing is read before it is written); calls that overlap on the GPU,
@@ -597,6 +605,26 @@ int ht3d_breakpoint_write(ht3d_ctx* ctx, const char* path, const double* Tc_ex, 
                           double dt, int nx, int ny, int nz);
 int ht3d_breakpoint_read(ht3d_ctx* ctx, const char* path, double* Tc_ex, double* Pc_ex, double* time, double* dt,
                          int nx, int ny, int nz);
+
+/* The same restart state in the reference's own file format: the HDF5 file
+   Breakpoint%05d.h5 that v18.jl:579-588 writes with HDF5.jl (datasets Tc_ex and
+   Pc_ex, float64, dataspace dimensions (nz+2, ny+2, nx+2) -- the Julia array
+   (nx+2, ny+2, nz+2) as HDF5.jl stores it -- and the float64 scalars time and
+   dt), so each side can restart from the other's files.  Written and read
+   without an HDF5 library, from the public file-format specification:
+   superblock version 0, a symbol-table root group, version-1 object headers,
+   contiguous storage.  Reading accepts superblock versions 0-1, version-1
+   object headers and contiguous or compact datasets; other HDF5 layouts give
+   HT3D_ERR_IO, a grid other than nx, ny, nz HT3D_ERR_ARG. */
+int ht3d_breakpoint_write_h5(ht3d_ctx* ctx, const char* path, const double* Tc_ex, const double* Pc_ex, double time,
+                             double dt, int nx, int ny, int nz);
+int ht3d_breakpoint_read_h5(ht3d_ctx* ctx, const char* path, double* Tc_ex, double* Pc_ex, double* time, double* dt,
+                            int nx, int ny, int nz);
+/* Host-only forms of the two above (HOST arrays, no context or GPU). */
+int ht3d_h5_breakpoint_image(const char* path, const double* Tc_ex, const double* Pc_ex, double time, double dt,
+                             int nx, int ny, int nz);
+int ht3d_h5_breakpoint_parse(const char* path, double* Tc_ex, double* Pc_ex, double* time, double* dt, int nx, int ny,
+                             int nz);
 
 #ifdef __cplusplus
 }

@@ -53,3 +53,31 @@ def test_null_ctx_is_rejected_without_gpu(lib):
     assert lib.ht3d_ctx_destroy(None) == abi.ERR_ARG
     assert lib.ht3d_ctx_launch_count(None) == 0
     assert lib.ht3d_ComputeFlux(None, *([None] * 7), 1.0, 1.0, 1.0, 4, 4, 4) == abi.ERR_ARG
+
+
+def _noalloc_args(ptr, bc_type, n_iter=3, n=(4, 4, 4)):
+    """Arguments of ht3d_dyrel_iterate_noalloc with every array at `ptr` (never
+    dereferenced: each case is refused, or does nothing, before a launch)."""
+    return (ptr,) * 7 + (1.0, 0.25, 0.25, 0.25, abi.int6(*bc_type), abi.dbl6(0, 0, 1, 0, 0, 0), 0.9, 0.1, 0.01,
+                         n_iter, *n, None)
+
+
+def test_noalloc_rejects_bad_arguments_without_launching(lib):
+    """Refusals of the allocation-free iteration happen on the host, before
+    any CUDA call: null arrays, a BC type other than Neumann (0) or Dirichlet
+    (1), a negative iteration count, empty grids, grids beyond the static
+    scratch.  n_iter == 0 checks its arguments and touches nothing."""
+    fake = ctypes.c_void_p(0x1000)  # stands in for a device array
+    good = (0, 0, 1, 1, 0, 0)
+    fn = lib.ht3d_dyrel_iterate_noalloc
+    args = list(_noalloc_args(fake, good))
+    for i in range(7):
+        bad = list(args)
+        bad[i] = None
+        assert fn(*bad) == abi.ERR_ARG, i
+    assert fn(*_noalloc_args(fake, (0, 0, 2, 1, 0, 0))) == abi.ERR_ARG
+    assert fn(*_noalloc_args(fake, (0, 0, 1, 1, 0, -1))) == abi.ERR_ARG
+    assert fn(*_noalloc_args(fake, good, n_iter=-1)) == abi.ERR_ARG
+    assert fn(*_noalloc_args(fake, good, n=(0, 4, 4))) == abi.ERR_ARG
+    assert fn(*_noalloc_args(fake, good, n=(100, 100, 100))) == abi.ERR_SCRATCH
+    assert fn(*_noalloc_args(fake, good, n_iter=0)) == abi.OK
