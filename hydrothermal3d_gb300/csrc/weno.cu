@@ -16,7 +16,8 @@ namespace {
 // One SSP-RK2 stage along AXIS on ghosted (ex) fields.
 //   PREC 0: FP64 reference-order arithmetic (parity form; this translation
 //           unit is compiled with -fmad=false)
-//   PREC 1: FP32 stencil arithmetic, FP64 state (mixed form)
+//   PREC 1: mixed form: FP64 state, differences, central candidate and
+//           corrections; FP32 smoothness indicators and weights (weno5_mixed)
 //   STAGE 1: dst = src - dt*(Vp*dFm + Vm*dFp)
 //   STAGE 2: dst = 0.5*(src - dt*(...)) + 0.5*T0   (TimeAveraging!, order 2)
 template <int AXIS, int QUIRK, int STAGE, int PREC>
@@ -56,17 +57,23 @@ __global__ void __launch_bounds__(256) k_weno_stage(const double* __restrict__ s
         const double dFp = upwind_active(Vm) ? weno5_ref(p1, p2, p3, p4, p5) : 0.0;
         rhs = Vp * dFm + Vm * dFp;
     } else {
+        // FP64 differences e[o] = X[I+o-2] - X[I+o-3]; FP32 copies scaled by h
+        // for the smoothness indicators (weno5_mixed)
+        double e[6];
+        float f[6];
         const float hf = (float)h;
-        float d[6];
 #pragma unroll
-        for (int o = 0; o < 6; ++o) d[o] = hf * (float)(x[o + 1] - x[o]);  // d[o] = h*(X[I+o-2]-X[I+o-3])
-        const float m5 = QUIRK ? hf * (float)(x[5] - x[2]) : d[4];
-        // both derivatives always: this form is bound by the FP64 conversions
-        // above, and skipping a zero-factor derivative made it slower (37.7 to
-        // 40.2 ms per 511^3 sweep)
-        const float dFm = weno5_f32(d[0], d[1], d[2], d[3], m5);
-        const float dFp = weno5_f32(d[5], d[4], d[3], d[2], d[1]);
-        rhs = (double)((float)Vp * dFm + (float)Vm * dFp);
+        for (int o = 0; o < 6; ++o) {
+            e[o] = x[o + 1] - x[o];
+            f[o] = hf * (float)e[o];
+        }
+        const double e5 = QUIRK ? x[5] - x[2] : e[4];
+        const float f5 = QUIRK ? hf * (float)e5 : f[4];
+        const double dFm = upwind_active(Vp) ? h * weno5_mixed(e[0], e[1], e[2], e[3], e5, f[0], f[1], f[2], f[3], f5)
+                                             : 0.0;
+        const double dFp = upwind_active(Vm) ? h * weno5_mixed(e[5], e[4], e[3], e[2], e[1], f[5], f[4], f[3], f[2], f[1])
+                                             : 0.0;
+        rhs = Vp * dFm + Vm * dFp;
     }
     const double t = x[3] - dt * rhs;
     if (STAGE == 1) dst[e] = t;

@@ -51,6 +51,33 @@ __device__ __forceinline__ float weno5_f32(float v1, float v2, float v3, float v
     return __fdividef(w1 * p1 + w2 * p2 + w3 * p3, w1 + w2 + w3);
 }
 
+// Mixed-precision form: the weighted sum of the three candidate stencils is
+// rewritten as the central candidate plus weighted corrections,
+//   w1 p1 + w2 p2 + w3 p3 = p2 + (w1 (p1 - p2) + w3 (p3 - p2)) / (w1 + w2 + w3),
+// with p2 and the corrections (third differences) evaluated in FP64 from the
+// FP64 differences v, and only the smoothness indicators and weights in FP32
+// (from f, the same differences scaled and rounded to FP32).  A weight error
+// then multiplies a correction, which is small wherever the field is smooth,
+// instead of the derivative itself: FP32 weights cost ~1e-7 of the
+// corrections, not ~1e-7 of the derivative.  v are unscaled differences; the
+// caller multiplies the result by the grid factor h (f carry h already).
+__device__ __forceinline__ double weno5_mixed(double v1, double v2, double v3, double v4, double v5, float f1,
+                                              float f2, float f3, float f4, float f5) {
+    const double p2 = __fma_rn(2.0, v4, __fma_rn(5.0, v3, -v2)) * (1.0 / 6.0);
+    const float c1 = (float)(__fma_rn(3.0, v3 - v2, v1 - v4) * (1.0 / 3.0));  // p1 - p2
+    const float c3 = (float)(__fma_rn(3.0, v4 - v3, v2 - v5) * (1.0 / 6.0));  // p3 - p2
+    const float maxV = fmaxf(fmaxf(fmaxf(fmaxf(f1 * f1, f2 * f2), f3 * f3), f4 * f4), f5 * f5);
+    const float e = 1e-18f + 1e-6f * maxV;
+    const float a1 = f1 - 2.0f * f2 + f3, b1 = f1 - 4.0f * f2 + 3.0f * f3;
+    const float a2 = f2 - 2.0f * f3 + f4, b2 = f2 - f4;
+    const float a3 = f3 - 2.0f * f4 + f5, b3 = 3.0f * f3 - 4.0f * f4 + f5;
+    const float s1 = (13.0f / 12.0f) * (a1 * a1) + 0.25f * (b1 * b1) + e;
+    const float s2 = (13.0f / 12.0f) * (a2 * a2) + 0.25f * (b2 * b2) + e;
+    const float s3 = (13.0f / 12.0f) * (a3 * a3) + 0.25f * (b3 * b3) + e;
+    const float w1 = __fdividef(0.1f, s1 * s1), w2 = __fdividef(0.6f, s2 * s2), w3 = __fdividef(0.3f, s3 * s3);
+    return p2 + (double)__fdividef(w1 * c1 + w3 * c3, w1 + w2 + w3);
+}
+
 // Upwinding multiplies each one-sided WENO5 derivative by a velocity factor
 // that is exactly zero wherever the flow through that face has the other
 // sign.  A derivative whose factor is zero is skipped (taken as 0): the
