@@ -2,8 +2,10 @@
 time step) against the oracle, FP64 and mixed precision.
 
 Tolerances (relative, max-norm over the compared cells):
-  FP64 form  : <= 1e-12 (the plain form's contract; FMA contraction and one
-               reciprocal differ from the oracle by rounding only)
+  FP64 form  : <= 1e-12 (the plain form's contract); the fused solver and the
+               HRL time step round like the oracle (no FMA contraction, the
+               reference's statement order, canonical tree sums) and are
+               compared bit for bit where that holds
   mixed form : <= 1e-6 in T after a full step (its accuracy target), solver
                outputs within the DYREL tolerance.
 Edge and corner ghost cells are excluded (the reference writes them with a
@@ -146,31 +148,48 @@ def test_fused_weno_fp64_and_mixed(ctx, orc, n, variant):
         np.testing.assert_array_equal(got[0], T[0])  # ghosts untouched
 
 
-@pytest.mark.parametrize("n", [(16, 16, 16), (33, 31, 29)])
-def test_step_hrl_fp64_matches_oracle(ctx, orc, n):
+def _vel_err(Vd, V):
+    """Max-norm difference of the three face velocities relative to max|V|."""
+    scale = max(np.abs(v).max() for v in V)
+    return max(np.max(np.abs(ht.to_numpy(a) - b)) for a, b in zip(Vd, V)) / scale
+
+
+def _hrl_fp64_vs_oracle(ctx, orc, n, steps, nitout):
     nx, ny, nz = n
     T, P, ktv, kfv = hrl.initial_fields(nx, ny, nz, seed=1)
-    p_o = hrl.params(nx, ny, nz, nitout=100)
-    p_d = hrl.params(nx, ny, nz, nitout=100)
+    p_o = hrl.params(nx, ny, nz, nitout=nitout)
+    p_d = hrl.params(nx, ny, nz, nitout=nitout)
     V = [np.zeros(s, order="F") for s in ((nx + 1, ny, nz), (nx, ny + 1, nz), (nx, ny, nz + 1))]
     Td, Pd = ht.from_numpy(T), ht.from_numpy(P)
     Vd = [ht.zeros(*v.shape) for v in V]
     ktd, kfd = ht.from_numpy(ktv), ht.from_numpy(kfv)
     m = no_edges_mask(T.shape)
-    for step in range(3):
+    inner = (slice(1, -1),) * 3
+    for step in range(steps):
         s, st_t, st_d = orc.step_hrl(T, P, ktv, kfv, *V, p_o)
         assert s == 0
         gt, gd = api.step_hrl(ctx, Td, Pd, ktd, kfd, *Vd, p_d, abi.FP64)
-        assert gt.iters == st_t.iters and gd.iters == st_d.iters
-        assert rel_err(ht.to_numpy(Td), T, m) <= 1e-12
-        Pn, Pg = P[1:-1, 1:-1, 1:-1], ht.to_numpy(Pd)[1:-1, 1:-1, 1:-1]
-        assert rel_err(Pg - Pg.mean(), Pn - Pn.mean()) <= 1e-10
-        # V = -k (grad P - Ra T e_y) is a small difference of O(Ra) terms while
-        # the flow is near hydrostatic: measure it against the term scale
-        vscale = p_o.Ra * np.abs(T).max()
-        for a, b in zip(Vd, V):
-            assert np.max(np.abs(ht.to_numpy(a) - b)) <= 1e-12 * vscale
-        assert abs(p_d.dt - p_o.dt) <= 1e-9 * p_o.dt
+        assert (gt.iters, gd.iters) == (st_t.iters, st_d.iters), step
+        np.testing.assert_array_equal(ht.to_numpy(Td)[m], T[m])
+        Pn, Pg = P[inner], ht.to_numpy(Pd)[inner]
+        np.testing.assert_array_equal(Pg, Pn)
+        assert rel_err(Pg - Pg.mean(), Pn - Pn.mean()) <= 1e-12
+        assert _vel_err(Vd, V) <= 1e-12, step
+        assert abs(p_d.dt - p_o.dt) <= 1e-12 * p_o.dt
+
+
+@pytest.mark.parametrize("n", [(16, 16, 16), (33, 31, 29)])
+def test_step_hrl_fp64_matches_oracle(ctx, orc, n):
+    """Three HRL time steps: same iteration counts, T and P bit for bit, the
+    Darcy velocities within 1e-12 of max|V|, the same adapted dt."""
+    _hrl_fp64_vs_oracle(ctx, orc, n, 3, 100)
+
+
+def test_hrl_63_ten_steps_match_oracle(ctx, orc):
+    """The 63^3 workload as stated (Ra 1000, tolerance 1e-8, nitout 1000, WENO5
+    v1, adaptive dt, 10 time steps) against the oracle on the host: T and P
+    bit for bit after every step."""
+    _hrl_fp64_vs_oracle(ctx, orc, (63, 63, 63), 10, 1000)
 
 
 def test_step_hrl_mixed_error_vs_oracle(ctx, orc):
