@@ -63,6 +63,14 @@ def parse():
                     help="time steps of the 127^3 dimensional (v18) box, plain FP64 (0 = skip)")
     ap.add_argument("--fault-steps", type=int, default=0,
                     help="time steps of the 511^3 fault-slab HRL case (mixed form; 0 = skip)")
+    ap.add_argument("--c3-steps", type=int, default=0,
+                    help="time steps of the 255^3 mixed-vs-FP64 accuracy study (100 as the workload states it; "
+                         "0 = skip)")
+    ap.add_argument("--c3-n", type=int, default=255, help="cells per axis of the accuracy study")
+    ap.add_argument("--c3-cadence-control", type=int, default=500,
+                    help="check cadence of the accuracy study's second FP64 control (0 = no such control)")
+    ap.add_argument("--c3-out", default="",
+                    help="also write the accuracy study's record (one JSON object) to this file")
     return ap.parse_args()
 
 
@@ -389,6 +397,8 @@ def run_ours(a):
         out["diagnostics"] = post_bench(ctx, stream, a.post_n)
     if a.nu_steps and rank == 0:
         out["nusselt_63"] = nusselt_bench(ctx, stream, a.nu_steps)
+    if a.c3_steps and rank == 0:
+        out["accuracy_255"] = accuracy_bench(ctx, stream, a.c3_steps, a.c3_n, a.c3_cadence_control, a.c3_out)
 
     if rank == 0:
         v, cores, desc, _ = cpu_sample(n, a.cpu_seconds, threads=os.cpu_count())
@@ -652,6 +662,99 @@ def growth_bench(ctx, stream, steps, n=127, eps=1e-8):
     out["note"] = ("a 1e-8 perturbation of the FP64 run grows like the mixed form's difference: the accumulated "
                    "difference measures the convective instability of the workload, the per-step error the form")
     return out
+
+
+def accuracy_bench(ctx, stream, steps, n=255, cadence=500, out_path="", eps=1e-8):
+    """The mixed form's error against the FP64 form over `steps` HRL time steps
+    at n^3 (Ra 1000, tolerance 1e-8, seed-1 initial condition), every run
+    forced onto the FP64 run's dt sequence.  Per step, the max-norm relative
+    difference of T, P (mean removed) and the Darcy velocities Vx, Vy, Vz
+    against the FP64 run, for:
+      local      one mixed step taken from the FP64 state of the step before
+                 (the error the mixed form adds in one step);
+      mixed      the mixed run from the initial condition (accumulated);
+      perturbed  an FP64 run from the initial condition perturbed by
+                 eps * U(-1, 1) relative (seed 9);
+      cadence    an FP64 run that tests convergence every `cadence`
+                 pseudo-iterations instead of 1000: another FP64 answer that
+                 meets the same tolerance.
+    The two FP64 controls measure how far the workload itself carries a
+    difference of the size the solver tolerance leaves."""
+    import torch
+    import hydrothermal3d_gb300 as ht
+    from hydrothermal3d_gb300 import api, abi, hrl
+    T0, P0, ktv, kfv = hrl.initial_fields(n, n, n, seed=1)
+    Tp = T0.copy(order="F")
+    Tp[1:-1, 1:-1, 1:-1] *= 1.0 + eps * np.random.default_rng(9).uniform(-1, 1, (n, n, n))
+    ktd, kfd = ht.from_numpy(ktv), ht.from_numpy(kfv)
+
+    def vel():
+        return [ht.zeros(n + 1, n, n), ht.zeros(n, n + 1, n), ht.zeros(n, n, n + 1)]
+
+    runs = {"fp64": (T0, abi.FP64, 1000), "mixed": (T0, abi.MIXED, 1000), "perturbed": (Tp, abi.FP64, 1000)}
+    if cadence:
+        runs["cadence"] = (T0, abi.FP64, cadence)
+    state = {k: [ht.from_numpy(t), ht.from_numpy(P0)] + vel() for k, (t, _, _) in runs.items()}
+    local = [ht.zeros(n + 2, n + 2, n + 2), ht.zeros(n + 2, n + 2, n + 2)] + vel()
+    inner = (slice(1, -1),) * 3
+    names = ("T", "P", "Vx", "Vy", "Vz")
+
+    def errors(s, r):
+        e = {}
+        for nm, x, y in zip(names, s, r):
+            if nm == "T":
+                x, y = x[inner], y[inner]
+            elif nm == "P":
+                x, y = x[inner] - x[inner].mean(), y[inner] - y[inner].mean()
+            e[nm] = float((x - y).abs().max() / y.abs().max())
+        return e
+
+    rec = {"n": n, "steps": steps, "tolerance": 1e-8, "perturbation": eps, "cadence_control_nitout": cadence,
+           "per_step": []}
+    p = hrl.params(n, n, n)
+    t_start = time.perf_counter()
+    with torch.cuda.stream(stream):
+        torch.cuda.synchronize()
+        for k in range(steps):
+            dt = p.dt
+            for dst, src in zip(local, state["fp64"]):
+                dst.copy_(src)
+            f = state["fp64"]
+            gt, gd = api.step_hrl(ctx, f[0], f[1], ktd, kfd, *f[2:], p, abi.FP64)
+            row = {"step": k + 1, "dt": dt, "iters_fp64": [gt.iters, gd.iters]}
+            q = hrl.params(n, n, n)
+            q.dt = dt
+            lt, ld = api.step_hrl(ctx, local[0], local[1], ktd, kfd, *local[2:], q, abi.MIXED)
+            row["iters_local"] = [lt.iters, ld.iters]
+            for key in runs:
+                if key == "fp64":
+                    continue
+                q = hrl.params(n, n, n, nitout=runs[key][2])
+                q.dt = dt
+                s = state[key]
+                st, sd = api.step_hrl(ctx, s[0], s[1], ktd, kfd, *s[2:], q, runs[key][1])
+                row["iters_" + key] = [st.iters, sd.iters]
+            torch.cuda.synchronize()
+            ref = state["fp64"]
+            row["local"] = errors(local, ref)
+            for key in runs:
+                if key != "fp64":
+                    row[key] = errors(state[key], ref)
+            T = ref[0][inner]
+            row["T_range"] = [float(T.min()), float(T.max())]
+            row["max_abs_V"] = max(float(v.abs().max()) for v in ref[2:])
+            rec["per_step"].append(row)
+            print(json.dumps({"accuracy_step": row}), file=sys.stderr, flush=True)
+    rec["seconds"] = time.perf_counter() - t_start
+    ps = rec["per_step"]
+    rec["max_local"] = {nm: max(r["local"][nm] for r in ps) for nm in names}
+    for key in runs:
+        if key != "fp64":
+            rec["final_" + key] = ps[-1][key]
+    if out_path:
+        with open(out_path, "w") as f:
+            json.dump(rec, f)
+    return rec
 
 
 def v18_bench(ctx, stream, steps, n=127):
