@@ -699,17 +699,25 @@ def write_vtr(path, xc, yc, zc, fields):
     return p if p.endswith(".vtr") else p + ".vtr"
 
 
+def _h5(path):
+    return str(path).endswith(".h5")
+
+
 def breakpoint_write(ctx, path, Tc_ex, Pc_ex, time, dt):
-    """Restart state Tc_ex, Pc_ex, time, dt to a file (v18.jl:579-588)."""
+    """Restart state Tc_ex, Pc_ex, time, dt to a file (v18.jl:579-588): the
+    reference's HDF5 format when the path ends in .h5 (ht3d_breakpoint_write_h5),
+    else the library's raw format (ht3d_breakpoint_write)."""
     nx, ny, nz = _cells_ex(Tc_ex, "Tc_ex"); S = _shapes(nx, ny, nz)
-    ctx.call("ht3d_breakpoint_write", str(path).encode(), _ptr(Tc_ex, S["ex"], "Tc_ex"), _ptr(Pc_ex, S["ex"], "Pc_ex"),
-             float(time), float(dt), nx, ny, nz)
+    ctx.call("ht3d_breakpoint_write_h5" if _h5(path) else "ht3d_breakpoint_write", str(path).encode(),
+             _ptr(Tc_ex, S["ex"], "Tc_ex"), _ptr(Pc_ex, S["ex"], "Pc_ex"), float(time), float(dt), nx, ny, nz)
 
 
 def breakpoint_read(ctx, path, Tc_ex, Pc_ex):
-    """Fill Tc_ex, Pc_ex from a restart file (v18.jl:384-395); returns (time, dt)."""
+    """Fill Tc_ex, Pc_ex from a restart file (v18.jl:384-395), HDF5 when the
+    path ends in .h5, else raw; returns (time, dt)."""
     nx, ny, nz = _cells_ex(Tc_ex, "Tc_ex"); S = _shapes(nx, ny, nz)
     t, d = ctypes.c_double(), ctypes.c_double()
-    ctx.call("ht3d_breakpoint_read", str(path).encode(), _ptr(Tc_ex, S["ex"], "Tc_ex"), _ptr(Pc_ex, S["ex"], "Pc_ex"),
-             ctypes.byref(t), ctypes.byref(d), nx, ny, nz)
+    ctx.call("ht3d_breakpoint_read_h5" if _h5(path) else "ht3d_breakpoint_read", str(path).encode(),
+             _ptr(Tc_ex, S["ex"], "Tc_ex"), _ptr(Pc_ex, S["ex"], "Pc_ex"), ctypes.byref(t), ctypes.byref(d), nx, ny,
+             nz)
     return t.value, d.value

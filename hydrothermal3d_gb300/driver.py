@@ -10,8 +10,9 @@ ht3d_step_hrl, with the driver-side pieces of the reference's loops:
   the values the reference prints per check (Dimensional/HydroThermal3D_v18.jl:
   440-441, 463, 575-577) and the Nu/time series Alban writes (:500-505);
 * restart files every nout steps and restart from one
-  (Dimensional/HydroThermal3D_v18.jl:384-395, 579-588), through
-  ht3d_breakpoint_write/read.
+  (Dimensional/HydroThermal3D_v18.jl:384-395, 579-588): Breakpoint%05d.h5 in
+  the reference's HDF5 layout (ht3d_breakpoint_write_h5/read_h5), or the
+  library's raw format (fmt="bin").
 
 The state (T, P) is never modified outside ht3d_step_hrl: Nu is computed on a
 copy, so a run with the driver is bit-identical to a bare loop of steps."""
@@ -53,12 +54,12 @@ class NusseltProbe:
         return api.Nusselt(self.ctx, self.qy, nx * p.dx, nz * p.dz)
 
 
-def breakpoint_path(out_dir, it):
-    return os.path.join(out_dir, f"Breakpoint{it:05d}.bin")
+def breakpoint_path(out_dir, it, fmt="h5"):
+    return os.path.join(out_dir, f"Breakpoint{it:05d}.{fmt}")
 
 
 def run_hrl(ctx, T, P, ktv, kfv, V, params, steps, precision=abi.MIXED, log=None, nout=0, out_dir=None,
-            restart_from=0, time=0.0):
+            restart_from=0, time=0.0, fmt="h5"):
     """Steps it = restart_from + 1 .. restart_from + steps of the HRL model in
     place on the device fields T, P (ghosted) and V = (Vx, Vy, Vz).  log: a
     path (JSON lines appended) or None.  nout > 0 writes a restart file every
@@ -66,7 +67,7 @@ def run_hrl(ctx, T, P, ktv, kfv, V, params, steps, precision=abi.MIXED, log=None
     (T, P, time and dt).  Returns the list of per-step records."""
     nx, ny, nz = (int(s) - 2 for s in T.shape)
     if restart_from > 0:
-        time, params.dt = api.breakpoint_read(ctx, breakpoint_path(out_dir, restart_from), T, P)
+        time, params.dt = api.breakpoint_read(ctx, breakpoint_path(out_dir, restart_from, fmt), T, P)
     probe = NusseltProbe(ctx, nx, ny, nz)
     records = []
     fh = open(log, "a") if log else None
@@ -85,7 +86,7 @@ def run_hrl(ctx, T, P, ktv, kfv, V, params, steps, precision=abi.MIXED, log=None
                 fh.write(json.dumps(rec) + "\n")
                 fh.flush()
             if nout > 0 and it % nout == 0:
-                api.breakpoint_write(ctx, breakpoint_path(out_dir, it), T, P, time, params.dt)
+                api.breakpoint_write(ctx, breakpoint_path(out_dir, it, fmt), T, P, time, params.dt)
     finally:
         if fh:
             fh.close()

@@ -30,7 +30,7 @@ def test_log_breakpoints_and_restart(ctx, tmp_path):
         assert r["thermal"]["status"] == 0 and r["darcy"]["status"] == 0 and r["thermal"]["iters"] > 0
         assert abs(r["Nu"] - 1.0) < 0.05  # near-conductive start of the HRL run
         assert 0.0 <= r["T_min"] <= r["T_max"] <= 1.0 + 1e-3
-    assert (tmp_path / "Breakpoint00002.bin").exists() and (tmp_path / "Breakpoint00004.bin").exists()
+    assert (tmp_path / "Breakpoint00002.h5").exists() and (tmp_path / "Breakpoint00004.h5").exists()
     # restart from step 2: steps 3 and 4 again, identical to the first run
     T2, P2, _, _, V2 = fields()
     q = hrl.params(N, N, N, dt_max=2e-3)
