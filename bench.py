@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--skip-ensemble", action="store_true")
     ap.add_argument("--mixed-refresh", type=int, default=0,
                     help="FP64 refresh cadence of the mixed form in inner iterations (0 = library default)")
+    ap.add_argument("--temporal", type=int, default=-1,
+                    help="two inner iterations per pass of the mixed form (HT3D_TUNE_TEMPORAL; -1 = library default)")
     ap.add_argument("--nu-steps", type=int, default=60,
                     help="time steps of the 63^3 Nusselt time series, FP64 vs mixed (0 = skip)")
     ap.add_argument("--post-n", type=int, default=255, help="cells per axis of the output-diagnostics pass (0 = skip)")
@@ -61,6 +63,12 @@ def parse():
                          "against FP64; 0 = skip)")
     ap.add_argument("--v18-steps", type=int, default=2,
                     help="time steps of the 127^3 dimensional (v18) box, plain FP64 (0 = skip)")
+    ap.add_argument("--v18-nitmax", type=int, default=100000,
+                    help="DYREL iteration cap of the dimensional box (the reference's 1e4 stops the 127^3 Darcy "
+                         "solves before the 1e-10 tolerance)")
+    ap.add_argument("--c127-steps", type=int, default=0,
+                    help="first time steps of the 127^3 dimensional box on the oracle (host cores) against the "
+                         "GPU FP64 form: T, P, V errors (0 = skip; minutes of host time per step)")
     ap.add_argument("--fault-steps", type=int, default=0,
                     help="time steps of the 511^3 fault-slab HRL case (mixed form; 0 = skip)")
     ap.add_argument("--c3-steps", type=int, default=0,
@@ -81,6 +89,8 @@ def workload_config(a, extra=None):
          "parallelism": f"replicas x{a.gpus}"}
     if getattr(a, "mixed_refresh", 0):
         c["mixed_refresh"] = a.mixed_refresh
+    if getattr(a, "temporal", -1) >= 0:
+        c["temporal"] = a.temporal
     if extra:
         c.update(extra)
     return c
@@ -201,7 +211,8 @@ def cpu_sample(n, seconds, threads=None):
     nbytes = iters * hrl.bytes_per_iteration(n, n, n, 8) + adv * hrl.bytes_per_advection(n, n, n, 8)
     desc = (f"oracle FP64 at {n}^3: {iters} DYREL pseudo-iterations (thermal+Darcy, incl. per-solve Gershgorin set-up)"
             f" + {adv} WENO5 advections in {t_tot:.1f} s")
-    return nbytes / t_tot / 1e9, cores, desc, t_tot
+    cell_updates = iters * n ** 3 / t_tot  # pseudo-iteration cell updates per second (advection time included)
+    return nbytes / t_tot / 1e9, cores, desc, t_tot, cell_updates
 
 
 def oracle_c63(steps, threads=None):
@@ -275,17 +286,24 @@ def run_reference(a):
         return
     cores = os.cpu_count()
     vals = []
+    cups = []
     for s in range(a.warmup + a.steps):
-        v, cores, desc, _ = cpu_sample(a.n, max(2.0, a.cpu_seconds / 4), threads=os.cpu_count())
+        v, cores, desc, _, cu = cpu_sample(a.n, max(2.0, a.cpu_seconds / 4), threads=os.cpu_count())
         if s >= a.warmup:
             vals.append(v)
+            cups.append(cu)
     value = float(np.mean(vals))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
             "warmup": a.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded HRL initial condition)",
             "config": workload_config(a, {"reference_impl": "CPU oracle port (reference is Julia; not runnable here)"}),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc},
-            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "cell_updates_per_s": float(np.mean(cups)),
+            "work_note": ("T_eff counts 8 B per field value here and 4 B in the mixed GPU form; cell_updates_per_s "
+                          "(DYREL pseudo-iterations x cells per second, advection time included) compares the arms "
+                          "at equal work. Each step is a bounded sample of the workload, not a full time step: one "
+                          "255^3 FP64 time step takes minutes on the host cores")}
     if a.c63_steps:
         line["config_63"] = oracle_c63(a.c63_steps, threads=os.cpu_count())[0]
     print(json.dumps(line))
@@ -304,6 +322,8 @@ def run_ours(a):
     ctx = ht.Context(device=dev, stream=stream.cuda_stream)
     if a.mixed_refresh:
         ctx.set_tuning(abi.TUNE_MIXED_REFRESH, a.mixed_refresh)
+    if a.temporal >= 0:
+        ctx.set_tuning(abi.TUNE_TEMPORAL, a.temporal)
     n = a.n
     N = n ** 3
     T0, P0, ktv, kfv = hrl.initial_fields(n, n, n, seed=1)
@@ -353,10 +373,12 @@ def run_ours(a):
            "ms_per_step": mixed["ms"] / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f32+f64 (mixed)", "data": "synthetic (seeded HRL initial condition)",
            "config": workload_config(a), "time_steps_per_s": steps_per_s,
+           "cell_updates_per_s": sum(x + y for x, y in mixed["iters"]) * N * ws / t_mixed,
            "pseudo_iterations_per_step": [list(x) for x in mixed["iters"]], "gpu_launches": mixed["launches"]}
     if fp64 is not None:
         t64, b64 = reduce_max_sum(ws, fp64["ms"] / 1e3, fp64["bytes"])
         out["fp64"] = {"T_eff_GBs": b64 / t64 / 1e9, "time_steps_per_s": a.steps * ws / t64,
+                       "cell_updates_per_s": sum(x + y for x, y in fp64["iters"]) * N * ws / t64,
                        "ms_per_step": fp64["ms"] / a.steps,
                        "pseudo_iterations_per_step": [list(x) for x in fp64["iters"]]}
         out["mixed_vs_fp64_time_steps_speedup"] = steps_per_s / out["fp64"]["time_steps_per_s"]
@@ -388,7 +410,9 @@ def run_ours(a):
     if a.fault_steps:
         out["fault_slab_511"] = fault_bench(ctx, stream, a)
     if a.v18_steps:
-        out["dimensional_127"] = v18_bench(ctx, stream, a.v18_steps)
+        out["dimensional_127"] = v18_bench(ctx, stream, a.v18_steps, nitmax=a.v18_nitmax)
+    if a.c127_steps and rank == 0:
+        out["config_127"] = c127_bench(ctx, stream, a.c127_steps, nitmax=a.v18_nitmax)
     if a.growth_steps:
         out["error_growth_127"] = growth_bench(ctx, stream, a.growth_steps)
     if a.c63_steps and rank == 0:
@@ -401,8 +425,9 @@ def run_ours(a):
         out["accuracy_255"] = accuracy_bench(ctx, stream, a.c3_steps, a.c3_n, a.c3_cadence_control, a.c3_out)
 
     if rank == 0:
-        v, cores, desc, _ = cpu_sample(n, a.cpu_seconds, threads=os.cpu_count())
-        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc}
+        v, cores, desc, _, cu = cpu_sample(n, a.cpu_seconds, threads=os.cpu_count())
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc,
+                               "cell_updates_per_s": cu}
     if rank == 0:
         print(json.dumps(out))
     ctx.close()
@@ -757,16 +782,16 @@ def accuracy_bench(ctx, stream, steps, n=255, cadence=500, out_path="", eps=1e-8
     return rec
 
 
-def v18_bench(ctx, stream, steps, n=127):
+def v18_bench(ctx, stream, steps, n=127, nitmax=100000):
     """Dimensional model (ht3d_step_v18, plain FP64) on the 10 x 10 x 5 km box
     at n^3: the steady initialisation step (it = 0) and the following steps
-    with pluton insertion and WENO5-v2 sub-stepping.  T_eff counts 10N*8+N
-    bytes per thermal and 11N*8+N per Darcy pseudo-iteration plus 21N*8 per
-    advection sub-step."""
+    with pluton insertion and WENO5-v2 sub-stepping, DYREL tolerance 1e-10.
+    T_eff counts 10N*8+N bytes per thermal and 11N*8+N per Darcy
+    pseudo-iteration plus 21N*8 per advection sub-step."""
     import torch
     import hydrothermal3d_gb300 as ht
     from hydrothermal3d_gb300 import api, v18
-    b = v18.box(n, n, n, seed=2)
+    b = v18.box(n, n, n, seed=2, nitmax=nitmax)
     p = b["params"]
     T, P = ht.from_numpy(b["T"]), ht.from_numpy(b["P"])
     args = (ht.from_numpy(b["phc"]), ht.from_numpy(b["phv"]), ht.from_numpy(b["wN"]), ht.from_numpy(b["kmul"]))
@@ -780,15 +805,59 @@ def v18_bench(ctx, stream, steps, n=127):
         for it in range(steps):
             p.it = it
             gt, gd = api.step_v18(ctx, T, P, *args, *V, p)
-            rows.append({"it": it, "iters": [gt.iters, gd.iters], "advection_substeps": p.n_adv})
+            rows.append({"it": it, "iters": [gt.iters, gd.iters], "converged": [gt.converged, gd.converged],
+                         "nF_rel": [gt.nF_rel, gd.nF_rel], "advection_substeps": p.n_adv})
             nbytes += gt.iters * bt + gd.iters * bd + p.n_adv * 21 * n ** 3 * 8
         e1.record(stream)
         torch.cuda.synchronize()
     t = e0.elapsed_time(e1) / 1e3
+    iters = sum(sum(r["iters"]) for r in rows)
     return {"n": n, "steps": steps, "seconds": t, "time_steps_per_s": steps / t, "T_eff_GBs": nbytes / t / 1e9,
+            "cell_updates_per_s": iters * n ** 3 / t, "all_converged": all(all(r["converged"]) for r in rows),
             "per_step": rows, "dtype": "f64",
             "case": "10x10x5 km box, T 600->20 C, log10 k ~ N(-15, 0.5) with 500 m correlation (seed 2), "
-                    "DYREL tol 1e-10 relative, nitmax 1e4, WENO5 v2 with the reference's stencil, CFL 0.5"}
+                    f"DYREL tol 1e-10 relative, nitmax {nitmax}, WENO5 v2 with the reference's stencil, CFL 0.5"}
+
+
+def c127_bench(ctx, stream, steps, n=127, nitmax=100000):
+    """The first `steps` time steps of the 127^3 dimensional box on the oracle
+    (C++ FP64, OpenMP over the host cores) and on the GPU's FP64 form: the
+    iteration counts and the max-norm relative difference of T, P and the
+    Darcy velocities after each step."""
+    import torch
+    import oracle
+    import hydrothermal3d_gb300 as ht
+    from hydrothermal3d_gb300 import api, v18
+    oracle.set_threads(os.cpu_count())
+    b = v18.box(n, n, n, seed=2, nitmax=nitmax)
+    q = v18.box(n, n, n, seed=2, nitmax=nitmax)["params"]
+    p = b["params"]
+    T, P = b["T"].copy(order="F"), b["P"].copy(order="F")
+    V = [np.zeros(s, order="F") for s in ((n + 1, n, n), (n, n + 1, n), (n, n, n + 1))]
+    Td, Pd = ht.from_numpy(T), ht.from_numpy(P)
+    Vd = [ht.zeros(*v.shape) for v in V]
+    args = (ht.from_numpy(b["phc"]), ht.from_numpy(b["phv"]), ht.from_numpy(b["wN"]), ht.from_numpy(b["kmul"]))
+    inner = (slice(1, -1),) * 3
+    rows = []
+    t_oracle = 0.0
+    for it in range(steps):
+        p.it = q.it = it
+        with torch.cuda.stream(stream):
+            gt, gd = api.step_v18(ctx, Td, Pd, *args, *Vd, q)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s, ot, od = oracle.step_v18(T, P, b["phc"], b["phv"], b["wN"], b["kmul"], *V, p)
+        t_oracle += time.perf_counter() - t0
+        rel = lambda a, c: float(np.abs(a - c).max() / np.abs(c).max())
+        Tg, Pg = ht.to_numpy(Td), ht.to_numpy(Pd)
+        rows.append({"it": it, "iters_gpu": [gt.iters, gd.iters], "iters_oracle": [ot.iters, od.iters],
+                     "T_rel_err": rel(Tg[inner], T[inner]), "P_rel_err": rel(Pg[inner], P[inner]),
+                     "V_rel_err": max(rel(ht.to_numpy(a), c) for a, c in zip(Vd, V)),
+                     "T_bitwise": bool(np.array_equal(Tg, T)), "P_bitwise": bool(np.array_equal(Pg, P)),
+                     "dt_equal": q.dt == p.dt, "n_adv": [q.n_adv, p.n_adv]})
+        print(json.dumps({"config_127_step": rows[-1]}), file=sys.stderr, flush=True)
+    return {"n": n, "steps": steps, "per_step": rows, "oracle_seconds": t_oracle, "oracle_cores": oracle.num_threads(),
+            "case": "10x10x5 km box (seed 2), DYREL tol 1e-10, nitmax %d, WENO5 v2 (reference stencil)" % nitmax}
 
 
 def post_bench(ctx, stream, n, reps=5):

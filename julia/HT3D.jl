@@ -1556,6 +1556,30 @@ function breakpoint_read!(path, Tc_ex, Pc_ex; ctx::Context = context())
 end
 
 """
+    breakpoint_write_h5(path, Tc_ex, Pc_ex, time, dt)
+
+`ht3d_breakpoint_write_h5` (include/ht3d.h).
+"""
+function breakpoint_write_h5(path, Tc_ex, Pc_ex, time, dt; ctx::Context = context())
+    nx, ny, nz = size(Tc_ex) .- 2
+    _check(ctx, C.ht3d_breakpoint_write_h5(ctx.ptr, path, Tc_ex, Pc_ex, time, dt, nx, ny, nz))
+    return nothing
+end
+
+"""
+    breakpoint_read_h5!(path, Tc_ex, Pc_ex)
+
+`ht3d_breakpoint_read_h5` (include/ht3d.h); returns time, dt.
+"""
+function breakpoint_read_h5!(path, Tc_ex, Pc_ex; ctx::Context = context())
+    nx, ny, nz = size(Tc_ex) .- 2
+    time = Ref{Cdouble}()
+    dt = Ref{Cdouble}()
+    _check(ctx, C.ht3d_breakpoint_read_h5(ctx.ptr, path, Tc_ex, Pc_ex, time, dt, nx, ny, nz))
+    return time[], dt[]
+end
+
+"""
     ensemble_step!(members::Vector{Instance}, precision)
 
 One time step of every member (`ht3d_ensemble_step`); returns the members' statuses.

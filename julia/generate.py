@@ -368,6 +368,8 @@ FUSED = [
     ("Nusselt", "ht3d_Nusselt", "qy", "fy", ["Nu"]),
     ("breakpoint_write", "ht3d_breakpoint_write", "Tc_ex", "ex", []),
     ("breakpoint_read!", "ht3d_breakpoint_read", "Tc_ex", "ex", ["time", "dt"]),
+    ("breakpoint_write_h5", "ht3d_breakpoint_write_h5", "Tc_ex", "ex", []),
+    ("breakpoint_read_h5!", "ht3d_breakpoint_read_h5", "Tc_ex", "ex", ["time", "dt"]),
 ]
 OUT_TYPES = {"stats": "DyrelStats", "st_thermal": "DyrelStats", "st_darcy": "DyrelStats", "Nu": "Cdouble",
              "time": "Cdouble", "dt": "Cdouble"}

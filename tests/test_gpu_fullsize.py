@@ -8,6 +8,11 @@ against each other where the oracle would take minutes to hours:
   FP64 step from the same seeded state; T within 1e-6 (relative max-norm,
   the mixed form's accuracy target) and P (mean removed) within 1e-6; both
   forms' solves converge.
+* 255^3 HRL, six steps on the FP64 trajectory (through the onset of
+  convection, where the reference's dt rule takes a CFL-22 advection step):
+  at every step one mixed step from the FP64 state with the FP64 run's dt
+  stays within 1e-6 of the FP64 step in T and P, with the same iteration
+  counts.
 * 511^3 WENO5 sweep (blob in the seeded divergence-free curl velocity, CFL
   0.5): the FP32 sweep within 2e-5 and the mixed sweep within 2e-6 of the
   FP64 sweep (relative to max |T|), the per-sweep tolerances of the
@@ -51,6 +56,35 @@ def test_hrl_255_mixed_step_tracks_fp64(ctx):
     assert float((Tm - T6).abs().max() / T6.abs().max()) <= 1e-6
     assert float((Pm - P6).abs().max() / P6.abs().max()) <= 1e-6
     assert abs(dtm - dt6) <= 1e-6 * dt6  # the next step's dt comes from the velocity of each form
+
+
+def test_hrl_255_mixed_step_error_on_the_fp64_trajectory(ctx):
+    """The error the mixed form adds per time step, over the first six steps
+    of the 255^3 workload (the sixth takes the onset step)."""
+    n = 255
+    T, P, ktv, kfv = hrl.initial_fields(n, n, n, seed=1)
+    ktd, kfd = ht.from_numpy(ktv), ht.from_numpy(kfv)
+    vel = lambda: [ht.zeros(n + 1, n, n), ht.zeros(n, n + 1, n), ht.zeros(n, n, n + 1)]
+    Td, Pd, V = ht.from_numpy(T), ht.from_numpy(P), vel()
+    Tl, Pl, Vl = ht.zeros(*Td.shape), ht.zeros(*Pd.shape), vel()
+    p = hrl.params(n, n, n)
+    errs = []
+    for step in range(6):
+        ctx.synchronize()
+        Tl.copy_(Td)
+        Pl.copy_(Pd)
+        torch.cuda.synchronize()
+        q = hrl.params(n, n, n)
+        q.dt = p.dt
+        lt, ld = api.step_hrl(ctx, Tl, Pl, ktd, kfd, *Vl, q, abi.MIXED)
+        gt, gd = api.step_hrl(ctx, Td, Pd, ktd, kfd, *V, p, abi.FP64)
+        assert (lt.iters, ld.iters) == (gt.iters, gd.iters), step
+        ctx.synchronize()
+        t6, tm = Td[INNER], Tl[INNER]
+        p6, pm = Pd[INNER] - Pd[INNER].mean(), Pl[INNER] - Pl[INNER].mean()
+        errs.append((float((tm - t6).abs().max() / t6.abs().max()), float((pm - p6).abs().max() / p6.abs().max())))
+    assert max(e[0] for e in errs) <= 1e-6, errs
+    assert max(e[1] for e in errs) <= 1e-6, errs
 
 
 def _f32(t):
