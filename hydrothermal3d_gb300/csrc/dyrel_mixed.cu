@@ -228,47 +228,61 @@ __global__ void __launch_bounds__(HT3D_MIX_BS, HT3D_MIX_MINB) k_mixed_inner(cons
 }
 
 // ---------------------------------------------------------------------------
-// Two inner iterations per pass (temporal blocking).  A CTA owns a column tile
-// of TB_X x TB_Y cells (its "halo tile") whose inner (TB_X-2) x (TB_Y-2) cells
-// it updates twice, marching through a chunk of zchunk planes:
+// Two inner iterations per pass (temporal blocking).  A CTA of TB_Y warps
+// owns a column tile of TB_X x TB_Y cells (its "halo tile"): warp w is row
+// y0 + w, lane l the quad of cells x0 + 4l .. x0 + 4l + 3, as in
+// k_mixed_inner.  Marching through a chunk of zchunk planes it computes
 //   A: iteration n on every cell of the halo tile, plane p;
-//   B: iteration n+1 on the inner cells of plane p-1 from D' planes p-2
-//      (register), p-1 (shared), p (register).
-// Halo cells (one ring in x and y, one plane before and after the chunk) are
-// computed by both neighbouring CTAs.  Every field is read once per pass and
-// D', D'' are written once each (the next pass needs both: D'' and its
-// previous correction D'); both go to buffers the pass does not read, since
-// the halo reads neighbouring cells' D and Dprev.  Iteration B's Dprev is
-// iteration A's input D, already in registers.  Both iterations use
-// mixed_cell, so the result is bit-identical to two k_mixed_inner launches.
+//   B: iteration n+1 on the inner cells (lanes 1..30, warps 1..TB_Y-2) of
+//      plane p-1 from D' of planes p-2 (registers), p-1 (own quad in
+//      registers, x-neighbours by warp shuffles, y-neighbours from shared
+//      memory) and p (registers).
+// Halo cells (one quad in x, one row in y, one plane before and after the
+// chunk) are computed by both neighbouring CTAs.  Every field is read once
+// per pass and D', D'' are written once each (the next pass needs both: D''
+// and its previous correction D'); both go to buffers the pass does not
+// read, since the halo reads neighbouring cells' D and Dprev.  Iteration B's
+// Dprev is iteration A's input D, already in registers, and B's face
+// conductivities and residual are A's, carried in registers from the plane
+// before.  Both iterations use mixed_cell, so the result is bit-identical to
+// two k_mixed_inner launches.
 //
-// The inputs of plane p (D over the tile plus one ring, kx, ky, kz, Rin, Dprev)
-// are brought into shared memory by TMA tensor copies (one thread issues six
-// 3-D box loads per plane, completing on the plane's mbarrier) two planes
-// ahead, in a ring of TB_STAGES planes.  Boxes are TB_BW floats wide and start
-// on a 4-float boundary below the tile (TMA wants 16-byte aligned x); elements
-// outside the arrays are zero-filled.  Every mbarrier wait is bounded: on
-// timeout the CTA records HT3D_ERR_TIMEOUT in *err, waits (bounded) for its
-// copies in flight and returns.
+// The inputs of plane p (D over the tile plus one ring, kx, ky, kz, Rin,
+// Dprev) are brought into shared memory by TMA tensor copies (one thread
+// issues six 3-D box loads per plane, completing on the plane's mbarrier) two
+// planes ahead, in a ring of TB_STAGES planes.  Boxes start on 4-float
+// boundaries (TMA wants 16-byte aligned x: x0 is a multiple of 4); elements
+// outside the arrays are zero-filled.  Every thread reads its quads with
+// 16-byte shared loads.  Every mbarrier wait is bounded: on timeout the CTA
+// records HT3D_ERR_TIMEOUT in *err, waits (bounded) for its copies in flight
+// and returns.
 // ---------------------------------------------------------------------------
-constexpr int TB_X = 32, TB_Y = 16, TB_STAGES = 3, TB_BW = 40;
+#ifndef HT3D_TB_Y
+#define HT3D_TB_Y 16
+#endif
+constexpr int TB_LANES = 32, TB_X = 4 * TB_LANES, TB_Y = HT3D_TB_Y, TB_STAGES = 3;
+constexpr int TB_OX = TB_X - 8, TB_OY = TB_Y - 2;  // cells of a tile that iteration B updates
+constexpr int TB_WD = TB_X + 8;                    // D box: x0 - 4 .. x0 + TB_X + 3
+constexpr int TB_WK = TB_X + 4;                    // kx box: x0 .. x0 + TB_X + 3 (east face of the last quad)
 constexpr unsigned kTbWaitLimit = 1u << 22;
 
 struct __align__(128) TbStage {
-    float D[TB_Y + 2][TB_BW];   // rows y0-1 .. y0+TB_Y, columns xD .. xD+TB_BW-1
-    float pad0[(128 - ((TB_Y + 2) * TB_BW * 4) % 128) % 128 / 4];
-    float kx[TB_Y][TB_BW];      // rows y0 .. y0+TB_Y-1, columns xK ..
-    float ky[TB_Y + 1][TB_BW];  // rows y0 .. y0+TB_Y
-    float pad1[(128 - ((TB_Y + 1) * TB_BW * 4) % 128) % 128 / 4];
-    float kz[TB_Y][TB_BW];
-    float R[TB_Y][TB_BW];
-    float Dp[TB_Y][TB_BW];      // previous correction
+    float D[TB_Y + 2][TB_WD];   // rows y0-1 .. y0+TB_Y, columns x0-4 ..
+    float pad0[(128 - ((TB_Y + 2) * TB_WD * 4) % 128) % 128 / 4];
+    float kx[TB_Y][TB_WK];      // rows y0 .. y0+TB_Y-1, columns x0 ..
+    float pad1[(128 - (TB_Y * TB_WK * 4) % 128) % 128 / 4];
+    float ky[TB_Y + 1][TB_X];   // rows y0 .. y0+TB_Y
+    float kz[TB_Y][TB_X];
+    float R[TB_Y][TB_X];
+    float Dp[TB_Y][TB_X];       // previous correction
 };
-constexpr unsigned kTbStageBytes = 4u * TB_BW * ((TB_Y + 2) + 5 * TB_Y + 1);  // bytes the six boxes deliver
+constexpr unsigned kTbStageBytes = 4u * ((TB_Y + 2) * TB_WD + TB_Y * TB_WK + (TB_Y + 1) * TB_X + 3 * TB_Y * TB_X);
 static_assert(offsetof(TbStage, kx) % 128 == 0 && offsetof(TbStage, ky) % 128 == 0 &&
                   offsetof(TbStage, kz) % 128 == 0 && offsetof(TbStage, R) % 128 == 0 &&
                   offsetof(TbStage, Dp) % 128 == 0 && sizeof(TbStage) % 128 == 0,
               "TMA destinations must be 128-byte aligned");
+static_assert((TB_WD * 4) % 16 == 0 && (TB_WK * 4) % 16 == 0 && TB_WD <= 256 && TB_WK <= 256,
+              "TMA box rows must be whole 16-byte units of at most 256 elements");
 
 struct TbMaps {  // tensor maps of one pass (by value, in the constant bank)
     CUtensorMap D, kx, ky, kz, R, Dp;
@@ -302,48 +316,81 @@ __device__ __forceinline__ void tma_load3(void* dst, const CUtensorMap* map, int
         : "memory");
 }
 
+__device__ __forceinline__ float4 lds4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+
+// Coefficients of a quad (face conductivities and residual) and its input
+// correction: what iteration B at a plane reuses from iteration A there.
+struct QuadIn {
+    float4 kW, kS, kN, kB, kF, r, xc;
+    float kE3;  // east face of the quad's last cell
+};
+
+// One iteration on a quad: the four cells of mixed_quad with the same ghost
+// rules (i0, j, k: the quad's first cell; neighbours passed in).
+__device__ __forceinline__ void pair_quad(const QuadIn& c, float4 xp, float dW, float dE, float4 xs4, float4 xn4,
+                                          float4 xb4, float4 xf4, int i0, int j, int k, const Pad& p,
+                                          const BC6<float>& bc, const MixScal& s, float _dx2, float _dy2, float _dz2,
+                                          float4& xout, float4& fout) {
+    const bool south = j > 0, north = j < p.ny - 1, back = k > 0, front = k < p.nz - 1;
+    float o[4], of[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        const int i = i0 + m;
+        const float xc = c4(c.xc, m);
+        const float xw = (i == 0) ? ghost(bc, 0, xc) : (m == 0 ? dW : c4(c.xc, m - 1));
+        const float xe = (i == p.nx - 1) ? ghost(bc, 1, xc) : (m == 3 ? dE : c4(c.xc, m + 1));
+        const float xs = south ? c4(xs4, m) : ghost(bc, 2, xc);
+        const float xn = north ? c4(xn4, m) : ghost(bc, 3, xc);
+        const float xb = back ? c4(xb4, m) : ghost(bc, 4, xc);
+        const float xf = front ? c4(xf4, m) : ghost(bc, 5, xc);
+        const float kE = m == 3 ? c.kE3 : c4(c.kW, m + 1);
+        mixed_cell(xc, xw, xe, xs, xn, xb, xf, c4(c.kW, m), kE, c4(c.kS, m), c4(c.kN, m), c4(c.kB, m), c4(c.kF, m),
+                   c4(c.r, m), c4(xp, m), s.mom, s.dh2, s.cX, s._dx, s._dy, s._dz, _dx2, _dy2, _dz2, of[m], o[m]);
+        if (i >= p.nx) o[m] = of[m] = 0.f;  // padding stays zero
+    }
+    xout = make_float4(o[0], o[1], o[2], o[3]);
+    fout = make_float4(of[0], of[1], of[2], of[3]);
+}
+
 template <bool STOREF>
-__global__ void __launch_bounds__(TB_X* TB_Y, 2) k_mixed_inner2(const __grid_constant__ TbMaps maps,
-                                                                const float* __restrict__ Din, float* __restrict__ D1out,
-                                                                float* __restrict__ D2out, float* __restrict__ F,
-                                                                MixScal s, BC6<float> bc, Pad p, int zchunk,
-                                                                int* __restrict__ err, int skip_plane,
-                                                                unsigned detect_limit) {
+__global__ void __launch_bounds__(TB_LANES* TB_Y, TB_Y <= 8 ? 2 : 1) k_mixed_inner2(const __grid_constant__ TbMaps maps,
+                                                                    const float* __restrict__ Din,
+                                                                    float* __restrict__ D1out,
+                                                                    float* __restrict__ D2out, float* __restrict__ F,
+                                                                    MixScal s, BC6<float> bc, Pad p, int zchunk,
+                                                                    int* __restrict__ err, int skip_plane,
+                                                                    unsigned detect_limit) {
     extern __shared__ unsigned char tb_raw[];
     unsigned char* base = tb_raw + ((128 - (smem_u32(tb_raw) & 127)) & 127);
     TbStage* st = reinterpret_cast<TbStage*>(base);
-    float* dpbuf = reinterpret_cast<float*>(base + sizeof(TbStage) * TB_STAGES);  // two D' planes
-    uint64_t* bar = reinterpret_cast<uint64_t*>(base + sizeof(TbStage) * TB_STAGES + sizeof(float) * 2 * TB_Y * TB_X);
+    float* xbuf = reinterpret_cast<float*>(base + sizeof(TbStage) * TB_STAGES);  // A's result, three planes
+    uint64_t* bar = reinterpret_cast<uint64_t*>(base + sizeof(TbStage) * TB_STAGES + sizeof(float) * 3 * TB_Y * TB_X);
     __shared__ int abort_flag;
-    const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + TB_X * ty;
-    const int x0 = blockIdx.x * (TB_X - 2) - 1, y0 = blockIdx.y * (TB_Y - 2) - 1;  // halo tile origin
-    const int xD = (x0 - 1) & ~3, xK = x0 & ~3;  // 16-byte aligned box origins (floor)
-    const int gi = x0 + tx, gj = y0 + ty;
-    const bool in = gi >= 0 && gi < p.nx && gj >= 0 && gj < p.ny;
-    const bool inner = in && tx >= 1 && tx <= TB_X - 2 && ty >= 1 && ty <= TB_Y - 2;
-    const bool gW = gi == 0, gE = gi == p.nx - 1, gS = gj == 0, gN = gj == p.ny - 1;
+    const int lane = threadIdx.x, ty = threadIdx.y, tid = lane + TB_LANES * ty;
+    const int x0 = blockIdx.x * TB_OX - 4, y0 = blockIdx.y * TB_OY - 1;  // halo tile origin (x0 % 4 == 0)
+    const int i0 = x0 + 4 * lane, j = y0 + ty;
+    const bool rowin = j >= 0 && j < p.PY && i0 >= 0 && i0 < p.PX;  // quad inside the padded array
+    const bool inner = i0 >= 0 && i0 < p.nx && j >= 0 && j < p.ny && lane >= 1 && lane <= TB_LANES - 2 &&
+                       ty >= 1 && ty <= TB_Y - 2;
     const int k0 = blockIdx.z * zchunk, k1 = min(p.nz, k0 + zchunk);
     const int pa0 = max(k0 - 1, 0);
     const int plast = min(k1 + 1, p.nz);  // last staged plane (plane nz: its bottom z-faces)
-    const float mom = s.mom, dh2 = s.dh2, cX = s.cX, _dx = s._dx, _dy = s._dy, _dz = s._dz;
-    const float _dx2 = __fmul_rn(_dx, _dx), _dy2 = __fmul_rn(_dy, _dy), _dz2 = __fmul_rn(_dz, _dz);
-    // this thread's element offsets inside a stage's tiles (fixed over planes)
-    const int oD = (ty + 1) * TB_BW + tx + (x0 - xD);  // D centre
-    const int oK = ty * TB_BW + tx + (x0 - xK);        // faces / cell fields
-    const int oP = ty * TB_X + tx;                      // D' planes
-    // skip_plane >= 0 (HT3D_TUNE_WAIT_TEST only): that plane's copies are never
-    // issued, so its wait runs out and the error path below is exercised
+    const float _dx2 = __fmul_rn(s._dx, s._dx), _dy2 = __fmul_rn(s._dy, s._dy), _dz2 = __fmul_rn(s._dz, s._dz);
+    // this thread's offsets inside a stage (fixed over planes)
+    const int oD = (ty + 1) * TB_WD + 4 + 4 * lane;  // D, quad centre
+    const int oK = ty * TB_WK + 4 * lane;            // kx
+    const int oC = ty * TB_X + 4 * lane;             // ky (south), kz, R, Dp, and the A-result planes
     auto issue = [&](int k) {  // thread 0: the six boxes of plane k into slot k % TB_STAGES
-        if (k == skip_plane) return;
+        if (k == skip_plane) return;  // HT3D_TUNE_WAIT_TEST only: never issued, its wait runs out
         TbStage& S = st[k % TB_STAGES];
         uint64_t* b = &bar[k % TB_STAGES];
         mbar_expect_tx(b, kTbStageBytes);
-        tma_load3(&S.D[0][0], &maps.D, xD, y0 - 1, k, b);
-        tma_load3(&S.kx[0][0], &maps.kx, xK, y0, k, b);
-        tma_load3(&S.ky[0][0], &maps.ky, xK, y0, k, b);
-        tma_load3(&S.kz[0][0], &maps.kz, xK, y0, k, b);
-        tma_load3(&S.R[0][0], &maps.R, xK, y0, k, b);
-        tma_load3(&S.Dp[0][0], &maps.Dp, xK, y0, k, b);
+        tma_load3(&S.D[0][0], &maps.D, x0 - 4, y0 - 1, k, b);
+        tma_load3(&S.kx[0][0], &maps.kx, x0, y0, k, b);
+        tma_load3(&S.ky[0][0], &maps.ky, x0, y0, k, b);
+        tma_load3(&S.kz[0][0], &maps.kz, x0, y0, k, b);
+        tma_load3(&S.R[0][0], &maps.R, x0, y0, k, b);
+        tma_load3(&S.Dp[0][0], &maps.Dp, x0, y0, k, b);
     };
     if (tid == 0) {
         abort_flag = 0;
@@ -356,22 +403,28 @@ __global__ void __launch_bounds__(TB_X* TB_Y, 2) k_mixed_inner2(const __grid_con
         if (pa0 + 1 <= plast) issue(pa0 + 1);
     }
     int issued = min(pa0 + 1, plast);  // last plane whose copies are in flight or done
-    // rotating stage pointers (planes pl, pl + 1, pl + 2) and D' planes
     const TbStage* S0 = &st[pa0 % TB_STAGES];
     const TbStage* S1 = &st[(pa0 + 1) % TB_STAGES];
     const TbStage* S2 = &st[(pa0 + 2) % TB_STAGES];
-    float* dpw = dpbuf + (pa0 & 1) * TB_Y * TB_X + oP;  // written by A at plane pl
-    float* dpr = dpbuf + ((pa0 + 1) & 1) * TB_Y * TB_X + oP;  // plane pl - 1, read by B
-    // running global addresses of this column for B's plane q = pl - 1
-    const long long colo = gi + (long long)p.PX * gj;
+    // A's result of plane pl goes to buffer pl % 3; B reads plane pl - 1's.  A of
+    // plane pl + 2 reuses the buffer B of plane pl - 1 reads, and every warp has
+    // finished that B before the CTA barrier that plane pl + 1's A precedes.
+    float* xw_ = xbuf + (pa0 % 3) * TB_Y * TB_X + oC;
+    float* xr_ = xbuf + ((pa0 + 2) % 3) * TB_Y * TB_X + oC;
+    float* xn_ = xbuf + ((pa0 + 1) % 3) * TB_Y * TB_X + oC;
+    const long long colo = i0 + (long long)p.PX * j;
     float* outD1 = D1out + colo + p.plane * (long long)(pa0 - 1);
     float* outD2 = D2out + colo + p.plane * (long long)(pa0 - 1);
     float* outF = F + colo + p.plane * (long long)(pa0 - 1);
-    float dm1 = (pa0 > 0 && in) ? Din[p.plane * (pa0 - 1) + colo] : 0.f;  // D(p-1)
-    float dpm = 0.f, dpc = 0.f;
-    float cW = 0.f, cE = 0.f, cS = 0.f, cN = 0.f, cB = 0.f, cF = 0.f, cr = 0.f, cd0 = 0.f;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 dm1 = (pa0 > 0 && rowin) ? *reinterpret_cast<const float4*>(Din + p.plane * (pa0 - 1) + colo) : z4;
+    float4 dpm = z4, dpc = z4;  // A's result at planes pl - 2 and pl - 1
+    QuadIn cb{};                // A's inputs at plane pl - 1 (B's coefficients)
     for (int pl = pa0; pl <= k1; ++pl) {
         if (pl + 2 <= plast) {
+            // slot (pl + 2) % 3 was last read by iteration A of planes pl - 1 and
+            // pl - 2, which every warp finished before the CTA barrier of the
+            // previous plane
             if (tid == 0) {
                 // order the earlier generic reads of this slot before the async-proxy writes
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -380,17 +433,43 @@ __global__ void __launch_bounds__(TB_X* TB_Y, 2) k_mixed_inner2(const __grid_con
             issued = pl + 2;
         }
         // planes pl and pl + 1 have landed (phase = number of earlier uses of the
-        // slot); thread 0 polls the barriers, the CTA barrier then releases (and
-        // orders the copied data for) every other thread
-        if (tid == 0) {
-            bool ok = mbar_wait_bounded(&bar[pl % TB_STAGES], ((pl - pa0) / TB_STAGES) & 1, detect_limit);
+        // slot): lane 0 of every warp polls the barriers, __syncwarp then orders
+        // the copied data for the warp's other lanes.  A warp runs at most one
+        // plane ahead of another (one CTA barrier per plane), so the phase it
+        // waits for is always the slot's next one.
+        bool ok = true;
+        if (lane == 0) {
+            ok = mbar_wait_bounded(&bar[pl % TB_STAGES], ((pl - pa0) / TB_STAGES) & 1, detect_limit);
             if (pl + 1 <= plast)
                 ok = ok && mbar_wait_bounded(&bar[(pl + 1) % TB_STAGES], ((pl + 1 - pa0) / TB_STAGES) & 1,
                                              detect_limit);
             if (!ok) abort_flag = 1;
         }
+        ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+        __syncwarp();
+        // ---- A: iteration n at plane pl, every quad of the halo tile
+        QuadIn ca{};
+        float4 da = z4;
+        if (ok && pl < p.nz) {
+            const float* d0 = &S0->D[0][0] + oD;
+            ca.xc = lds4(d0);
+            ca.kW = lds4(&S0->kx[0][0] + oK);
+            ca.kE3 = (&S0->kx[0][0])[oK + 4];
+            ca.kS = lds4(&S0->ky[0][0] + oC);
+            ca.kN = lds4(&S0->ky[0][0] + oC + TB_X);
+            ca.kB = lds4(&S0->kz[0][0] + oC);
+            ca.kF = lds4(&S1->kz[0][0] + oC);
+            ca.r = lds4(&S0->R[0][0] + oC);
+            const float4 xp = lds4(&S0->Dp[0][0] + oC);
+            const float4 xs4 = lds4(d0 - TB_WD), xn4 = lds4(d0 + TB_WD);
+            const float4 xf4 = lds4(&S1->D[0][0] + oD);
+            float4 fa;
+            pair_quad(ca, xp, d0[-1], d0[4], xs4, xn4, dm1, xf4, i0, j, pl, p, bc, s, _dx2, _dy2, _dz2, da, fa);
+            dm1 = ca.xc;
+            *reinterpret_cast<float4*>(xw_) = da;
+        }
         __syncthreads();
-        if (abort_flag) {
+        if (abort_flag) {  // a wait gave up: every thread leaves here
             if (tid == 0) {
                 atomicExch(err, HT3D_ERR_TIMEOUT);
                 // every copy issued must land before the CTA's shared memory is released
@@ -400,66 +479,39 @@ __global__ void __launch_bounds__(TB_X* TB_Y, 2) k_mixed_inner2(const __grid_con
             __syncthreads();
             return;
         }
-        float da = 0.f, aW = 0.f, aE = 0.f, aS = 0.f, aN = 0.f, aB = 0.f, aF = 0.f, ar = 0.f, ad0 = 0.f;
-        if (pl < p.nz) {
-            const float* d0 = &S0->D[0][0] + oD;
-            const float* k0p = &S0->kx[0][0] + oK;
-            const float* y0p = &S0->ky[0][0] + oK;
-            aW = k0p[0];
-            aE = k0p[1];
-            aS = y0p[0];
-            aN = y0p[TB_BW];
-            aB = (&S0->kz[0][0])[oK];
-            aF = (&S1->kz[0][0])[oK];
-            ar = (&S0->R[0][0])[oK];
-            const float xp = (&S0->Dp[0][0])[oK];
-            const float xc = d0[0];
-            const float xw = gW ? ghost(bc, 0, xc) : d0[-1];
-            const float xe = gE ? ghost(bc, 1, xc) : d0[1];
-            const float xs = gS ? ghost(bc, 2, xc) : d0[-TB_BW];
-            const float xn = gN ? ghost(bc, 3, xc) : d0[TB_BW];
-            const float xb = (pl == 0) ? ghost(bc, 4, xc) : dm1;
-            const float xf = (pl == p.nz - 1) ? ghost(bc, 5, xc) : (&S1->D[0][0])[oD];
-            float f;
-            mixed_cell(xc, xw, xe, xs, xn, xb, xf, aW, aE, aS, aN, aB, aF, ar, xp, mom, dh2, cX, _dx, _dy, _dz, _dx2,
-                       _dy2, _dz2, f, da);
-            ad0 = xc;  // iteration B's previous correction at this cell
-            dm1 = xc;
-            *dpw = da;
-        }
-        __syncthreads();
+        // ---- B: iteration n+1 at plane pl - 1 on the inner quads
+        // every lane takes part in the shuffles
+        const float bW = __shfl_up_sync(0xffffffffu, dpc.w, 1);
+        const float bE = __shfl_down_sync(0xffffffffu, dpc.x, 1);
         if (pl - 1 >= k0 && inner) {
             const int q = pl - 1;
-            const float xc = dpc;
-            const float xw = gW ? ghost(bc, 0, xc) : dpr[-1];
-            const float xe = gE ? ghost(bc, 1, xc) : dpr[1];
-            const float xs = gS ? ghost(bc, 2, xc) : dpr[-TB_X];
-            const float xn = gN ? ghost(bc, 3, xc) : dpr[TB_X];
-            const float xb = (q == 0) ? ghost(bc, 4, xc) : dpm;
-            const float xf = (q == p.nz - 1) ? ghost(bc, 5, xc) : da;
-            float f, xn1;
-            mixed_cell(xc, xw, xe, xs, xn, xb, xf, cW, cE, cS, cN, cB, cF, cr, cd0, mom, dh2, cX, _dx, _dy, _dz, _dx2,
-                       _dy2, _dz2, f, xn1);
-            *outD1 = xc;
-            *outD2 = xn1;
-            if (STOREF) *outF = f;
+            QuadIn c = cb;
+            const float4 xprev = c.xc;  // B's previous correction: A's input
+            c.xc = dpc;
+            float4 xb2, fb;
+            pair_quad(c, xprev, bW, bE, lds4(xr_ - TB_X), lds4(xr_ + TB_X), dpm, da, i0, j, q, p, bc, s, _dx2, _dy2,
+                      _dz2, xb2, fb);
+            *reinterpret_cast<float4*>(outD1) = dpc;
+            *reinterpret_cast<float4*>(outD2) = xb2;
+            if (STOREF) *reinterpret_cast<float4*>(outF) = fb;
         }
         outD1 += p.plane;
         outD2 += p.plane;
         outF += p.plane;
         dpm = dpc;
         dpc = da;
-        cW = aW; cE = aE; cS = aS; cN = aN; cB = aB; cF = aF; cr = ar; cd0 = ad0;
+        cb = ca;
         const TbStage* t = S0;
         S0 = S1;
         S1 = S2;
         S2 = t;
-        float* u = dpw;
-        dpw = dpr;
-        dpr = u;
+        float* u = xr_;
+        xr_ = xw_;
+        xw_ = xn_;
+        xn_ = u;
     }
 }
-constexpr size_t kTbSmem = 128 + sizeof(TbStage) * TB_STAGES + sizeof(float) * 2 * TB_Y * TB_X + 8 * TB_STAGES;
+constexpr size_t kTbSmem = 128 + sizeof(TbStage) * TB_STAGES + sizeof(float) * 3 * TB_Y * TB_X + 8 * TB_STAGES;
 
 // cuTensorMapEncodeTiled, fetched from the driver at run time (no libcuda link)
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -480,13 +532,13 @@ EncodeTiledFn encode_tiled() {
     });
     return fn;
 }
-// map of a padded FP32 field: (PX, PY, nz+1) elements, boxes TB_BW x rows x 1
-bool tb_map(CUtensorMap* m, const float* field, const Pad& P, unsigned rows) {
+// map of a padded FP32 field: (PX, PY, nz+1) elements, boxes width x rows x 1
+bool tb_map(CUtensorMap* m, const float* field, const Pad& P, unsigned width, unsigned rows) {
     EncodeTiledFn fn = encode_tiled();
     if (!fn) return false;
     const cuuint64_t dims[3] = {(cuuint64_t)P.PX, (cuuint64_t)P.PY, (cuuint64_t)P.nz + 1};
     const cuuint64_t strides[2] = {(cuuint64_t)P.PX * 4, (cuuint64_t)P.plane * 4};
-    const cuuint32_t box[3] = {(cuuint32_t)TB_BW, rows, 1};
+    const cuuint32_t box[3] = {width, rows, 1};
     const cuuint32_t es[3] = {1, 1, 1};
     return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)field, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -779,17 +831,25 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
     // two iterations per pass (k_mixed_inner2) inside runs of inner iterations
     bool pairs = want_pairs;
     int zc = ctx->mixed_temporal >= 2 ? ctx->mixed_temporal : 0;
-    const int tiles = ((nx + TB_X - 3) / (TB_X - 2)) * ((ny + TB_Y - 3) / (TB_Y - 2));
-    if (!zc) zc = (int)std::min<long long>(64, std::max<long long>(8, (long long)nz * tiles / (8LL * ctx->num_sms)));
-    const dim3 tb(TB_X, TB_Y), tg((nx + TB_X - 3) / (TB_X - 2), (ny + TB_Y - 3) / (TB_Y - 2), (nz + zc - 1) / zc);
+    const int tiles = ((nx + TB_OX - 1) / TB_OX) * ((ny + TB_OY - 1) / TB_OY);
+    if (!zc) {  // fewest waves x (chunk + the two planes iteration A adds)
+        const long long slots = (long long)ctx->num_sms * (TB_Y <= 8 ? 2 : 1);  // resident CTAs
+        long long best = -1;
+        for (int c = 8; c <= 64; ++c) {
+            const long long ctas = (long long)tiles * ((nz + c - 1) / c);
+            const long long cost = (ctas + slots - 1) / slots * (std::min(c, nz) + 2);
+            if (best < 0 || cost < best) best = cost, zc = c;
+        }
+    }
+    const dim3 tb(TB_LANES, TB_Y), tg((nx + TB_OX - 1) / TB_OX, (ny + TB_OY - 1) / TB_OY, (nz + zc - 1) / zc);
     TbMaps mk;                       // conductivity and residual maps
     CUtensorMap mapD[4], mapP[4];    // each correction buffer as a pass's D (with its ring) and as its Dprev
     int* derr = nullptr;
     if (pairs) {
-        pairs = tb_map(&mk.kx, kx32, P, TB_Y) && tb_map(&mk.ky, ky32, P, TB_Y + 1) && tb_map(&mk.kz, kz32, P, TB_Y) &&
-                tb_map(&mk.R, Rin, P, TB_Y);
+        pairs = tb_map(&mk.kx, kx32, P, TB_WK, TB_Y) && tb_map(&mk.ky, ky32, P, TB_X, TB_Y + 1) &&
+                tb_map(&mk.kz, kz32, P, TB_X, TB_Y) && tb_map(&mk.R, Rin, P, TB_X, TB_Y);
         for (int q = 0; q < 4 && pairs; ++q)
-            pairs = tb_map(&mapD[q], Dbuf[q], P, TB_Y + 2) && tb_map(&mapP[q], Dbuf[q], P, TB_Y);
+            pairs = tb_map(&mapD[q], Dbuf[q], P, TB_WD, TB_Y + 2) && tb_map(&mapP[q], Dbuf[q], P, TB_X, TB_Y);
     }
     if (pairs) {
         static_assert(kTbSmem <= 227 * 1024, "staging ring exceeds the shared memory of a CTA");
