@@ -232,12 +232,14 @@ __global__ void __launch_bounds__(HT3D_MIX_BS, HT3D_MIX_MINB) k_mixed_inner(cons
 // owns a column tile of TB_X x TB_Y cells (its "halo tile"): warp w is row
 // y0 + w, lane l the quad of cells x0 + 4l .. x0 + 4l + 3, as in
 // k_mixed_inner.  Marching through a chunk of zchunk planes it computes
-//   A: iteration n on every cell of the halo tile, plane p;
-//   B: iteration n+1 on the inner cells (lanes 1..30, warps 1..TB_Y-2) of
+//   A: iteration n on every cell of the tile and on one cell past each end
+//      of its rows (lane 0 the cell x0 - 1, lane 31 the cell x0 + TB_X),
+//      plane p;
+//   B: iteration n+1 on the cells of the inner rows (warps 1..TB_Y-2) of
 //      plane p-1 from D' of planes p-2 (registers), p-1 (own quad in
-//      registers, x-neighbours by warp shuffles, y-neighbours from shared
-//      memory) and p (registers).
-// Halo cells (one quad in x, one row in y, one plane before and after the
+//      registers, x-neighbours by warp shuffles or the end cells,
+//      y-neighbours from shared memory) and p (registers).
+// Halo cells (one cell in x, one row in y, one plane before and after the
 // chunk) are computed by both neighbouring CTAs.  Every field is read once
 // per pass and D', D'' are written once each (the next pass needs both: D''
 // and its previous correction D'); both go to buffers the pass does not
@@ -250,8 +252,8 @@ __global__ void __launch_bounds__(HT3D_MIX_BS, HT3D_MIX_MINB) k_mixed_inner(cons
 // The inputs of plane p (D over the tile plus one ring, kx, ky, kz, Rin,
 // Dprev) are brought into shared memory by TMA tensor copies (one thread
 // issues six 3-D box loads per plane, completing on the plane's mbarrier) two
-// planes ahead, in a ring of TB_STAGES planes.  Boxes start on 4-float
-// boundaries (TMA wants 16-byte aligned x: x0 is a multiple of 4); elements
+// planes ahead, in a ring of TB_STAGES planes.  Every box covers columns
+// x0 - 4 .. x0 + TB_X + 3 (TMA wants 16-byte aligned x: x0 is a multiple of 4); elements
 // outside the arrays are zero-filled.  Every thread reads its quads with
 // 16-byte shared loads.  Every mbarrier wait is bounded: on timeout the CTA
 // records HT3D_ERR_TIMEOUT in *err, waits (bounded) for its copies in flight
@@ -261,27 +263,30 @@ __global__ void __launch_bounds__(HT3D_MIX_BS, HT3D_MIX_MINB) k_mixed_inner(cons
 #define HT3D_TB_Y 16
 #endif
 constexpr int TB_LANES = 32, TB_X = 4 * TB_LANES, TB_Y = HT3D_TB_Y, TB_STAGES = 3;
-constexpr int TB_OX = TB_X - 8, TB_OY = TB_Y - 2;  // cells of a tile that iteration B updates
-constexpr int TB_WD = TB_X + 8;                    // D box: x0 - 4 .. x0 + TB_X + 3
-constexpr int TB_WK = TB_X + 4;                    // kx box: x0 .. x0 + TB_X + 3 (east face of the last quad)
+constexpr int TB_OX = TB_X, TB_OY = TB_Y - 2;  // cells of a tile that iteration B updates
+constexpr int TB_W = TB_X + 8;                 // every box: columns x0 - 4 .. x0 + TB_X + 3
 constexpr unsigned kTbWaitLimit = 1u << 22;
 
 struct __align__(128) TbStage {
-    float D[TB_Y + 2][TB_WD];   // rows y0-1 .. y0+TB_Y, columns x0-4 ..
-    float pad0[(128 - ((TB_Y + 2) * TB_WD * 4) % 128) % 128 / 4];
-    float kx[TB_Y][TB_WK];      // rows y0 .. y0+TB_Y-1, columns x0 ..
-    float pad1[(128 - (TB_Y * TB_WK * 4) % 128) % 128 / 4];
-    float ky[TB_Y + 1][TB_X];   // rows y0 .. y0+TB_Y
-    float kz[TB_Y][TB_X];
-    float R[TB_Y][TB_X];
-    float Dp[TB_Y][TB_X];       // previous correction
+    float D[TB_Y + 2][TB_W];    // rows y0-1 .. y0+TB_Y
+    float pad0[(128 - ((TB_Y + 2) * TB_W * 4) % 128) % 128 / 4];
+    float kx[TB_Y][TB_W];       // rows y0 .. y0+TB_Y-1
+    float pad1[(128 - (TB_Y * TB_W * 4) % 128) % 128 / 4];
+    float ky[TB_Y + 1][TB_W];   // rows y0 .. y0+TB_Y
+    float pad2[(128 - ((TB_Y + 1) * TB_W * 4) % 128) % 128 / 4];
+    float kz[TB_Y][TB_W];
+    float pad3[(128 - (TB_Y * TB_W * 4) % 128) % 128 / 4];
+    float R[TB_Y][TB_W];
+    float pad4[(128 - (TB_Y * TB_W * 4) % 128) % 128 / 4];
+    float Dp[TB_Y][TB_W];       // previous correction
+    float pad5[(128 - (TB_Y * TB_W * 4) % 128) % 128 / 4];
 };
-constexpr unsigned kTbStageBytes = 4u * ((TB_Y + 2) * TB_WD + TB_Y * TB_WK + (TB_Y + 1) * TB_X + 3 * TB_Y * TB_X);
+constexpr unsigned kTbStageBytes = 4u * TB_W * ((TB_Y + 2) + TB_Y + (TB_Y + 1) + 3 * TB_Y);
 static_assert(offsetof(TbStage, kx) % 128 == 0 && offsetof(TbStage, ky) % 128 == 0 &&
                   offsetof(TbStage, kz) % 128 == 0 && offsetof(TbStage, R) % 128 == 0 &&
                   offsetof(TbStage, Dp) % 128 == 0 && sizeof(TbStage) % 128 == 0,
               "TMA destinations must be 128-byte aligned");
-static_assert((TB_WD * 4) % 16 == 0 && (TB_WK * 4) % 16 == 0 && TB_WD <= 256 && TB_WK <= 256,
+static_assert((TB_W * 4) % 16 == 0 && TB_W <= 256,
               "TMA box rows must be whole 16-byte units of at most 256 elements");
 
 struct TbMaps {  // tensor maps of one pass (by value, in the constant bank)
@@ -352,6 +357,25 @@ __device__ __forceinline__ void pair_quad(const QuadIn& c, float4 xp, float dW, 
     fout = make_float4(of[0], of[1], of[2], of[3]);
 }
 
+// One iteration on one cell (the end cells of a tile's rows), with the ghost
+// rules of mixed_quad; sh points at the cell in a stage's D tile.
+__device__ __forceinline__ float pair_cell(const float* d, const float* kxr, const float* kyr, float kB, float kF,
+                                           float r, float xp, float xb, float xf, int i, int j, int k, const Pad& p,
+                                           const BC6<float>& bc, const MixScal& s, float _dx2, float _dy2,
+                                           float _dz2) {
+    const float xc = d[0];
+    const float xw = (i == 0) ? ghost(bc, 0, xc) : d[-1];
+    const float xe = (i == p.nx - 1) ? ghost(bc, 1, xc) : d[1];
+    const float xs = (j > 0) ? d[-TB_W] : ghost(bc, 2, xc);
+    const float xn = (j < p.ny - 1) ? d[TB_W] : ghost(bc, 3, xc);
+    const float xbb = (k > 0) ? xb : ghost(bc, 4, xc);
+    const float xff = (k < p.nz - 1) ? xf : ghost(bc, 5, xc);
+    float f, x;
+    mixed_cell(xc, xw, xe, xs, xn, xbb, xff, kxr[0], kxr[1], kyr[0], kyr[TB_W], kB, kF, r, xp, s.mom, s.dh2, s.cX,
+               s._dx, s._dy, s._dz, _dx2, _dy2, _dz2, f, x);
+    return x;
+}
+
 template <bool STOREF>
 __global__ void __launch_bounds__(TB_LANES* TB_Y, TB_Y <= 8 ? 2 : 1) k_mixed_inner2(const __grid_constant__ TbMaps maps,
                                                                     const float* __restrict__ Din,
@@ -367,30 +391,33 @@ __global__ void __launch_bounds__(TB_LANES* TB_Y, TB_Y <= 8 ? 2 : 1) k_mixed_inn
     uint64_t* bar = reinterpret_cast<uint64_t*>(base + sizeof(TbStage) * TB_STAGES + sizeof(float) * 3 * TB_Y * TB_X);
     __shared__ int abort_flag;
     const int lane = threadIdx.x, ty = threadIdx.y, tid = lane + TB_LANES * ty;
-    const int x0 = blockIdx.x * TB_OX - 4, y0 = blockIdx.y * TB_OY - 1;  // halo tile origin (x0 % 4 == 0)
+    const int x0 = blockIdx.x * TB_OX, y0 = blockIdx.y * TB_OY - 1;  // tile origin (x0 % 4 == 0)
     const int i0 = x0 + 4 * lane, j = y0 + ty;
-    const bool rowin = j >= 0 && j < p.PY && i0 >= 0 && i0 < p.PX;  // quad inside the padded array
-    const bool inner = i0 >= 0 && i0 < p.nx && j >= 0 && j < p.ny && lane >= 1 && lane <= TB_LANES - 2 &&
-                       ty >= 1 && ty <= TB_Y - 2;
+    const bool rowin = j >= 0 && j < p.PY && i0 < p.PX;  // quad inside the padded array
+    const bool inner = i0 < p.nx && j >= 0 && j < p.ny && ty >= 1 && ty <= TB_Y - 2;
+    // end cells: lane 0 computes x0 - 1, lane 31 x0 + TB_X (iteration A only)
+    const bool endc = lane == 0 || lane == TB_LANES - 1;
+    const int ie = lane == 0 ? x0 - 1 : x0 + TB_X;
+    const int ce = lane == 0 ? 3 : TB_X + 4;  // its column in the boxes
     const int k0 = blockIdx.z * zchunk, k1 = min(p.nz, k0 + zchunk);
     const int pa0 = max(k0 - 1, 0);
     const int plast = min(k1 + 1, p.nz);  // last staged plane (plane nz: its bottom z-faces)
     const float _dx2 = __fmul_rn(s._dx, s._dx), _dy2 = __fmul_rn(s._dy, s._dy), _dz2 = __fmul_rn(s._dz, s._dz);
     // this thread's offsets inside a stage (fixed over planes)
-    const int oD = (ty + 1) * TB_WD + 4 + 4 * lane;  // D, quad centre
-    const int oK = ty * TB_WK + 4 * lane;            // kx
-    const int oC = ty * TB_X + 4 * lane;             // ky (south), kz, R, Dp, and the A-result planes
+    const int oD = (ty + 1) * TB_W + 4 + 4 * lane;  // D, quad centre
+    const int oK = ty * TB_W + 4 + 4 * lane;        // kx, ky (south), kz, R, Dp
+    const int oC = ty * TB_X + 4 * lane;            // the A-result planes
     auto issue = [&](int k) {  // thread 0: the six boxes of plane k into slot k % TB_STAGES
         if (k == skip_plane) return;  // HT3D_TUNE_WAIT_TEST only: never issued, its wait runs out
         TbStage& S = st[k % TB_STAGES];
         uint64_t* b = &bar[k % TB_STAGES];
         mbar_expect_tx(b, kTbStageBytes);
         tma_load3(&S.D[0][0], &maps.D, x0 - 4, y0 - 1, k, b);
-        tma_load3(&S.kx[0][0], &maps.kx, x0, y0, k, b);
-        tma_load3(&S.ky[0][0], &maps.ky, x0, y0, k, b);
-        tma_load3(&S.kz[0][0], &maps.kz, x0, y0, k, b);
-        tma_load3(&S.R[0][0], &maps.R, x0, y0, k, b);
-        tma_load3(&S.Dp[0][0], &maps.Dp, x0, y0, k, b);
+        tma_load3(&S.kx[0][0], &maps.kx, x0 - 4, y0, k, b);
+        tma_load3(&S.ky[0][0], &maps.ky, x0 - 4, y0, k, b);
+        tma_load3(&S.kz[0][0], &maps.kz, x0 - 4, y0, k, b);
+        tma_load3(&S.R[0][0], &maps.R, x0 - 4, y0, k, b);
+        tma_load3(&S.Dp[0][0], &maps.Dp, x0 - 4, y0, k, b);
     };
     if (tid == 0) {
         abort_flag = 0;
@@ -418,6 +445,10 @@ __global__ void __launch_bounds__(TB_LANES* TB_Y, TB_Y <= 8 ? 2 : 1) k_mixed_inn
     float* outF = F + colo + p.plane * (long long)(pa0 - 1);
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
     float4 dm1 = (pa0 > 0 && rowin) ? *reinterpret_cast<const float4*>(Din + p.plane * (pa0 - 1) + colo) : z4;
+    // the end cell's D at the plane before, and its A result at the plane before
+    const bool endin = endc && j >= 0 && j < p.PY && ie >= 0 && ie < p.PX;
+    float em1 = (pa0 > 0 && endin) ? Din[p.plane * (pa0 - 1) + ie + (long long)p.PX * j] : 0.f;
+    float ec = 0.f;
     float4 dpm = z4, dpc = z4;  // A's result at planes pl - 2 and pl - 1
     QuadIn cb{};                // A's inputs at plane pl - 1 (B's coefficients)
     for (int pl = pa0; pl <= k1; ++pl) {
@@ -455,18 +486,27 @@ __global__ void __launch_bounds__(TB_LANES* TB_Y, TB_Y <= 8 ? 2 : 1) k_mixed_inn
             ca.xc = lds4(d0);
             ca.kW = lds4(&S0->kx[0][0] + oK);
             ca.kE3 = (&S0->kx[0][0])[oK + 4];
-            ca.kS = lds4(&S0->ky[0][0] + oC);
-            ca.kN = lds4(&S0->ky[0][0] + oC + TB_X);
-            ca.kB = lds4(&S0->kz[0][0] + oC);
-            ca.kF = lds4(&S1->kz[0][0] + oC);
-            ca.r = lds4(&S0->R[0][0] + oC);
-            const float4 xp = lds4(&S0->Dp[0][0] + oC);
-            const float4 xs4 = lds4(d0 - TB_WD), xn4 = lds4(d0 + TB_WD);
+            ca.kS = lds4(&S0->ky[0][0] + oK);
+            ca.kN = lds4(&S0->ky[0][0] + oK + TB_W);
+            ca.kB = lds4(&S0->kz[0][0] + oK);
+            ca.kF = lds4(&S1->kz[0][0] + oK);
+            ca.r = lds4(&S0->R[0][0] + oK);
+            const float4 xp = lds4(&S0->Dp[0][0] + oK);
+            const float4 xs4 = lds4(d0 - TB_W), xn4 = lds4(d0 + TB_W);
             const float4 xf4 = lds4(&S1->D[0][0] + oD);
             float4 fa;
             pair_quad(ca, xp, d0[-1], d0[4], xs4, xn4, dm1, xf4, i0, j, pl, p, bc, s, _dx2, _dy2, _dz2, da, fa);
             dm1 = ca.xc;
             *reinterpret_cast<float4*>(xw_) = da;
+        }
+        float ea = 0.f;  // the end cell's A result at plane pl
+        if (ok && pl < p.nz && endc) {
+            const int oe = ty * TB_W + ce;
+            const float* de = &S0->D[0][0] + (ty + 1) * TB_W + ce;
+            ea = pair_cell(de, &S0->kx[0][0] + oe, &S0->ky[0][0] + oe, (&S0->kz[0][0])[oe], (&S1->kz[0][0])[oe],
+                           (&S0->R[0][0])[oe], (&S0->Dp[0][0])[oe], em1, (&S1->D[0][0])[(ty + 1) * TB_W + ce], ie, j,
+                           pl, p, bc, s, _dx2, _dy2, _dz2);
+            em1 = de[0];
         }
         __syncthreads();
         if (abort_flag) {  // a wait gave up: every thread leaves here
@@ -481,8 +521,10 @@ __global__ void __launch_bounds__(TB_LANES* TB_Y, TB_Y <= 8 ? 2 : 1) k_mixed_inn
         }
         // ---- B: iteration n+1 at plane pl - 1 on the inner quads
         // every lane takes part in the shuffles
-        const float bW = __shfl_up_sync(0xffffffffu, dpc.w, 1);
-        const float bE = __shfl_down_sync(0xffffffffu, dpc.x, 1);
+        float bW = __shfl_up_sync(0xffffffffu, dpc.w, 1);
+        float bE = __shfl_down_sync(0xffffffffu, dpc.x, 1);
+        if (lane == 0) bW = ec;
+        if (lane == TB_LANES - 1) bE = ec;
         if (pl - 1 >= k0 && inner) {
             const int q = pl - 1;
             QuadIn c = cb;
@@ -500,6 +542,7 @@ __global__ void __launch_bounds__(TB_LANES* TB_Y, TB_Y <= 8 ? 2 : 1) k_mixed_inn
         outF += p.plane;
         dpm = dpc;
         dpc = da;
+        ec = ea;
         cb = ca;
         const TbStage* t = S0;
         S0 = S1;
@@ -846,10 +889,10 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
     CUtensorMap mapD[4], mapP[4];    // each correction buffer as a pass's D (with its ring) and as its Dprev
     int* derr = nullptr;
     if (pairs) {
-        pairs = tb_map(&mk.kx, kx32, P, TB_WK, TB_Y) && tb_map(&mk.ky, ky32, P, TB_X, TB_Y + 1) &&
-                tb_map(&mk.kz, kz32, P, TB_X, TB_Y) && tb_map(&mk.R, Rin, P, TB_X, TB_Y);
+        pairs = tb_map(&mk.kx, kx32, P, TB_W, TB_Y) && tb_map(&mk.ky, ky32, P, TB_W, TB_Y + 1) &&
+                tb_map(&mk.kz, kz32, P, TB_W, TB_Y) && tb_map(&mk.R, Rin, P, TB_W, TB_Y);
         for (int q = 0; q < 4 && pairs; ++q)
-            pairs = tb_map(&mapD[q], Dbuf[q], P, TB_WD, TB_Y + 2) && tb_map(&mapP[q], Dbuf[q], P, TB_X, TB_Y);
+            pairs = tb_map(&mapD[q], Dbuf[q], P, TB_W, TB_Y + 2) && tb_map(&mapP[q], Dbuf[q], P, TB_W, TB_Y);
     }
     if (pairs) {
         static_assert(kTbSmem <= 227 * 1024, "staging ring exceeds the shared memory of a CTA");

@@ -259,14 +259,15 @@ def test_mixed_fixed_iterations_track_fp64(ctx, orc, n, bc, niter):
 
 
 @pytest.mark.parametrize("n", [(1, 1, 1), (2, 3, 2), (5, 4, 3), (30, 14, 9), (31, 15, 40), (64, 29, 33), (95, 47, 70),
-                               (121, 15, 4), (130, 29, 6), (255, 16, 3)])
+                               (128, 15, 4), (129, 15, 3), (130, 29, 6), (255, 16, 3), (257, 17, 3)])
 @pytest.mark.parametrize("niter,refresh", [(40, 8), (37, 8), (25, 256), (100, 16)])
 @pytest.mark.parametrize("zchunk", [1, 2, 7])
 def test_mixed_temporal_blocking_is_bit_identical(ctx, n, niter, refresh, zchunk):
     """k_mixed_inner2 (two iterations per pass through memory, with halo
     recomputation across tiles and z-chunks) gives bit for bit the result of
     one k_mixed_inner launch per iteration: X, F, F0 and the check sums.
-    Sizes cover one to three tiles of 120 cells in x and of 14 rows in y."""
+    Sizes cover one to three tiles of 128 cells in x (and a last tile of one
+    cell) and of 14 rows in y."""
     nx, ny, nz = n
     X, R, k = problem(n, seed=37)
     types, vals = BCS["mixedbc"]
