@@ -44,7 +44,7 @@ struct ht3d_ctx {
     int sync_each_call = 1;
     int dyrel_variant = 0;                // thread layout of the fused DYREL iteration (0 = per precision)
     int mixed_refresh = 512;              // FP64 defect-correction cadence of the mixed solver
-    int mixed_temporal = 0;               // mixed form: two inner iterations per pass (>= 2: z-chunk)
+    int mixed_temporal = 1;               // mixed form: two inner iterations per pass (>= 2: z-chunk)
     int wait_test = 0;                    // > 0: the next pass skips plane wait_test - 1 (bounded-wait test)
     int time_inner = 0;                   // time the mixed solver's inner-iteration runs
     std::vector<cudaEvent_t> events;      // event pool of the inner-iteration timer

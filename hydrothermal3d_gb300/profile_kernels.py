@@ -8,7 +8,8 @@ Kernels: weno_f32 (one FP32 WENO5 sweep in a curl velocity),
 dyrel_f32 (FP32 pseudo-iteration on the reference layout),
 dyrel_f64 (plain FP64 pseudo-iteration), mixed_solve (a mixed-form DYREL
 solve of --iters pseudo-iterations: two FP64 checks, then the padded FP32
-inner kernel k_mixed_inner), weno_f64 / weno_mixed (one fused WENO5
+inner iterations, two per pass in k_mixed_inner2, or one per launch in
+k_mixed_inner with --tune 6=0), weno_f64 / weno_mixed (one fused WENO5
 advection), post (one fused pass of the twelve output diagnostics, k_post),
 dim_step (one dimensional v18 time step, it = 0, with --iters pseudo-iterations
 per solve: k_dim_iter thermal then Darcy).
@@ -85,7 +86,9 @@ def main():
         ms, nl = ctx.inner_timing(reset=True)
         t = ms / 1e3 / max(1, nl)
         alg = hrl.bytes_per_iteration(n, n, n, 4)
-        print(json.dumps({"kernel": "k_mixed_inner", "n": n, "tune": a.tune, "inner_iterations": nl,
+        single = any(kv.replace(" ", "") == f"{abi.TUNE_TEMPORAL}=0" for kv in a.tune)
+        print(json.dumps({"kernel": "k_mixed_inner" if single else "k_mixed_inner2 (two iterations per pass)",
+                          "n": n, "tune": a.tune, "inner_iterations": nl,
                           "us_per_iteration": t * 1e6, "alg_GBs": alg / t / 1e9}))
     elif a.kernel == "ensemble":
         from hydrothermal3d_gb300 import api

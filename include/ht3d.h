@@ -73,13 +73,12 @@ extern "C" {
                                        0 = autotune on first use (64/128/256), or fixed   */
 #define HT3D_TUNE_ENS_GRAPH 5       /* 1 (default): replay windows of 16 batched inner
                                        iterations as CUDA graphs; 0: launch one by one    */
-#define HT3D_TUNE_TEMPORAL 6        /* mixed form: 0 (default) = one FP32 inner iteration per
-                                       launch; 1 = two per pass through memory (temporal
-                                       blocking, z-chunk chosen per grid), >= 2 = the same
-                                       with that many planes per chunk; bit-identical
-                                       results (on GB300 the two-iteration pass, TMA-staged,
-                                       is still instruction-issue bound and slower: 94
-                                       vs 76 us per iteration at 255^3)                  */
+#define HT3D_TUNE_TEMPORAL 6        /* mixed form: 0 = one FP32 inner iteration per launch;
+                                       1 (default) = two per pass through memory (temporal
+                                       blocking, TMA-staged planes, z-chunk chosen per grid),
+                                       >= 2 = the same with that many planes per chunk;
+                                       bit-identical results (255^3: 59.6 against 75.8 us
+                                       per iteration)                                    */
 #define HT3D_TUNE_WAIT_TEST 7       /* test hook of the bounded waits: v > 0 makes the next
                                        two-iteration pass (HT3D_TUNE_TEMPORAL) skip the
                                        copies of plane v - 1 and give up after 4096 polls;

@@ -283,7 +283,7 @@ def test_mixed_temporal_blocking_is_bit_identical(ctx, n, niter, refresh, zchunk
                                          vals, prm, Fd, F0d, abi.MIXED, n_iter_fixed=niter)
             out.append((ht.to_numpy(Xd), ht.to_numpy(Fd), ht.to_numpy(F0d), st.nF_abs, st.lambda_min, st.iters))
     finally:
-        ctx.set_tuning(abi.TUNE_TEMPORAL, 0)
+        ctx.set_tuning(abi.TUNE_TEMPORAL, 1)
         ctx.set_tuning(abi.TUNE_MIXED_REFRESH, 512)
     a, b = out
     m = no_edges_mask(X.shape)
@@ -322,7 +322,7 @@ def test_bounded_wait_runs_out_and_context_recovers(ctx):
         single = solve()
     finally:
         ctx.set_tuning(abi.TUNE_WAIT_TEST, 0)
-        ctx.set_tuning(abi.TUNE_TEMPORAL, 0)
+        ctx.set_tuning(abi.TUNE_TEMPORAL, 1)
     m = no_edges_mask(X.shape)
     np.testing.assert_array_equal(paired[0][m], single[0][m])
     np.testing.assert_array_equal(paired[1], single[1])
