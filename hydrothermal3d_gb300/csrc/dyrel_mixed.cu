@@ -830,7 +830,13 @@ int ht3d_dyrel_solve_mixed(ht3d_ctx* ctx, double* X, const double* R, const doub
     double* X2 = (double*)ht3d_scratch(ctx, SLOT_X2, sizeof(double) * nex);
     // correction buffers: the current D and its previous correction, plus two
     // more for the two-iteration passes (which write neither buffer they read)
-    const bool want_pairs = ctx->mixed_temporal != 0;
+    // two iterations per pass: always for an explicit z-chunk (>= 2); by default
+    // (1) where the pass pays: grids of 2^21 cells or more whose x extent fills
+    // its 128-cell tiles to 3/4 or more (smaller grids run faster one iteration
+    // per launch: the pass's tiles would be mostly empty and its set-up is per solve)
+    const int tiles_x = (nx + 127) / 128;
+    const bool want_pairs = ctx->mixed_temporal >= 2 ||
+                            (ctx->mixed_temporal == 1 && n >= (1LL << 21) && 4LL * nx >= 3LL * 128 * tiles_x);
     float* Dbuf[4] = {(float*)ht3d_scratch(ctx, SLOT_F32_X, pbytes), (float*)ht3d_scratch(ctx, SLOT_F32_X2, pbytes),
                       want_pairs ? (float*)ht3d_scratch(ctx, SLOT_F32_D3, pbytes) : nullptr,
                       want_pairs ? (float*)ht3d_scratch(ctx, SLOT_F32_D4, pbytes) : nullptr};

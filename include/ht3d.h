@@ -75,8 +75,10 @@ extern "C" {
                                        iterations as CUDA graphs; 0: launch one by one    */
 #define HT3D_TUNE_TEMPORAL 6        /* mixed form: 0 = one FP32 inner iteration per launch;
                                        1 (default) = two per pass through memory (temporal
-                                       blocking, TMA-staged planes, z-chunk chosen per grid),
-                                       >= 2 = the same with that many planes per chunk;
+                                       blocking, TMA-staged planes, z-chunk chosen per grid)
+                                       on grids of >= 2^21 cells whose x extent fills 128-cell
+                                       tiles to >= 3/4, one per launch otherwise; >= 2 = two
+                                       per pass on every grid, that many planes per chunk;
                                        bit-identical results (255^3: 59.6 against 75.8 us
                                        per iteration)                                    */
 #define HT3D_TUNE_WAIT_TEST 7       /* test hook of the bounded waits: v > 0 makes the next

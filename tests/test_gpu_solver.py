@@ -261,7 +261,7 @@ def test_mixed_fixed_iterations_track_fp64(ctx, orc, n, bc, niter):
 @pytest.mark.parametrize("n", [(1, 1, 1), (2, 3, 2), (5, 4, 3), (30, 14, 9), (31, 15, 40), (64, 29, 33), (95, 47, 70),
                                (128, 15, 4), (129, 15, 3), (130, 29, 6), (255, 16, 3), (257, 17, 3)])
 @pytest.mark.parametrize("niter,refresh", [(40, 8), (37, 8), (25, 256), (100, 16)])
-@pytest.mark.parametrize("zchunk", [1, 2, 7])
+@pytest.mark.parametrize("zchunk", [2, 7, 64])
 def test_mixed_temporal_blocking_is_bit_identical(ctx, n, niter, refresh, zchunk):
     """k_mixed_inner2 (two iterations per pass through memory, with halo
     recomputation across tiles and z-chunks) gives bit for bit the result of
@@ -312,7 +312,7 @@ def test_bounded_wait_runs_out_and_context_recovers(ctx):
         return ht.to_numpy(Xd), ht.to_numpy(Fd), ht.to_numpy(F0d)
 
     try:
-        ctx.set_tuning(abi.TUNE_TEMPORAL, 1)
+        ctx.set_tuning(abi.TUNE_TEMPORAL, 3)
         ctx.set_tuning(abi.TUNE_WAIT_TEST, 2)
         with pytest.raises(api.Ht3dError) as e:
             solve()
