@@ -37,7 +37,9 @@ __device__ __forceinline__ float weno5_f32(float v1, float v2, float v3, float v
     const float p1 = v1 * (1.0f / 3.0f) - (7.0f / 6.0f) * v2 + (11.0f / 6.0f) * v3;
     const float p2 = -v2 * (1.0f / 6.0f) + (5.0f / 6.0f) * v3 + v4 * (1.0f / 3.0f);
     const float p3 = v3 * (1.0f / 3.0f) + (5.0f / 6.0f) * v4 - v5 * (1.0f / 6.0f);
-    const float maxV = fmaxf(fmaxf(fmaxf(fmaxf(v1 * v1, v2 * v2), v3 * v3), v4 * v4), v5 * v5);
+    // max of the squares = square of the largest magnitude (rounding is monotonic)
+    const float vm = fmaxf(fmaxf(fmaxf(fmaxf(fabsf(v1), fabsf(v2)), fabsf(v3)), fabsf(v4)), fabsf(v5));
+    const float maxV = vm * vm;
     const float e = 1e-18f + 1e-6f * maxV;
     const float a1 = v1 - 2.0f * v2 + v3, b1 = v1 - 4.0f * v2 + 3.0f * v3;
     const float a2 = v2 - 2.0f * v3 + v4, b2 = v2 - v4;

@@ -27,6 +27,20 @@ __device__ __forceinline__ float weno_point_f32(float x0, float x1, float x2, fl
     return x3 - dt * (Vp * dFm + Vm * dFp);
 }
 
+// The same point from its six one-sided differences d[o] = h (x[o+1] - x[o])
+// (the march kernels keep them in a window: one new difference per point);
+// x2, x5 only for the v2 stencil quirk, x3 the point itself.
+template <int QUIRK>
+__device__ __forceinline__ float weno_point_f32_d(const float (&d)[6], float x2, float x3, float x5, float a, float b,
+                                                  float dt, float h) {
+    const float Vm = a < 0.0f ? a : 0.0f;
+    const float Vp = b >= 0.0f ? b : 0.0f;
+    const float m5 = QUIRK ? h * (x5 - x2) : d[4];
+    const float dFm = upwind_active(Vp) ? weno5_f32(d[0], d[1], d[2], d[3], m5) : 0.0f;
+    const float dFp = upwind_active(Vm) ? weno5_f32(d[5], d[4], d[3], d[2], d[1]) : 0.0f;
+    return x3 - dt * (Vp * dFm + Vm * dFp);
+}
+
 // ghost value at position p (< 0 or >= n) from its mirror value v
 __device__ __forceinline__ float weno_ghost(float v, bool left, const WenoBC& bc) {
     const int t = left ? bc.typeL : bc.typeR;
@@ -171,12 +185,18 @@ __global__ void __launch_bounds__(128) k_weno_march_f32(const float* __restrict_
     }
 #pragma unroll
     for (int q = 0; q < 5; ++q) v[q] = c0 + q <= n ? vline[(long long)(c0 + q) * vs] : 0.f;
+    // difference windows: dw0[q] = h (w0[q+1] - w0[q]); dw1 likewise for w1[0..5]
+    float dw0[6], dw1[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) dw0[q] = h * (w0[q + 1] - w0[q]);
+#pragma unroll
+    for (int q = 0; q < 5; ++q) dw1[q] = h * (w1[q + 1] - w1[q]);
 #pragma unroll 2
     for (int c = c0; c < c1; ++c) {
         const int p = c + 3;  // T1 position entering the window
         float head;
         if (p < n) {
-            head = weno_point_f32<QUIRK>(w0[0], w0[1], w0[2], w0[3], w0[4], w0[5], w0[6], v[3], v[4], dt, h);
+            head = weno_point_f32_d<QUIRK>(dw0, w0[2], w0[3], w0[5], v[3], v[4], dt, h);
         } else {
             // mirror 2n-1-p of T1 is in the window: w1[q] holds T1[c-3+q]
             const int q = 2 * n - 1 - p - (c - 3);
@@ -187,13 +207,19 @@ __global__ void __launch_bounds__(128) k_weno_march_f32(const float* __restrict_
             head = weno_ghost(m, false, bc);
         }
         w1[6] = head;
-        const float t = weno_point_f32<QUIRK>(w1[0], w1[1], w1[2], w1[3], w1[4], w1[5], w1[6], v[0], v[1], dt, h);
+        dw1[5] = h * (head - w1[5]);
+        const float t = weno_point_f32_d<QUIRK>(dw1, w1[2], w1[3], w1[5], v[0], v[1], dt, h);
         out[(long long)c * stride] = 0.5f * t + 0.5f * w0[0];
 #pragma unroll
         for (int q = 0; q < 6; ++q) w1[q] = w1[q + 1];
 #pragma unroll
+        for (int q = 0; q < 5; ++q) dw1[q] = dw1[q + 1];
+#pragma unroll
         for (int q = 0; q < 6; ++q) w0[q] = w0[q + 1];
         w0[6] = (c + 4 < n) ? line_at<float>(line, stride, c + 7, n, bc) : 0.f;
+#pragma unroll
+        for (int q = 0; q < 5; ++q) dw0[q] = dw0[q + 1];
+        dw0[5] = h * (w0[6] - w0[5]);
 #pragma unroll
         for (int q = 0; q < 4; ++q) v[q] = v[q + 1];
         v[4] = (c + 5 <= n) ? vline[(long long)(c + 5) * vs] : 0.f;
