@@ -2,10 +2,11 @@
 // dimension-split sweep as ht3d_weno5_advect (tools/Weno5_Routines.jl /
 // tools/Weno5_Routines_v2.jl) on float fields, for the standalone sweep of
 // the large-grid workload.  The epsilon floor of the weights is 1e-18 instead
-// of 1e-99 (see weno5_f32).  Both stages of an axis run in one kernel (rows in
-// shared memory along x, register windows marching along y and z), so every
-// axis reads T and V once and writes T once; periodic y/z axes use one launch
-// per stage.
+// of 1e-99 (see weno5_f32).  Both stages of an axis run in one kernel: every
+// thread marches along a segment of a line (register streams, below), along
+// y and z straight from HBM with threads consecutive in x, along x over rows
+// that a warp stages in shared memory.  Every axis reads T and V once and
+// writes T once; periodic axes use the per-point kernels.
 #include "weno_core.cuh"
 
 namespace {
@@ -27,57 +28,456 @@ __device__ __forceinline__ float weno_point_f32(float x0, float x1, float x2, fl
     return x3 - dt * (Vp * dFm + Vm * dFp);
 }
 
-// The same point from its six one-sided differences d[o] = h (x[o+1] - x[o])
-// (the march kernels keep them in a window: one new difference per point);
-// x2, x5 only for the v2 stencil quirk, x3 the point itself.
-template <int QUIRK>
-__device__ __forceinline__ float weno_point_f32_d(const float (&d)[6], float x2, float x3, float x5, float a, float b,
-                                                  float dt, float h) {
-    const float Vm = a < 0.0f ? a : 0.0f;
-    const float Vp = b >= 0.0f ? b : 0.0f;
-    const float m5 = QUIRK ? h * (x5 - x2) : d[4];
-    const float dFm = upwind_active(Vp) ? weno5_f32(d[0], d[1], d[2], d[3], m5) : 0.0f;
-    const float dFp = upwind_active(Vm) ? weno5_f32(d[5], d[4], d[3], d[2], d[1]) : 0.0f;
-    return x3 - dt * (Vp * dFm + Vm * dFp);
-}
-
 // ghost value at position p (< 0 or >= n) from its mirror value v
 __device__ __forceinline__ float weno_ghost(float v, bool left, const WenoBC& bc) {
     const int t = left ? bc.typeL : bc.typeR;
     return t == HT3D_BC_DIRICHLET ? (float)(2 * (left ? bc.valL : bc.valR)) - v : v;
 }
 
-// Unfused stage (any BC, incl. periodic): one launch per stage and axis.
-template <int AXIS, int QUIRK, int STAGE>
-__global__ void __launch_bounds__(256) k_weno_stage_f32(const float* __restrict__ src, float* dst, const float* T0,
-                                                        const float* __restrict__ V, float dt, float h, WenoBC bc,
-                                                        int nx, int ny, int nz) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z;
-    if (i >= nx || j >= ny || k >= nz) return;
-    const int n1 = nx + 2, n2 = ny + 2;
-    const long long e = (i + 1) + (long long)n1 * ((j + 1) + (long long)n2 * (k + 1));
-    const int idx = AXIS == 0 ? i : (AXIS == 1 ? j : k);
-    const int n = AXIS == 0 ? nx : (AXIS == 1 ? ny : nz);
-    const long long stride = AXIS == 0 ? 1 : (AXIS == 1 ? (long long)n1 : (long long)n1 * n2);
-    const float* line = src + e - (long long)idx * stride;
-    float x[7];
+// --------------------------------------------------------------- streams
+// A stream is the rolling state of one SSP-RK2 stage marching along a line:
+// init() takes x_{i-3} .. x_{i+2} for the first point i, step() takes
+// x_{i+3} and the velocities of the faces i (left) and i+1 (right), returns
+// the stage value at i and advances to i+1.
+
+// Face-shared form (WENO5 v1 stencil).  With one-sided differences
+// D_j = h (x_{j+1} - x_j), every smoothness indicator of dFdx_Weno5!
+// (tools/Weno5_Routines.jl:51-66) belongs to a triple (D_{j-1}, D_j, D_{j+1})
+// with second difference a_j and spread c_j = D_{j-1} - D_{j+1}:
+//   13/12 a^2 + 1/4 (2a - c)^2 = bC + a (a - c)   (first stencil,  "bL_j")
+//   13/12 a^2 + 1/4 c^2        = bC               (central stencil, "bC_j")
+//   13/12 a^2 + 1/4 (2a + c)^2 = bC + a (a + c)   (third stencil,  "bR_j")
+// and reversing a triple swaps bL and bR, so
+//   dF-(i) uses bL_{i-2}, bC_{i-1}, bR_i   and   dF+(i) uses bR_{i+1}, bC_i, bL_{i-1}.
+// The weighted sum of the candidates is the central candidate p2 plus
+// weighted third differences (p1 - p2 and p3 - p2), and those are differences
+// of consecutive a:  g_j = a_j - a_{j-1}.  So each new face adds one triple
+// (a, c, the three indicators, g) and one five-difference maximum e, and each
+// point evaluates only its weights: the indicators are computed once per
+// face instead of once per point and side.
+struct WenoStreamShared {
+    float x[6];   // x_{i-3} .. x_{i+2}
+    float D[4];   // D_{i-2} .. D_{i+1}
+    float bl[3];  // bL_{i-2} .. bL_i
+    float bc[2];  // bC_{i-1}, bC_i
+    float br;     // bR_i
+    float g1[2];  // g_{i-1} / 3, g_i / 3
+    float g3;     // g_i / 2
+    float e;      // 1e-18 + 1e-6 max|D_{i-3} .. D_{i+1}|^2
+    float ap;     // a_i
+    float h;
+
+    __device__ __forceinline__ static float rcp(float v) {
+        float r;
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v));
+        return r;
+    }
+    // p2 + (w1 (p1 - p2) + w3 (p3 - p2)) / (w1 + w2 + w3) with w_k = d_k / s_k^2,
+    // d = (0.1, 0.6, 0.3), all weights scaled by 10: n1 = p1 - p2, n3 = 3 (p3 - p2).
+    // s >= 1e-18 keeps 1/s^2 <= 1e36 and the weight sum finite; |D| up to ~1e9
+    // keeps it above the FP32 normal range.
+    __device__ __forceinline__ static float mix(float b1, float b2, float b3, float e, float p2, float n1, float n3) {
+        const float r1 = rcp(b1 + e), r2 = rcp(b2 + e), r3 = rcp(b3 + e);
+        const float q1 = r1 * r1, q2 = r2 * r2, q3 = r3 * r3;
+        const float W = fmaf(3.0f, q3, fmaf(6.0f, q2, q1));
+        const float N = fmaf(q1, n1, q3 * n3);
+        return fmaf(N, rcp(W), p2);
+    }
+    __device__ __forceinline__ static void triple(float Dm, float D0, float Dp, float& a, float& L, float& C,
+                                                  float& R) {
+        a = fmaf(-2.0f, D0, Dm) + Dp;
+        const float c = Dm - Dp;
+        C = fmaf(0.25f * c, c, (13.0f / 12.0f) * a * a);
+        L = fmaf(a, a - c, C);
+        R = fmaf(a, a + c, C);
+    }
+    __device__ __forceinline__ static float floor5(float d0, float d1, float d2, float d3, float d4) {
+        const float m = fmaxf(fmaxf(fmaxf(fabsf(d0), fabsf(d1)), fmaxf(fabsf(d2), fabsf(d3))), fabsf(d4));
+        return fmaf(1e-6f * m, m, 1e-18f);
+    }
+
+    __device__ __forceinline__ void init(const float (&x6)[6], float h_) {
+        h = h_;
 #pragma unroll
-    for (int o = 0; o < 7; ++o) x[o] = line_at<float>(line, stride, idx + o - 3, n, bc);
-    long long vl, vs;
-    if (AXIS == 0) { vl = ix3(i, j, k, nx + 1, ny); vs = 1; }
-    else if (AXIS == 1) { vl = ix3(i, j, k, nx, ny + 1); vs = nx; }
-    else { vl = ix3(i, j, k, nx, ny); vs = (long long)nx * ny; }
-    const float t = weno_point_f32<QUIRK>(x[0], x[1], x[2], x[3], x[4], x[5], x[6], V[vl], V[vl + vs], dt, h);
-    if (STAGE == 1) dst[e] = t;
-    else dst[e] = 0.5f * t + 0.5f * T0[e];
+        for (int q = 0; q < 6; ++q) x[q] = x6[q];
+        float d[5];
+#pragma unroll
+        for (int q = 0; q < 5; ++q) d[q] = h * (x[q + 1] - x[q]);  // D_{i-3} .. D_{i+1}
+        float a2, a1, a0, unused0, unused1, unused2;
+        triple(d[0], d[1], d[2], a2, bl[0], unused0, unused1);   // centre i-2
+        triple(d[1], d[2], d[3], a1, bl[1], bc[0], unused2);     // centre i-1
+        triple(d[2], d[3], d[4], a0, bl[2], bc[1], br);          // centre i
+        g1[0] = (a1 - a2) * (1.0f / 3.0f);
+        g1[1] = (a0 - a1) * (1.0f / 3.0f);
+        g3 = 0.5f * (a0 - a1);
+        ap = a0;
+        e = floor5(d[0], d[1], d[2], d[3], d[4]);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) D[q] = d[q + 1];
+    }
+
+    __device__ __forceinline__ float back() const { return x[0]; }
+
+    __device__ __forceinline__ float step(float xn, float va, float vb, float dt) {
+        const float Dn = h * (xn - x[5]);  // D_{i+2}
+        float a1, bL1, bC1, bR1;
+        triple(D[2], D[3], Dn, a1, bL1, bC1, bR1);  // centre i+1
+        const float g = a1 - ap;
+        const float G1n = g * (1.0f / 3.0f), G3n = 0.5f * g;
+        const float e1 = floor5(D[0], D[1], D[2], D[3], Dn);
+        const float Vm = fminf(va, 0.0f), Vp = fmaxf(vb, 0.0f);
+        float dFm = 0.0f, dFp = 0.0f;
+        if (upwind_active(Vp)) {
+            const float p2 = fmaf(5.0f / 6.0f, D[1], fmaf(1.0f / 3.0f, D[2], (-1.0f / 6.0f) * D[0]));
+            dFm = mix(bl[0], bc[0], br, e, p2, -g1[0], -g3);
+        }
+        if (upwind_active(Vm)) {
+            const float p2 = fmaf(5.0f / 6.0f, D[2], fmaf(1.0f / 3.0f, D[1], (-1.0f / 6.0f) * D[3]));
+            dFp = mix(bR1, bc[1], bl[1], e1, p2, G1n, g3);
+        }
+        const float out = x[3] - dt * (Vp * dFm + Vm * dFp);
+#pragma unroll
+        for (int q = 0; q < 5; ++q) x[q] = x[q + 1];
+        x[5] = xn;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) D[q] = D[q + 1];
+        D[3] = Dn;
+        bl[0] = bl[1];
+        bl[1] = bl[2];
+        bl[2] = bL1;
+        bc[0] = bc[1];
+        bc[1] = bC1;
+        br = bR1;
+        g1[0] = g1[1];
+        g1[1] = G1n;
+        g3 = G3n;
+        e = e1;
+        ap = a1;
+        return out;
+    }
+};
+
+// Window form: the 7-point window and weno_point_f32, for the v2 stencil
+// quirk (whose fifth difference of dF- spans three cells).
+template <int QUIRK>
+struct WenoStreamWindow {
+    float x[6];
+    float h;
+    __device__ __forceinline__ void init(const float (&x6)[6], float h_) {
+        h = h_;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) x[q] = x6[q];
+    }
+    __device__ __forceinline__ float back() const { return x[0]; }
+    __device__ __forceinline__ float step(float xn, float va, float vb, float dt) {
+        const float out = weno_point_f32<QUIRK>(x[0], x[1], x[2], x[3], x[4], x[5], xn, va, vb, dt, h);
+#pragma unroll
+        for (int q = 0; q < 5; ++q) x[q] = x[q + 1];
+        x[5] = xn;
+        return out;
+    }
+};
+
+template <int QUIRK> struct StreamOf { using type = WenoStreamWindow<QUIRK>; };
+template <> struct StreamOf<0> { using type = WenoStreamShared; };
+
+// ------------------------------------------------------------------ march
+// Both stages along the segment [c0, c1) of a line of n cells (Neumann or
+// Dirichlet ends, n >= 3, c1 - c0 >= 3, c0 == 0 or c0 >= 8).  Stage 1 runs
+// three points ahead of stage 2: it starts at c0 - 3 (for c0 == 0 the three
+// points before the line are replaced by the mirror rule after the stage,
+// like Boundaries_*_Weno5!), and each step produces T1[c + 3] and then
+// T[c] = (T0[c] + stage2(T1)[c]) / 2.  Near the line's end T1 beyond it is the
+// mirror of the last three T1 values.
+
+// Dirichlet/Neumann ends of an FP32 sweep: g = (float)(2 * value), so a ghost
+// g - v rounds like the reference's 2 value - v evaluated in FP32.
+struct WenoBCf {
+    int typeL, typeR;
+    float gL, gR;
+};
+__device__ __forceinline__ float weno_ghost(float v, bool left, const WenoBCf& bc) {
+    const int t = left ? bc.typeL : bc.typeR;
+    return t == HT3D_BC_DIRICHLET ? (left ? bc.gL : bc.gR) - v : v;
 }
 
-// Both stages of one axis fused, x-axis: a warp owns a row; the row of T0 and
+template <class Stream>
+struct March {
+    Stream s1, s2;
+    float v0, v1, v2, v3;  // faces c .. c + 3 of the next step
+    float gq0, gq1, gq2;   // tail: the T1 ghosts n, n + 1, n + 2
+    float tq0, tq1, tq2;   // tail: T0[n - 3 .. n - 1]
+
+    //   src.t0(q): T0 at q in [c0 - 6, c0 + 6) (ghosts by the BC rule; positions
+    //              before -3 only feed discarded points: any finite value)
+    //   src.v(f):  face f in [c0 - 3, c0 + 3] (faces < 0: any finite value)
+    template <class Src>
+    __device__ __forceinline__ void start(const Src& src, int c0, const WenoBCf& bc, float dt, float h) {
+        {
+            float x[6];
+#pragma unroll
+            for (int q = 0; q < 6; ++q) x[q] = src.t0(c0 - 6 + q);
+            s1.init(x, h);
+        }
+        float w[6];  // T1[c0 - 3 .. c0 + 2]
+#pragma unroll
+        for (int r = 0; r < 6; ++r) w[r] = s1.step(src.t0(c0 + r), src.v(c0 - 3 + r), src.v(c0 - 2 + r), dt);
+        if (c0 == 0) {
+            w[0] = weno_ghost(w[5], true, bc);
+            w[1] = weno_ghost(w[4], true, bc);
+            w[2] = weno_ghost(w[3], true, bc);
+        }
+        s2.init(w, h);
+        v0 = src.v(c0);
+        v1 = src.v(c0 + 1);
+        v2 = src.v(c0 + 2);
+        v3 = src.v(c0 + 3);
+    }
+    // step c with its stage-1 point c + 3 inside the line: xa = T0[c + 6]
+    // (a ghost past the end), va = face c + 4; returns T[c]
+    __device__ __forceinline__ float step(float xa, float va, float dt) {
+        const float t0c = s1.back();  // T0[c]
+        const float t1 = s1.step(xa, v3, va, dt);
+        const float t = s2.step(t1, v0, v1, dt);
+        v0 = v1;
+        v1 = v2;
+        v2 = v3;
+        v3 = va;
+        return 0.5f * t + 0.5f * t0c;
+    }
+    // at c = n - 3: s1 holds T0[n - 3 .. n + 2], s2 T1[n - 6 .. n - 1]
+    __device__ __forceinline__ void tail_enter(const WenoBCf& bc) {
+        tq0 = s1.x[0];
+        tq1 = s1.x[1];
+        tq2 = s1.x[2];
+        gq0 = weno_ghost(s2.x[5], false, bc);
+        gq1 = weno_ghost(s2.x[4], false, bc);
+        gq2 = weno_ghost(s2.x[3], false, bc);
+    }
+    __device__ __forceinline__ float tail_step(float dt) {  // c = n - 3, n - 2, n - 1 in turn
+        const float t = s2.step(gq0, v0, v1, dt);
+        const float out = 0.5f * t + 0.5f * tq0;
+        gq0 = gq1;
+        gq1 = gq2;
+        tq0 = tq1;
+        tq1 = tq2;
+        v0 = v1;
+        v1 = v2;
+        v2 = v3;
+        return out;
+    }
+};
+
+// y or z line straight from HBM (out of place: src -> dst, the inner cells);
+// the read-only loads may move ahead of the stores of earlier steps.
+struct LineSrc {
+    const float* line;  // inner cell 0 of the line
+    float* out;
+    const float* vline;  // face 0
+    long long stride, vs;
+    int n;
+    WenoBCf bc;
+    __device__ __forceinline__ float ld(int q) const { return __ldg(line + (long long)q * stride); }
+    __device__ __forceinline__ float t0(int q) const {
+        if (q >= 0 && q < n) return ld(q);
+        if (q < -3) return 0.0f;
+        return q < 0 ? weno_ghost(ld(-1 - q), true, bc) : weno_ghost(ld(2 * n - 1 - q), false, bc);
+    }
+    __device__ __forceinline__ float v(int f) const { return f >= 0 ? __ldg(vline + (long long)f * vs) : 0.0f; }
+    __device__ __forceinline__ void put(int c, float val) const { out[(long long)c * stride] = val; }
+};
+
+// Balanced segments: kMarchL cells per thread on average, at least 48 each
+// when a line has more than one.
+constexpr int kMarchL = 64;
+__host__ __device__ __forceinline__ int march_chunks(int n) { return n < 3 * kMarchL / 2 ? 1 : (n + kMarchL / 2) / kMarchL; }
+
+template <int AXIS, int QUIRK>
+__global__ void __launch_bounds__(128) k_weno_march_f32(const float* __restrict__ src, float* __restrict__ dst,
+                                                        const float* __restrict__ V, float dt, float h, WenoBCf bc,
+                                                        int nx, int ny, int nz) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int o = blockIdx.y;  // k for the y-march, j for the z-march
+    const int n = AXIS == 1 ? ny : nz;
+    const int K = march_chunks(n);
+    const int c0 = (int)((long long)blockIdx.z * n / K), c1 = (int)((long long)(blockIdx.z + 1) * n / K);
+    if (i >= nx) return;
+    const int n1 = nx + 2, n2 = ny + 2;
+    LineSrc s;
+    s.stride = AXIS == 1 ? (long long)n1 : (long long)n1 * n2;
+    const long long first = AXIS == 1 ? (i + 1) + (long long)n1 * (1 + (long long)n2 * (o + 1))
+                                      : (i + 1) + (long long)n1 * ((o + 1) + (long long)n2);
+    s.line = src + first;
+    s.out = dst + first;
+    s.vs = AXIS == 1 ? (long long)nx : (long long)nx * ny;
+    s.vline = AXIS == 1 ? V + i + (long long)nx * (ny + 1) * o : V + i + (long long)nx * o;
+    s.n = n;
+    s.bc = bc;
+    March<typename StreamOf<QUIRK>::type> M;
+    M.start(s, c0, bc, dt, h);
+    const int cA = c1 < n ? c1 : n - 3;  // steps whose stage-1 point c + 3 is inside the line
+    const int cB = min(cA, n - 6);       // ... and whose T0[c + 6] is too
+    int c = c0;
+#pragma unroll 4
+    for (; c < cB; ++c) s.put(c, M.step(s.ld(c + 6), s.v(c + 4), dt));
+    for (; c < cA; ++c) s.put(c, M.step(s.t0(c + 6), s.v(c + 4), dt));
+    if (c1 == n) {
+        M.tail_enter(bc);
+#pragma unroll
+        for (int r = 0; r < 3; ++r) s.put(n - 3 + r, M.tail_step(dt));
+    }
+}
+
+// x: a warp marches 32 consecutive rows (one per lane) along a segment of x.
+// T0 and Vx reach shared memory through per-row rings of three 8-cell tiles,
+// filled by asynchronous 4-byte copies one tile ahead of the march; a step
+// reads its own row's ring (odd row pitch: the 32 lanes hit 32 banks) and
+// leaves T[c] in the slot of T0[c], which the warp then stores coalesced.
+// Tile u of a segment holds positions b0 + 8u .. b0 + 8u + 7 (b0 = c0 - 8)
+// in ring slot u % 3; the steps c0 + 8v .. c0 + 8v + 7 (block v) read tiles
+// v + 1 and v + 2 and write tile v + 1.
+constexpr int kXW = 8;
+constexpr int kXPitch = 3 * kXW + 1;
+constexpr int kXWarps = 4;
+
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+struct RingSrc {
+    float* t;         // this lane's row of the T0 ring
+    const float* vp;  // ... of the Vx ring
+    int b0, n;
+    WenoBCf bc;
+    __device__ __forceinline__ int col(int q) const {
+        const int d = q - b0;
+        return ((d >> 3) % 3) * kXW + (d & 7);
+    }
+    __device__ __forceinline__ float t0(int q) const {
+        if (q >= 0 && q < n) return t[col(q)];
+        if (q < -3) return 0.0f;
+        return q < 0 ? weno_ghost(t[col(-1 - q)], true, bc) : weno_ghost(t[col(2 * n - 1 - q)], false, bc);
+    }
+    __device__ __forceinline__ float v(int f) const { return f >= 0 ? vp[col(f)] : 0.0f; }
+    __device__ __forceinline__ void put(int c, float val) const { t[col(c)] = val; }
+};
+
+template <int QUIRK>
+__global__ void __launch_bounds__(32 * kXWarps) k_weno_xstream_f32(float* __restrict__ T, const float* __restrict__ Vx,
+                                                                   float dt, float h, WenoBCf bc, int nx, int ny,
+                                                                   int nz) {
+    __shared__ float ring[kXWarps][2][32 * kXPitch];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long rows = (long long)ny * nz;
+    const long long row0 = ((long long)blockIdx.x * kXWarps + warp) * 32;
+    if (row0 >= rows) return;  // whole warps only
+    const int n = nx;
+    const int K = march_chunks(n);
+    const int c0 = (int)((long long)blockIdx.y * n / K), c1 = (int)((long long)(blockIdx.y + 1) * n / K);
+    const int b0 = c0 - kXW;
+    float* tr = ring[warp][0];
+    float* vr = ring[warp][1];
+    // copy lanes: column lane & 7 of rows sub + 4 k (k = 0 .. 7), rows past the
+    // last one read the last row and store nothing
+    const int sub = lane >> 3, cc = lane & 7;
+    const long long rlast = rows - 1;
+    const long long tbase = 1 + (long long)(nx + 2) * (1 + (long long)(ny + 2));  // inner cell 0 of row 0
+    unsigned rel[8];                                                              // row offsets from row0's
+    long long t0off;
+    {
+        const long long r0 = row0;
+        t0off = tbase + (long long)(nx + 2) * (r0 + 2 * (r0 / ny));
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const long long r = min(row0 + sub + 4 * k, rlast);
+            rel[k] = (unsigned)(tbase + (long long)(nx + 2) * (r + 2 * (r / ny)) - t0off);
+        }
+    }
+    const float* Tw = T + t0off;
+    const float* Vw = Vx + (long long)(nx + 1) * row0;
+    const int tq_lo = max(0, c0 - 6), tq_hi = min(n, c1 + 6);  // T0 positions a segment reads
+    const int vq_lo = max(0, c0 - 3), vq_hi = min(n, c1 + 3);  // faces (inclusive)
+    auto load_tile = [&](int u) {
+        const int q = b0 + kXW * u + cc;
+        float* td = tr + (u % 3) * kXW + cc;
+        float* vd = vr + (u % 3) * kXW + cc;
+        const bool tq = q >= tq_lo && q < tq_hi, vq = q >= vq_lo && q <= vq_hi;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int r = sub + 4 * k;
+            const long long rv = min(row0 + r, rlast) - row0;
+            if (tq) cp_async4(td + r * kXPitch, Tw + rel[k] + q);
+            if (vq) cp_async4(vd + r * kXPitch, Vw + (nx + 1) * rv + q);
+        }
+        cp_async_commit();
+    };
+    auto store_tile = [&](int u, int lo, int hi) {  // positions [lo, hi) of tile u
+        const int q = b0 + kXW * u + cc;
+        if (q < lo || q >= hi) return;
+        const float* ts = tr + (u % 3) * kXW + cc;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int r = sub + 4 * k;
+            if (row0 + r <= rlast) T[t0off + rel[k] + q] = ts[r * kXPitch];
+        }
+    };
+    load_tile(0);
+    load_tile(1);
+    load_tile(2);
+    cp_async_wait<0>();
+    __syncwarp();
+    RingSrc src;
+    src.t = tr + lane * kXPitch;
+    src.vp = vr + lane * kXPitch;
+    src.b0 = b0;
+    src.n = n;
+    src.bc = bc;
+    March<typename StreamOf<QUIRK>::type> M;
+    M.start(src, c0, bc, dt, h);
+    __syncwarp();
+    load_tile(3);
+    const int cA = c1 < n ? c1 : n - 3;
+    for (int v = 0, cb = c0; cb < c1; ++v, cb += kXW) {
+        float* tcur = src.t + ((v + 1) % 3) * kXW;  // positions cb .. cb + 7
+        const float* tnxt = src.t + ((v + 2) % 3) * kXW;
+        const float* vcur = src.vp + ((v + 1) % 3) * kXW;
+        const float* vnxt = src.vp + ((v + 2) % 3) * kXW;
+        if (cb + kXW <= cA && cb + kXW + 6 <= n) {  // eight steps without ghosts
+#pragma unroll
+            for (int m = 0; m < kXW; ++m) {
+                const float xa = m + 6 < kXW ? tcur[m + 6] : tnxt[m + 6 - kXW];
+                const float va = m + 4 < kXW ? vcur[m + 4] : vnxt[m + 4 - kXW];
+                tcur[m] = M.step(xa, va, dt);
+            }
+        } else {
+            for (int m = 0; m < kXW && cb + m < c1; ++m) {
+                const int c = cb + m;
+                float out;
+                if (c < cA) {
+                    out = M.step(src.t0(c + 6), src.v(c + 4), dt);
+                } else {
+                    if (c == n - 3) M.tail_enter(bc);
+                    out = M.tail_step(dt);
+                }
+                src.put(c, out);
+            }
+        }
+        __syncwarp();
+        store_tile(v + 1, c0, c1);
+        load_tile(v + 4);  // into the slot just stored
+        cp_async_wait<1>();
+        __syncwarp();
+    }
+    cp_async_wait<0>();
+}
+
+// Row-at-a-time x kernel for periodic x: a warp owns a row; the row of T0 and
 // of the stage-1 result T1 live in shared memory with three ghost cells on
-// each side (filled by the BC rules after each stage), so the stencils are
-// plain shared loads.  Reads T0 and Vx once and writes T once.
+// each side (filled by the BC rules after each stage).
 constexpr int kRowWarps = 8;
 
 // ghost cells r[-3..-1] and r[n..n+2] of a shared row r (r points at element 0)
@@ -122,108 +522,31 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_weno_rows_f32(float* __restr
     }
 }
 
-// Both stages of one axis fused, y or z axis (Neumann / Dirichlet ends),
-// out of place (src -> dst, the inner cells): a thread marches along a chunk
-// [c0, c0 + L) of its line with sliding register windows
-//   w0 = T0[c .. c+6], w1 = T1[c-3 .. c+3], v = V faces c .. c+4,
-// producing T1[c+3] and then T[c]; the first six T1 values of a chunk (and
-// the ghosts at the line's ends) are produced before the march.  Threads are
-// consecutive in x (coalesced); chunks multiply the parallelism of the lines.
-constexpr int kMarchL = 64;
-
-template <int AXIS, int QUIRK>
-__global__ void __launch_bounds__(128) k_weno_march_f32(const float* __restrict__ src, float* __restrict__ dst,
+// Unfused stage (any BC, incl. periodic): one launch per stage and axis.
+template <int AXIS, int QUIRK, int STAGE>
+__global__ void __launch_bounds__(256) k_weno_stage_f32(const float* __restrict__ src, float* dst, const float* T0,
                                                         const float* __restrict__ V, float dt, float h, WenoBC bc,
                                                         int nx, int ny, int nz) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int o = blockIdx.y;  // k for the y-march, j for the z-march
-    const int c0 = blockIdx.z * kMarchL;
-    const int n = AXIS == 1 ? ny : nz;
-    if (i >= nx || c0 >= n) return;
-    const int c1 = min(n, c0 + kMarchL);
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i >= nx || j >= ny || k >= nz) return;
     const int n1 = nx + 2, n2 = ny + 2;
-    const long long stride = AXIS == 1 ? (long long)n1 : (long long)n1 * n2;
-    const long long first = AXIS == 1 ? (i + 1) + (long long)n1 * (1 + (long long)n2 * (o + 1))
-                                      : (i + 1) + (long long)n1 * ((o + 1) + (long long)n2);
-    const float* line = src + first;
-    float* out = dst + first;
-    const long long vs = AXIS == 1 ? (long long)nx : (long long)nx * ny;
-    const float* vline = AXIS == 1 ? V + i + (long long)nx * (ny + 1) * o : V + i + (long long)nx * o;
-    float w0[7], w1[7], v[5];
-    // T1[c0-3 .. c0+2] (ghosts at the line's start)
-    {
-        const int pf = c0 == 0 ? 0 : c0 - 3;  // first real T1 produced here
-        const int np = c0 == 0 ? 3 : 6;       // how many
+    const long long e = (i + 1) + (long long)n1 * ((j + 1) + (long long)n2 * (k + 1));
+    const int idx = AXIS == 0 ? i : (AXIS == 1 ? j : k);
+    const int n = AXIS == 0 ? nx : (AXIS == 1 ? ny : nz);
+    const long long stride = AXIS == 0 ? 1 : (AXIS == 1 ? (long long)n1 : (long long)n1 * n2);
+    const float* line = src + e - (long long)idx * stride;
+    float x[7];
 #pragma unroll
-        for (int q = 0; q < 7; ++q) w0[q] = line_at<float>(line, stride, pf + q - 3, n, bc);
-        float t1[6];
-#pragma unroll
-        for (int r = 0; r < 6; ++r) {
-            if (r < np) {
-                const int pp = pf + r;
-                t1[r] = weno_point_f32<QUIRK>(w0[0], w0[1], w0[2], w0[3], w0[4], w0[5], w0[6], vline[pp * vs],
-                                              vline[(pp + 1) * vs], dt, h);
-#pragma unroll
-                for (int q = 0; q < 6; ++q) w0[q] = w0[q + 1];
-                w0[6] = (pp + 1 < n) ? line_at<float>(line, stride, pp + 4, n, bc) : 0.f;
-            } else {
-                t1[r] = 0.f;
-            }
-        }
-        if (c0 == 0) {
-            w1[0] = weno_ghost(t1[2], true, bc);
-            w1[1] = weno_ghost(t1[1], true, bc);
-            w1[2] = weno_ghost(t1[0], true, bc);
-            w1[3] = t1[0];
-            w1[4] = t1[1];
-            w1[5] = t1[2];
-        } else {
-#pragma unroll
-            for (int q = 0; q < 6; ++q) w1[q] = t1[q];
-        }
-        // w0 = T0[c0 .. c0+6] now
-    }
-#pragma unroll
-    for (int q = 0; q < 5; ++q) v[q] = c0 + q <= n ? vline[(long long)(c0 + q) * vs] : 0.f;
-    // difference windows: dw0[q] = h (w0[q+1] - w0[q]); dw1 likewise for w1[0..5]
-    float dw0[6], dw1[6];
-#pragma unroll
-    for (int q = 0; q < 6; ++q) dw0[q] = h * (w0[q + 1] - w0[q]);
-#pragma unroll
-    for (int q = 0; q < 5; ++q) dw1[q] = h * (w1[q + 1] - w1[q]);
-#pragma unroll 2
-    for (int c = c0; c < c1; ++c) {
-        const int p = c + 3;  // T1 position entering the window
-        float head;
-        if (p < n) {
-            head = weno_point_f32_d<QUIRK>(dw0, w0[2], w0[3], w0[5], v[3], v[4], dt, h);
-        } else {
-            // mirror 2n-1-p of T1 is in the window: w1[q] holds T1[c-3+q]
-            const int q = 2 * n - 1 - p - (c - 3);
-            float m = w1[5];
-#pragma unroll
-            for (int r = 0; r < 6; ++r)
-                if (r == q) m = w1[r];
-            head = weno_ghost(m, false, bc);
-        }
-        w1[6] = head;
-        dw1[5] = h * (head - w1[5]);
-        const float t = weno_point_f32_d<QUIRK>(dw1, w1[2], w1[3], w1[5], v[0], v[1], dt, h);
-        out[(long long)c * stride] = 0.5f * t + 0.5f * w0[0];
-#pragma unroll
-        for (int q = 0; q < 6; ++q) w1[q] = w1[q + 1];
-#pragma unroll
-        for (int q = 0; q < 5; ++q) dw1[q] = dw1[q + 1];
-#pragma unroll
-        for (int q = 0; q < 6; ++q) w0[q] = w0[q + 1];
-        w0[6] = (c + 4 < n) ? line_at<float>(line, stride, c + 7, n, bc) : 0.f;
-#pragma unroll
-        for (int q = 0; q < 5; ++q) dw0[q] = dw0[q + 1];
-        dw0[5] = h * (w0[6] - w0[5]);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) v[q] = v[q + 1];
-        v[4] = (c + 5 <= n) ? vline[(long long)(c + 5) * vs] : 0.f;
-    }
+    for (int o = 0; o < 7; ++o) x[o] = line_at<float>(line, stride, idx + o - 3, n, bc);
+    long long vl, vs;
+    if (AXIS == 0) { vl = ix3(i, j, k, nx + 1, ny); vs = 1; }
+    else if (AXIS == 1) { vl = ix3(i, j, k, nx, ny + 1); vs = nx; }
+    else { vl = ix3(i, j, k, nx, ny); vs = (long long)nx * ny; }
+    const float t = weno_point_f32<QUIRK>(x[0], x[1], x[2], x[3], x[4], x[5], x[6], V[vl], V[vl + vs], dt, h);
+    if (STAGE == 1) dst[e] = t;
+    else dst[e] = 0.5f * t + 0.5f * T0[e];
 }
 
 // inner cells of a ghosted field: dst = src
@@ -236,13 +559,23 @@ __global__ void k_copy_inner_f32(float* __restrict__ dst, const float* __restric
     dst[e] = src[e];
 }
 
+WenoBCf bcf(const WenoBC& b) {
+    return WenoBCf{b.typeL, b.typeR, (float)(2 * b.valL), (float)(2 * b.valR)};
+}
+
 // One axis: cur is the field before the axis; returns the field after it
 // (cur itself for in-place paths, `other` for the out-of-place march).
 template <int AXIS, int QUIRK>
 float* axis_f32(ht3d_ctx* ctx, float* cur, float* other, float* tmp, const float* V, float dt, float h, WenoBC bc,
                 int nx, int ny, int nz) {
     const bool periodic = bc.typeL == HT3D_BC_PERIODIC || bc.typeR == HT3D_BC_PERIODIC;
-    if (AXIS == 0) {
+    if constexpr (AXIS == 0) {
+        if (!periodic) {
+            const long long rows = (long long)ny * nz, per_block = 32LL * kXWarps;
+            const dim3 g((unsigned)((rows + per_block - 1) / per_block), march_chunks(nx));
+            HT3D_LAUNCH(ctx, k_weno_xstream_f32<QUIRK>, g, 32 * kXWarps, 0, cur, V, dt, h, bcf(bc), nx, ny, nz);
+            return cur;
+        }
         const size_t smem = sizeof(float) * 2 * (size_t)(nx + 6) * kRowWarps;
         if (smem <= 96 * 1024) {
             if (smem > 48 * 1024)
@@ -253,11 +586,13 @@ float* axis_f32(ht3d_ctx* ctx, float* cur, float* other, float* tmp, const float
                         cur, V, dt, h, bc, nx, ny, nz);
             return cur;
         }
-    } else if (!periodic) {
-        const int n = AXIS == 1 ? ny : nz;
-        const dim3 g((nx + 127) / 128, AXIS == 1 ? nz : ny, (n + kMarchL - 1) / kMarchL);
-        HT3D_LAUNCH(ctx, (k_weno_march_f32<AXIS, QUIRK>), g, 128, 0, cur, other, V, dt, h, bc, nx, ny, nz);
-        return other;
+    } else {
+        if (!periodic) {
+            const int n = AXIS == 1 ? ny : nz;
+            const dim3 g((nx + 127) / 128, AXIS == 1 ? nz : ny, march_chunks(n));
+            HT3D_LAUNCH(ctx, (k_weno_march_f32<AXIS, QUIRK>), g, 128, 0, cur, other, V, dt, h, bcf(bc), nx, ny, nz);
+            return other;
+        }
     }
     dim3 b(32, 8, 1), g((nx + 31) / 32, (ny + 7) / 8, nz);
     HT3D_LAUNCH(ctx, (k_weno_stage_f32<AXIS, QUIRK, 1>), g, b, 0, cur, tmp, (const float*)nullptr, V, dt, h, bc, nx, ny,

@@ -61,14 +61,36 @@ def test_sweep_precisions_against_oracle(ctx, orc, n, variant, bc):
     np.testing.assert_array_equal(got[0], np.float32(T[0]))  # ghosts untouched
 
 
+@pytest.mark.parametrize("n", [(65, 66, 130), (97, 49, 96), (255, 8, 7)])
+@pytest.mark.parametrize("variant", [abi.WENO_V1, abi.WENO_V2_REF])
+def test_sweep_f32_segments_against_oracle(ctx, orc, n, variant):
+    """The FP32 march kernels split lines into segments (x: several lanes of a
+    warp per shared-memory row; y, z: several threads per line): sizes whose
+    segments end one or two cells before the line's end, or right at it."""
+    nx, ny, nz = n
+    Vd = sweep.curl_velocity(nx, ny, nz, seed=6)
+    Td = sweep.blob(nx, ny, nz)
+    T, V = ht.to_numpy(Td), [ht.to_numpy(v) for v in Vd]
+    types, vals = BCS["hrl"]
+    h = (float(nx), float(ny), float(nz))
+    dt = sweep.cfl_dt(nx, ny, nz, cfl=0.5)
+    To = oracle_sweep(orc, T, V, dt, h, types, vals, variant)
+    inner = (slice(1, -1),) * 3
+    T32 = Td.float().permute(2, 1, 0).contiguous().permute(2, 1, 0)
+    V32 = [v.float().permute(2, 1, 0).contiguous().permute(2, 1, 0) for v in Vd]
+    api.weno5_advect_f32(ctx, T32, *V32, dt, *h, types, vals, variant)
+    got = T32.double().cpu().numpy()
+    assert rel_err(got[inner], To[inner]) <= 2e-5
+
+
 def test_sweep_f32_keeps_a_uniform_field(ctx):
     """All differences vanish: a uniform field is advected exactly (Neumann walls)."""
-    n = 19
-    Vd = [v.float().permute(2, 1, 0).contiguous().permute(2, 1, 0) for v in sweep.curl_velocity(n, n, n, seed=6)]
-    T = ht.zeros(n + 2, n + 2, n + 2, dtype=torch.float32) + 0.625
-    api.weno5_advect_f32(ctx, T, *Vd, sweep.cfl_dt(n, n, n), float(n), float(n), float(n), [0] * 6, [0.0] * 6,
-                         abi.WENO_V1)
-    assert bool((T == 0.625).all())
+    for n in (19, 67):
+        Vd = [v.float().permute(2, 1, 0).contiguous().permute(2, 1, 0) for v in sweep.curl_velocity(n, n, n, seed=6)]
+        T = ht.zeros(n + 2, n + 2, n + 2, dtype=torch.float32) + 0.625
+        api.weno5_advect_f32(ctx, T, *Vd, sweep.cfl_dt(n, n, n), float(n), float(n), float(n), [0] * 6, [0.0] * 6,
+                             abi.WENO_V1)
+        assert bool((T == 0.625).all()), n
 
 
 def test_sweep_f32_rejects_float64(ctx):
