@@ -14,6 +14,7 @@ TUNE_ENS_BLOCK = 4
 TUNE_ENS_GRAPH = 5
 TUNE_TEMPORAL = 6
 TUNE_WAIT_TEST = 7
+TUNE_ENS_TILE = 8
 DYREL_ZMARCH, DYREL_CELL = 1, 2
 
 

@@ -171,6 +171,11 @@ int ht3d_ctx_set_tuning(ht3d_ctx* ctx, int key, int value) {
         ctx->ens_block = value;
         return HT3D_OK;
     }
+    if (key == HT3D_TUNE_ENS_TILE) {
+        if (value < 0 || value > 6) return HT3D_ERR_ARG;
+        ctx->ens_tile = value;
+        return HT3D_OK;
+    }
     if (key == HT3D_TUNE_ENS_GRAPH) {
         if (value != 0 && value != 1) return HT3D_ERR_ARG;
         ctx->ens_graphs = value;

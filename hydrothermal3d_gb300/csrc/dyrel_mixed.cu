@@ -1,5 +1,6 @@
 // Mixed-precision DYREL solver (FP32 inner iterations, FP64 defect correction).
 #include <cuda.h>
+#include <algorithm>
 #include <cstddef>
 #include <mutex>
 
@@ -130,6 +131,61 @@ __device__ __forceinline__ void mixed_cell(float xc, float xw, float xe, float x
     xnew = __fmaf_rn(mom, __fsub_rn(xc, xprev), __fmaf_rn(-dh2, f, xc));
 }
 
+// x-neighbours across a quad's edges: the west neighbour of cell i0, the east
+// neighbour of cell i0+3 and the east face of cell i0+3, from the adjacent
+// lanes (same row) by warp shuffles, or by a scalar load at a warp edge.
+// Every lane of the warp takes part in the shuffles.
+__device__ __forceinline__ void quad_x_edges(const float* __restrict__ Din, const float* __restrict__ kx,
+                                             const float4& d, const float4& kx4, long long base, int i0, int q,
+                                             const Pad& p, int lane, float& dW, float& dE, float& kE3) {
+    const float dW_sh = __shfl_up_sync(0xffffffffu, d.w, 1);
+    const float dE_sh = __shfl_down_sync(0xffffffffu, d.x, 1);
+    const float kE_sh = __shfl_down_sync(0xffffffffu, kx4.x, 1);
+    dW = 0.f;
+    dE = 0.f;
+    kE3 = 0.f;
+    if (i0 > 0) dW = lane > 0 ? dW_sh : Din[base - 1];
+    if (i0 + 4 < p.nx) dE = lane < 31 ? dE_sh : Din[base + 4];
+    if (i0 + 3 < p.nx) kE3 = (lane < 31 && q < p.nq - 1) ? kE_sh : kx[base + 4];
+}
+
+// The four cells of a quad (mixed_cell each) from the loaded neighbourhood;
+// stores D' (and F) unless act is false.  Neighbours beyond the grid are the
+// ghost values of the BCs (dS .. dF are not read there).
+template <bool STOREF>
+__device__ __forceinline__ void quad_cells(const float4& d, const float4& kx4, const float4& dS, const float4& dN,
+                                           const float4& dB, const float4& dF, const float4& kyS, const float4& kyN,
+                                           const float4& kzB, const float4& kzF, const float4& r4, const float4& dp4,
+                                           float dW, float dE, float kE3, bool south, bool north, bool back,
+                                           bool front, int i0, const Pad& p, const MixScal& s, const BC6<float>& bc,
+                                           float* __restrict__ Dio, float* __restrict__ F, long long base, bool act) {
+    const float mom = s.mom, dh2 = s.dh2, cX = s.cX, _dx = s._dx, _dy = s._dy, _dz = s._dz;
+    const float _dx2 = __fmul_rn(_dx, _dx), _dy2 = __fmul_rn(_dy, _dy), _dz2 = __fmul_rn(_dz, _dz);
+    float outD[4], outF[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        const int i = i0 + m;
+        const float xc = c4(d, m);
+        const float xw = (i == 0) ? ghost(bc, 0, xc) : (m == 0 ? dW : c4(d, m - 1));
+        const float xe = (i == p.nx - 1) ? ghost(bc, 1, xc) : (m == 3 ? dE : c4(d, m + 1));
+        const float xs = south ? c4(dS, m) : ghost(bc, 2, xc);
+        const float xn = north ? c4(dN, m) : ghost(bc, 3, xc);
+        const float xb = back ? c4(dB, m) : ghost(bc, 4, xc);
+        const float xf = front ? c4(dF, m) : ghost(bc, 5, xc);
+        const float kW = c4(kx4, m), kE = m == 3 ? kE3 : c4(kx4, m + 1);
+        const float kS = c4(kyS, m), kN = c4(kyN, m), kB = c4(kzB, m), kF = c4(kzF, m);
+        float f, xn1;
+        mixed_cell(xc, xw, xe, xs, xn, xb, xf, kW, kE, kS, kN, kB, kF, c4(r4, m), c4(dp4, m), mom, dh2, cX, _dx, _dy,
+                   _dz, _dx2, _dy2, _dz2, f, xn1);
+        const bool valid = i < p.nx;
+        outD[m] = valid ? xn1 : 0.f;
+        outF[m] = valid ? f : 0.f;
+    }
+    if (!act) return;
+    *reinterpret_cast<float4*>(Dio + base) = make_float4(outD[0], outD[1], outD[2], outD[3]);
+    if (STOREF) *reinterpret_cast<float4*>(F + base) = make_float4(outF[0], outF[1], outF[2], outF[3]);
+}
+
 // FP32 inner iteration of the mixed solver on the padded layout, for the
 // quad of cells 4q..4q+3 of row j, plane k (t = q + nq*j is the thread's
 // position in the plane).  Every field moves with 16-byte loads; the
@@ -159,10 +215,6 @@ __device__ __forceinline__ void mixed_quad(const float* __restrict__ Din, float*
     const long long base = i0 + (long long)p.PX * j + p.plane * k;
     const float4 d = *reinterpret_cast<const float4*>(Din + base);
     const float4 kx4 = *reinterpret_cast<const float4*>(kx + base);
-    // every lane takes part in the shuffles
-    const float dW_sh = __shfl_up_sync(0xffffffffu, d.w, 1);
-    const float dE_sh = __shfl_down_sync(0xffffffffu, d.x, 1);
-    const float kE_sh = __shfl_down_sync(0xffffffffu, kx4.x, 1);
     const bool south = j > 0, north = j < p.ny - 1, back = k > 0, front = k < p.nz - 1;
     const float4 dS = south ? *reinterpret_cast<const float4*>(Din + base - p.PX) : d;
     const float4 dN = north ? *reinterpret_cast<const float4*>(Din + base + p.PX) : d;
@@ -174,38 +226,54 @@ __device__ __forceinline__ void mixed_quad(const float* __restrict__ Din, float*
     const float4 kzF = *reinterpret_cast<const float4*>(kz + base + p.plane);
     const float4 r4 = *reinterpret_cast<const float4*>(Rin + base);
     const float4 dp4 = prev0 ? make_float4(0.f, 0.f, 0.f, 0.f) : *reinterpret_cast<const float4*>(Dio + base);
-    // west neighbour of cell i0, east neighbour of cell i0+3, east face of cell i0+3
-    float dW = 0.f, dE = 0.f, kE3 = 0.f;
-    if (i0 > 0) dW = lane > 0 ? dW_sh : Din[base - 1];
-    if (i0 + 4 < p.nx) dE = lane < 31 ? dE_sh : Din[base + 4];
-    if (i0 + 3 < p.nx) kE3 = (lane < 31 && q < p.nq - 1) ? kE_sh : kx[base + 4];
-    const float mom = s.mom, dh2 = s.dh2, cX = s.cX, _dx = s._dx, _dy = s._dy, _dz = s._dz;
-    const float _dx2 = __fmul_rn(_dx, _dx), _dy2 = __fmul_rn(_dy, _dy), _dz2 = __fmul_rn(_dz, _dz);
-    float outD[4], outF[4];
-#pragma unroll
-    for (int m = 0; m < 4; ++m) {
-        const int i = i0 + m;
-        const float xc = c4(d, m);
-        const float xw = (i == 0) ? ghost(bc, 0, xc) : (m == 0 ? dW : c4(d, m - 1));
-        const float xe = (i == p.nx - 1) ? ghost(bc, 1, xc) : (m == 3 ? dE : c4(d, m + 1));
-        const float xs = south ? c4(dS, m) : ghost(bc, 2, xc);
-        const float xn = north ? c4(dN, m) : ghost(bc, 3, xc);
-        const float xb = back ? c4(dB, m) : ghost(bc, 4, xc);
-        const float xf = front ? c4(dF, m) : ghost(bc, 5, xc);
-        const float kW = c4(kx4, m), kE = m == 3 ? kE3 : c4(kx4, m + 1);
-        const float kS = c4(kyS, m), kN = c4(kyN, m), kB = c4(kzB, m), kF = c4(kzF, m);
-        float f, xn1;
-        mixed_cell(xc, xw, xe, xs, xn, xb, xf, kW, kE, kS, kN, kB, kF, c4(r4, m), c4(dp4, m), mom, dh2, cX, _dx, _dy,
-                   _dz, _dx2, _dy2, _dz2, f, xn1);
-        const bool valid = i < p.nx;
-        outD[m] = valid ? xn1 : 0.f;
-        outF[m] = valid ? f : 0.f;
-    }
-    if (!act) return;
-    *reinterpret_cast<float4*>(Dio + base) = make_float4(outD[0], outD[1], outD[2], outD[3]);
-    if (STOREF) *reinterpret_cast<float4*>(F + base) = make_float4(outF[0], outF[1], outF[2], outF[3]);
+    float dW, dE, kE3;
+    quad_x_edges(Din, kx, d, kx4, base, i0, q, p, lane, dW, dE, kE3);
+    quad_cells<STOREF>(d, kx4, dS, dN, dB, dF, kyS, kyN, kzB, kzF, r4, dp4, dW, dE, kE3, south, north, back, front,
+                       i0, p, s, bc, Dio, F, base, act);
 }
 
+// The same update for the quad column t (q, j) on planes k0 .. k1-1 in turn:
+// the plane below and the plane above (D and the z-faces) stay in registers
+// from one plane to the next, so a plane loads nine quads instead of twelve
+// and the quad's indices are computed once.  Bit-identical to mixed_quad
+// plane by plane (same neighbours, same quad_cells).
+template <bool STOREF>
+__device__ __forceinline__ void mixed_quad_march(const float* __restrict__ Din, float* __restrict__ Dio,
+                                                 const float* __restrict__ Rin, const float* __restrict__ kx,
+                                                 const float* __restrict__ ky, const float* __restrict__ kz,
+                                                 float* __restrict__ F, const MixScal& s, bool prev0,
+                                                 const BC6<float>& bc, const Pad& p, int t, int k0, int k1, int lane,
+                                                 bool live) {
+    const int q = t % p.nq;
+    int j = t / p.nq;
+    const bool act = live && j < p.ny;
+    if (j >= p.ny) j = p.ny - 1;
+    const int i0 = 4 * q;
+    const bool south = j > 0, north = j < p.ny - 1;
+    long long base = i0 + (long long)p.PX * j + p.plane * k0;
+    float4 d = *reinterpret_cast<const float4*>(Din + base);
+    float4 dB = k0 > 0 ? *reinterpret_cast<const float4*>(Din + base - p.plane) : d;
+    float4 kzB = *reinterpret_cast<const float4*>(kz + base);
+    for (int k = k0; k < k1; ++k, base += p.plane) {
+        const bool back = k > 0, front = k < p.nz - 1;
+        const float4 dF = front ? *reinterpret_cast<const float4*>(Din + base + p.plane) : d;
+        const float4 kzF = *reinterpret_cast<const float4*>(kz + base + p.plane);
+        const float4 kx4 = *reinterpret_cast<const float4*>(kx + base);
+        const float4 dS = south ? *reinterpret_cast<const float4*>(Din + base - p.PX) : d;
+        const float4 dN = north ? *reinterpret_cast<const float4*>(Din + base + p.PX) : d;
+        const float4 kyS = *reinterpret_cast<const float4*>(ky + base);
+        const float4 kyN = *reinterpret_cast<const float4*>(ky + base + p.PX);
+        const float4 r4 = *reinterpret_cast<const float4*>(Rin + base);
+        const float4 dp4 = prev0 ? make_float4(0.f, 0.f, 0.f, 0.f) : *reinterpret_cast<const float4*>(Dio + base);
+        float dW, dE, kE3;
+        quad_x_edges(Din, kx, d, kx4, base, i0, q, p, lane, dW, dE, kE3);
+        quad_cells<STOREF>(d, kx4, dS, dN, dB, dF, kyS, kyN, kzB, kzF, r4, dp4, dW, dE, kE3, south, north, back,
+                           front, i0, p, s, bc, Dio, F, base, act);
+        dB = d;
+        d = dF;
+        kzB = kzF;
+    }
+}
 // Launch shape of k_mixed_inner: 64-thread blocks, 16 per SM (64 registers,
 // half the SM's threads).  Measured at 255^3: 76.4 us per iteration against
 // 77.0 (128 x 8), 77.9 (32 x 32) and 78.1 (256 x 4); fewer registers spill,
@@ -613,6 +681,7 @@ struct EnsLaunch {
     int nblk;                             // blocks of this launch
     int block0[kEnsMaxPerLaunch + 1];     // first block of each member (block0[n] = nblk)
     int quads[kEnsMaxPerLaunch];          // quads per plane (nq * ny) of each member
+    int nbq[kEnsMaxPerLaunch];            // z-march kernel: blocks per plane (ceil(quads / BS))
     EnsInner rec[kEnsMaxPerLaunch];
 };
 static_assert(sizeof(EnsLaunch) <= 32000, "batched launch parameters exceed the 32 KB kernel parameter space");
@@ -637,6 +706,29 @@ __global__ void __launch_bounds__(BS) k_ens_inner(const __grid_constant__ EnsLau
     if (!live) k = e.P.nz - 1;
     mixed_quad<STOREF>(e.D[parity], e.D[parity ^ 1], e.Rin, e.kx, e.ky, e.kz, e.F, e.s, prev0 != 0, e.bc, e.P, t, k,
                        threadIdx.x & 31, live);
+}
+
+// The same iteration with each thread marching one quad column over KC planes
+// (mixed_quad_march): a member's blocks are nbq per plane range (BS quads of
+// a plane each) times ceil(nz / KC) plane ranges.
+template <bool STOREF, int BS, int KC>
+__global__ void __launch_bounds__(BS) k_ens_march(const __grid_constant__ EnsLaunch L, int parity, int prev0) {
+    int lo = 0, hi = L.n;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if ((int)blockIdx.x >= L.block0[mid]) lo = mid;
+        else hi = mid;
+    }
+    const EnsInner& e = L.rec[lo];
+    const int lb = (int)blockIdx.x - L.block0[lo];
+    const int nbq = L.nbq[lo];
+    const int bz = lb / nbq, bq = lb - bz * nbq;
+    const int pq = L.quads[lo];
+    const int t = bq * BS + (int)threadIdx.x;
+    const bool live = t < pq;
+    const int k0 = bz * KC, k1 = min(e.P.nz, k0 + KC);
+    mixed_quad_march<STOREF>(e.D[parity], e.D[parity ^ 1], e.Rin, e.kx, e.ky, e.kz, e.F, e.s, prev0 != 0, e.bc, e.P,
+                             live ? t : pq - 1, k0, k1, threadIdx.x & 31, live);
 }
 
 // FP64 check / refresh iteration of the mixed solver (see above).  FP64
@@ -1042,16 +1134,30 @@ struct Carve {
     }
 };
 
-constexpr int kEnsBS[3] = {64, 128, 256};
+// Tile shapes of the batched iteration the autotuner chooses from: threads
+// per block and planes per thread (0: one plane, k_ens_inner; KC: a z-march
+// over KC planes, k_ens_march).
+struct EnsCfg {
+    int bs, kc;
+};
+constexpr int kEnsNCfg = 6;
+constexpr int kEnsNCfgMax = 8;  // tile shapes the CUDA-graph key holds (3 bits)
+static_assert(kEnsNCfg <= kEnsNCfgMax, "tile shapes must fit the graph key");
+constexpr EnsCfg kEnsCfg[kEnsNCfg] = {{64, 0}, {128, 0}, {256, 0}, {64, 8}, {128, 8}, {128, 16}};
 constexpr int kEnsGraphIters = 16;
-constexpr int kEnsTuneRounds = 2;  // timed launches per block size
+constexpr int kEnsTuneRounds = 2;  // timed launches per tile shape
 
 template <bool STOREF>
 void ens_launch_raw(cudaStream_t st, int cfg, const EnsLaunch& L, int parity, int prev0) {
     const unsigned g = (unsigned)L.nblk;
-    if (cfg == 0) k_ens_inner<STOREF, 64><<<g, 64, 0, st>>>(L, parity, prev0);
-    else if (cfg == 1) k_ens_inner<STOREF, 128><<<g, 128, 0, st>>>(L, parity, prev0);
-    else k_ens_inner<STOREF, 256><<<g, 256, 0, st>>>(L, parity, prev0);
+    switch (cfg) {
+    case 0: k_ens_inner<STOREF, 64><<<g, 64, 0, st>>>(L, parity, prev0); break;
+    case 1: k_ens_inner<STOREF, 128><<<g, 128, 0, st>>>(L, parity, prev0); break;
+    case 2: k_ens_inner<STOREF, 256><<<g, 256, 0, st>>>(L, parity, prev0); break;
+    case 3: k_ens_march<STOREF, 64, 8><<<g, 64, 0, st>>>(L, parity, prev0); break;
+    case 4: k_ens_march<STOREF, 128, 8><<<g, 128, 0, st>>>(L, parity, prev0); break;
+    default: k_ens_march<STOREF, 128, 16><<<g, 128, 0, st>>>(L, parity, prev0); break;
+    }
 }
 
 template <bool STOREF>
@@ -1080,6 +1186,14 @@ struct EnsHost {
 
 unsigned long long mix_sig(unsigned long long h, unsigned long long v) {
     return (h ^ v) * 0x100000001b3ULL + 0x9e3779b97f4a7c15ULL;
+}
+
+// Key of the captured graphs: the launch groups' version (unique per build of
+// the groups on this context) and the tile shape, exactly (a hash of the two
+// could let a later solve replay an earlier solve's graph, whose member
+// records and scratch layout are stale).
+unsigned long long graph_sig(unsigned long long version, int cfg) {
+    return (version << 3) | (unsigned long long)cfg;
 }
 
 // Captures the two graphs (windows starting on parity 0 and 1) of the
@@ -1156,7 +1270,7 @@ void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
         HT3D_REQUIRE(I.X && I.R && I.kx && I.ky && I.kz && I.F && I.F0 && I.bc_type6 && I.bc_val6, "null argument");
         const Pad P = make_pad(I.nx, I.ny, I.nz);
         HT3D_REQUIRE(P.size < (1LL << 31), "grid too large for the padded FP32 layout");
-        HT3D_REQUIRE(((long long)P.nq * I.ny * I.nz + kEnsBS[0] - 1) / kEnsBS[0] < (1LL << 30),
+        HT3D_REQUIRE(((long long)P.nq * I.ny * I.nz + kEnsCfg[0].bs - 1) / kEnsCfg[0].bs < (1LL << 30),
                      "member too large for the batched launch");
         H[q].LC = iter_launch(ctx, I.nx, I.ny, I.nz, HT3D_DYREL_ZMARCH);
         maxparts = std::max(maxparts, std::max<long long>(H[q].LC.nblocks, (long long)((I.nx + 31) / 32) *
@@ -1232,13 +1346,24 @@ void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
 
     // ---- launch groups of the members still iterating, for each block size;
     // rebuilt when a check changes the members' scalars or stops a member
-    std::vector<EnsLaunch> groups[3];
+    std::vector<EnsLaunch> groups[kEnsNCfg];
     unsigned long long version = 0;
+    // members in launch order: largest first, so the blocks of the members
+    // with the most work start first and the launch's tail is made of small
+    // members' blocks (longest-processing-time-first); results do not depend
+    // on the order
+    std::vector<int> order;
+    for (int q = 0; q < n; ++q)
+        if (H[q].used) order.push_back(q);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return (long long)in[a].nx * in[a].ny * in[a].nz > (long long)in[b].nx * in[b].ny * in[b].nz;
+    });
     auto build_groups = [&]() {
         version = ++ctx->ens_version;
-        for (int c = 0; c < 3; ++c) {
+        for (int c = 0; c < kEnsNCfg; ++c) {
             groups[c].clear();
-            for (int q = 0; q < n; ++q) {
+            const int bs = kEnsCfg[c].bs, kc = kEnsCfg[c].kc;
+            for (int q : order) {
                 const EnsHost& h = H[q];
                 if (!h.active) continue;
                 if (groups[c].empty() || groups[c].back().n == kEnsMaxPerLaunch) {
@@ -1247,7 +1372,8 @@ void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
                 }
                 EnsLaunch& L = groups[c].back();
                 const long long pq = (long long)h.P.nq * in[q].ny;
-                const long long nb_q = (pq * in[q].nz + kEnsBS[c] - 1) / kEnsBS[c];
+                const long long nbq = (pq + bs - 1) / bs;
+                const long long nb_q = kc == 0 ? (pq * in[q].nz + bs - 1) / bs : nbq * ((in[q].nz + kc - 1) / kc);
                 if ((long long)L.nblk + nb_q >= (1LL << 31) - 1) {  // start a new group before the count overflows
                     groups[c].emplace_back();
                     std::memset(&groups[c].back(), 0, sizeof(EnsLaunch));
@@ -1256,6 +1382,7 @@ void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
                 const int m = G.n++;
                 G.block0[m] = G.nblk;
                 G.quads[m] = (int)pq;
+                G.nbq[m] = (int)nbq;
                 G.nblk += (int)nb_q;
                 G.block0[m + 1] = G.nblk;
                 EnsInner& e = G.rec[m];
@@ -1280,12 +1407,13 @@ void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
         if (H[q].used) shape = mix_sig(mix_sig(mix_sig(mix_sig(shape, q), in[q].nx), in[q].ny), in[q].nz);
     int cfg = -1;
     auto cfg_of = [](int bs) { return bs == 64 ? 0 : (bs == 128 ? 1 : 2); };
-    if (ctx->ens_block) cfg = cfg_of(ctx->ens_block);
-    else if (ctx->ens_tune_key == shape && ctx->ens_tune_bs) cfg = cfg_of(ctx->ens_tune_bs);
+    if (ctx->ens_tile) cfg = ctx->ens_tile - 1;
+    else if (ctx->ens_block) cfg = cfg_of(ctx->ens_block);
+    else if (ctx->ens_tune_key == shape && ctx->ens_tune_cfg) cfg = ctx->ens_tune_cfg - 1;
     bool tuning = cfg < 0;
     int tune_n = 0;
     if (tuning)
-        while ((int)ctx->tune_events.size() < 2 * 3 * kEnsTuneRounds) {
+        while ((int)ctx->tune_events.size() < 2 * kEnsNCfg * kEnsTuneRounds) {
             cudaEvent_t ev;
             HT3D_CUDA(cudaEventCreate(&ev));
             ctx->tune_events.push_back(ev);
@@ -1339,7 +1467,7 @@ void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
                        !is_storef(iter + window))
                     ++window;
                 if (window == kEnsGraphIters) {
-                    graphs = ens_capture(ctx, mix_sig(version, cfg), cfg, groups[cfg]);
+                    graphs = ens_capture(ctx, graph_sig(version, cfg), cfg, groups[cfg]);
                     if (!graphs) window = 1;
                 } else {
                     window = 1;
@@ -1353,7 +1481,7 @@ void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
                 int c = tuning ? 1 : cfg;
                 const bool timed = tuning && !storef;
                 if (timed) {
-                    c = tune_n % 3;
+                    c = tune_n % kEnsNCfg;
                     HT3D_CUDA(cudaEventRecord(ctx->tune_events[2 * tune_n], ctx->stream));
                 }
                 const int nl = storef ? ens_launch_all<true>(ctx->stream, c, groups[c], parity, prev0)
@@ -1362,14 +1490,14 @@ void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
                 timer.count();
                 if (timed) {
                     HT3D_CUDA(cudaEventRecord(ctx->tune_events[2 * tune_n + 1], ctx->stream));
-                    if (++tune_n == 3 * kEnsTuneRounds) {
+                    if (++tune_n == kEnsNCfg * kEnsTuneRounds) {
                         HT3D_CUDA(cudaEventSynchronize(ctx->tune_events[2 * tune_n - 1]));
                         float best = 0.f;
-                        for (int cc = 0; cc < 3; ++cc) {
+                        for (int cc = 0; cc < kEnsNCfg; ++cc) {
                             float sum = 0.f;
                             for (int r = 0; r < kEnsTuneRounds; ++r) {
                                 float ms = 0.f;
-                                const int t = r * 3 + cc;
+                                const int t = r * kEnsNCfg + cc;
                                 HT3D_CUDA(cudaEventElapsedTime(&ms, ctx->tune_events[2 * t], ctx->tune_events[2 * t + 1]));
                                 sum += ms;
                             }
@@ -1380,7 +1508,7 @@ void ht3d_ensemble_solve_mixed(ht3d_ctx* ctx, EnsSolveInst* in, int n) {
                         }
                         tuning = false;
                         ctx->ens_tune_key = shape;
-                        ctx->ens_tune_bs = kEnsBS[cfg];
+                        ctx->ens_tune_cfg = cfg + 1;
                     }
                 }
             }

@@ -54,7 +54,8 @@ struct ht3d_ctx {
     int ens_block = 0;                    // threads per block of the batched kernel (0 = autotune)
     int ens_graphs = 1;                   // replay windows of inner iterations as CUDA graphs
     unsigned long long ens_tune_key = 0;  // ensemble signature the tuned block size belongs to
-    int ens_tune_bs = 0;
+    int ens_tune_cfg = 0;                 // tuned tile shape of that ensemble (index + 1)
+    int ens_tile = 0;                     // fixed tile shape of the batched iteration (index + 1, 0 = autotune)
     std::vector<cudaEvent_t> tune_events;
     unsigned long long ens_version = 0;   // bumped whenever the batched launch parameters change
     unsigned long long ens_graph_sig = 0; // launch parameters the captured graphs carry

@@ -69,8 +69,9 @@ extern "C" {
 #define HT3D_TUNE_TIME_INNER 3      /* 1: the mixed solver brackets every run of consecutive
                                        FP32 inner-iteration launches with CUDA events on the
                                        ctx stream (read back by ht3d_ctx_inner_timing)    */
-#define HT3D_TUNE_ENS_BLOCK 4       /* threads per block of the batched ensemble iteration:
-                                       0 = autotune on first use (64/128/256), or fixed   */
+#define HT3D_TUNE_ENS_BLOCK 4       /* threads per block of the batched ensemble iteration
+                                       with one plane per thread: 64/128/256 fixes it, 0
+                                       leaves the tile shape to HT3D_TUNE_ENS_TILE        */
 #define HT3D_TUNE_ENS_GRAPH 5       /* 1 (default): replay windows of 16 batched inner
                                        iterations as CUDA graphs; 0: launch one by one    */
 #define HT3D_TUNE_TEMPORAL 6        /* mixed form: 0 = one FP32 inner iteration per launch;
@@ -81,6 +82,12 @@ extern "C" {
                                        per pass on every grid, that many planes per chunk;
                                        bit-identical results (255^3: 59.6 against 75.8 us
                                        per iteration)                                    */
+#define HT3D_TUNE_ENS_TILE 8        /* tile shape of the batched ensemble iteration: 0 =
+                                       autotune on first use of an ensemble shape over
+                                       six shapes, or 1..6 fixed: threads per block x planes
+                                       per thread = 64x1, 128x1, 256x1, 64x8 (z-march),
+                                       128x8, 128x16; overrides HT3D_TUNE_ENS_BLOCK;
+                                       bit-identical results                             */
 #define HT3D_TUNE_WAIT_TEST 7       /* test hook of the bounded waits: v > 0 makes the next
                                        two-iteration pass (HT3D_TUNE_TEMPORAL) skip the
                                        copies of plane v - 1 and give up after 4096 polls;

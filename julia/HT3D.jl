@@ -43,6 +43,7 @@ const TUNE_TIME_INNER = Cint(3)
 const TUNE_ENS_BLOCK = Cint(4)
 const TUNE_ENS_GRAPH = Cint(5)
 const TUNE_TEMPORAL = Cint(6)
+const TUNE_ENS_TILE = Cint(8)
 const TUNE_WAIT_TEST = Cint(7)
 
 # ---------------------------------------------------------------- structs

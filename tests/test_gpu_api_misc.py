@@ -43,6 +43,7 @@ def test_named_iterations_equal_generic(ctx, which):
 
 @pytest.mark.parametrize("key,value", [(abi.TUNE_DYREL_VARIANT, 3), (abi.TUNE_MIXED_REFRESH, -1),
                                        (abi.TUNE_TIME_INNER, 2), (abi.TUNE_ENS_BLOCK, 100),
-                                       (abi.TUNE_ENS_GRAPH, 5), (abi.TUNE_TEMPORAL, -3), (abi.TUNE_WAIT_TEST, -1), (99, 0)])
+                                       (abi.TUNE_ENS_GRAPH, 5), (abi.TUNE_TEMPORAL, -3), (abi.TUNE_WAIT_TEST, -1),
+                                       (abi.TUNE_ENS_TILE, 7), (99, 0)])
 def test_tuning_rejects_bad_values(ctx, key, value):
     assert ctx.lib.ht3d_ctx_set_tuning(ctx.ptr, key, value) == abi.ERR_ARG

@@ -1,7 +1,7 @@
 """Batched ensemble step (ht3d_ensemble_step) against the same members stepped
 one by one with ht3d_step_hrl.  The batched mixed solve runs the members'
 pseudo-iterations in lockstep (one launch over all members, CUDA-graph windows,
-tuned block size) but every kernel, schedule and reduction of a member is the
+tuned tile shape) but every kernel, schedule and reduction of a member is the
 single-instance one: the results must agree bit for bit."""
 import numpy as np
 import pytest
@@ -59,13 +59,19 @@ def tuned(ctx):
     yield ctx
     ctx.set_tuning(abi.TUNE_MIXED_REFRESH, 512)
     ctx.set_tuning(abi.TUNE_ENS_BLOCK, 0)
+    ctx.set_tuning(abi.TUNE_ENS_TILE, 0)
     ctx.set_tuning(abi.TUNE_ENS_GRAPH, 1)
 
 
-@pytest.mark.parametrize("block,graphs", [(0, 1), (64, 0), (128, 1), (256, 0)])
-def test_ensemble_mixed_bitwise_equals_sequential(tuned, block, graphs):
+# tile shapes: 0 = autotuned; 1-3 one plane per thread (64/128/256 threads),
+# 4-6 z-marching threads (64x8, 128x8, 128x16 planes); a block size alone
+# selects the one-plane kernel
+@pytest.mark.parametrize("block,tile,graphs", [(0, 0, 1), (64, 0, 0), (128, 0, 1), (256, 0, 0), (0, 4, 1),
+                                               (0, 5, 0), (0, 6, 1)])
+def test_ensemble_mixed_bitwise_equals_sequential(tuned, block, tile, graphs):
     ctx = tuned
     ctx.set_tuning(abi.TUNE_ENS_BLOCK, block)
+    ctx.set_tuning(abi.TUNE_ENS_TILE, tile)
     ctx.set_tuning(abi.TUNE_ENS_GRAPH, graphs)
     base = members_np()
     seq, ens = to_device(base), to_device(base)
@@ -81,6 +87,21 @@ def test_ensemble_mixed_bitwise_equals_sequential(tuned, block, graphs):
     assert all(m.st_thermal.converged and m.st_darcy.converged for m in ens)
     # one launch per lockstep pseudo-iteration instead of one per member
     assert l2 - l1 < l1 - l0
+
+
+def test_ensemble_tile_shape_changes_between_steps(tuned):
+    """Consecutive solves with different tile shapes (their CUDA graphs are
+    keyed by the launch groups' version and the shape): every step stays bit
+    for bit equal to the per-member steps."""
+    ctx = tuned
+    base = members_np(SIZES[:3])
+    seq, ens = to_device(base), to_device(base)
+    for tile in (1, 4, 2, 5, 3, 6, 0):
+        ctx.set_tuning(abi.TUNE_ENS_TILE, tile)
+        step_sequential(ctx, seq, abi.MIXED)
+        assert api.ensemble_step(ctx, ens, abi.MIXED) == [abi.OK] * len(ens)
+        torch.cuda.synchronize()
+        assert_same(ens, seq)
 
 
 def test_ensemble_fp64_equals_sequential(ctx):
