@@ -290,6 +290,7 @@ struct LineSrc {
 // Balanced segments: kMarchL cells per thread on average, at least 48 each
 // when a line has more than one.
 constexpr int kMarchL = 64;
+constexpr int kMarchUnroll = 4;  // steps per software-pipelined body of the y/z march
 __host__ __device__ __forceinline__ int march_chunks(int n) { return n < 3 * kMarchL / 2 ? 1 : (n + kMarchL / 2) / kMarchL; }
 
 template <int AXIS, int QUIRK>
@@ -318,7 +319,34 @@ __global__ void __launch_bounds__(128) k_weno_march_f32(const float* __restrict_
     const int cA = c1 < n ? c1 : n - 3;  // steps whose stage-1 point c + 3 is inside the line
     const int cB = min(cA, n - 6);       // ... and whose T0[c + 6] is too
     int c = c0;
-#pragma unroll 4
+    if (cB - c0 >= 2 * kMarchUnroll) {
+        // software pipeline: the T0 and face values of the next kMarchUnroll
+        // steps are loaded while the current ones compute
+        float qt[kMarchUnroll], qv[kMarchUnroll];
+#pragma unroll
+        for (int u = 0; u < kMarchUnroll; ++u) {
+            qt[u] = s.ld(c + 6 + u);
+            qv[u] = s.v(c + 4 + u);
+        }
+        for (; c + 2 * kMarchUnroll <= cB; c += kMarchUnroll) {
+            float nt[kMarchUnroll], nv[kMarchUnroll];
+#pragma unroll
+            for (int u = 0; u < kMarchUnroll; ++u) {
+                nt[u] = s.ld(c + kMarchUnroll + 6 + u);  // < cB + 6 <= n
+                nv[u] = s.v(c + kMarchUnroll + 4 + u);
+            }
+#pragma unroll
+            for (int u = 0; u < kMarchUnroll; ++u) s.put(c + u, M.step(qt[u], qv[u], dt));
+#pragma unroll
+            for (int u = 0; u < kMarchUnroll; ++u) {
+                qt[u] = nt[u];
+                qv[u] = nv[u];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kMarchUnroll; ++u) s.put(c + u, M.step(qt[u], qv[u], dt));
+        c += kMarchUnroll;
+    }
     for (; c < cB; ++c) s.put(c, M.step(s.ld(c + 6), s.v(c + 4), dt));
     for (; c < cA; ++c) s.put(c, M.step(s.t0(c + 6), s.v(c + 4), dt));
     if (c1 == n) {
