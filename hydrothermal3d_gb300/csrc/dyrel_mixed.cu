@@ -131,6 +131,13 @@ __device__ __forceinline__ void mixed_cell(float xc, float xw, float xe, float x
     xnew = __fmaf_rn(mom, __fsub_rn(xc, xprev), __fmaf_rn(-dh2, f, xc));
 }
 
+// Ghost value of the FP32 correction fields: their BCs are homogeneous (the
+// Dirichlet value lives in the FP64 state), so a ghost is -v (Dirichlet) or v
+// (Neumann): one select instead of the general 2 value - v.  Every FP32
+// kernel of the mixed form uses it, so they agree bit for bit (a zero ghost
+// may carry the other sign than 0 - v would).
+__device__ __forceinline__ float hghost(const BC6<float>& bc, int f, float v) { return bc.dir[f] ? -v : v; }
+
 // x-neighbours across a quad's edges: the west neighbour of cell i0, the east
 // neighbour of cell i0+3 and the east face of cell i0+3, from the adjacent
 // lanes (same row) by warp shuffles, or by a scalar load at a warp edge.
@@ -166,12 +173,12 @@ __device__ __forceinline__ void quad_cells(const float4& d, const float4& kx4, c
     for (int m = 0; m < 4; ++m) {
         const int i = i0 + m;
         const float xc = c4(d, m);
-        const float xw = (i == 0) ? ghost(bc, 0, xc) : (m == 0 ? dW : c4(d, m - 1));
-        const float xe = (i == p.nx - 1) ? ghost(bc, 1, xc) : (m == 3 ? dE : c4(d, m + 1));
-        const float xs = south ? c4(dS, m) : ghost(bc, 2, xc);
-        const float xn = north ? c4(dN, m) : ghost(bc, 3, xc);
-        const float xb = back ? c4(dB, m) : ghost(bc, 4, xc);
-        const float xf = front ? c4(dF, m) : ghost(bc, 5, xc);
+        const float xw = (i == 0) ? hghost(bc, 0, xc) : (m == 0 ? dW : c4(d, m - 1));
+        const float xe = (i == p.nx - 1) ? hghost(bc, 1, xc) : (m == 3 ? dE : c4(d, m + 1));
+        const float xs = south ? c4(dS, m) : hghost(bc, 2, xc);
+        const float xn = north ? c4(dN, m) : hghost(bc, 3, xc);
+        const float xb = back ? c4(dB, m) : hghost(bc, 4, xc);
+        const float xf = front ? c4(dF, m) : hghost(bc, 5, xc);
         const float kW = c4(kx4, m), kE = m == 3 ? kE3 : c4(kx4, m + 1);
         const float kS = c4(kyS, m), kN = c4(kyN, m), kB = c4(kzB, m), kF = c4(kzF, m);
         float f, xn1;
@@ -410,12 +417,12 @@ __device__ __forceinline__ void pair_quad(const QuadIn& c, float4 xp, float dW, 
     for (int m = 0; m < 4; ++m) {
         const int i = i0 + m;
         const float xc = c4(c.xc, m);
-        const float xw = (i == 0) ? ghost(bc, 0, xc) : (m == 0 ? dW : c4(c.xc, m - 1));
-        const float xe = (i == p.nx - 1) ? ghost(bc, 1, xc) : (m == 3 ? dE : c4(c.xc, m + 1));
-        const float xs = south ? c4(xs4, m) : ghost(bc, 2, xc);
-        const float xn = north ? c4(xn4, m) : ghost(bc, 3, xc);
-        const float xb = back ? c4(xb4, m) : ghost(bc, 4, xc);
-        const float xf = front ? c4(xf4, m) : ghost(bc, 5, xc);
+        const float xw = (i == 0) ? hghost(bc, 0, xc) : (m == 0 ? dW : c4(c.xc, m - 1));
+        const float xe = (i == p.nx - 1) ? hghost(bc, 1, xc) : (m == 3 ? dE : c4(c.xc, m + 1));
+        const float xs = south ? c4(xs4, m) : hghost(bc, 2, xc);
+        const float xn = north ? c4(xn4, m) : hghost(bc, 3, xc);
+        const float xb = back ? c4(xb4, m) : hghost(bc, 4, xc);
+        const float xf = front ? c4(xf4, m) : hghost(bc, 5, xc);
         const float kE = m == 3 ? c.kE3 : c4(c.kW, m + 1);
         mixed_cell(xc, xw, xe, xs, xn, xb, xf, c4(c.kW, m), kE, c4(c.kS, m), c4(c.kN, m), c4(c.kB, m), c4(c.kF, m),
                    c4(c.r, m), c4(xp, m), s.mom, s.dh2, s.cX, s._dx, s._dy, s._dz, _dx2, _dy2, _dz2, of[m], o[m]);
@@ -432,12 +439,12 @@ __device__ __forceinline__ float pair_cell(const float* d, const float* kxr, con
                                            const BC6<float>& bc, const MixScal& s, float _dx2, float _dy2,
                                            float _dz2) {
     const float xc = d[0];
-    const float xw = (i == 0) ? ghost(bc, 0, xc) : d[-1];
-    const float xe = (i == p.nx - 1) ? ghost(bc, 1, xc) : d[1];
-    const float xs = (j > 0) ? d[-TB_W] : ghost(bc, 2, xc);
-    const float xn = (j < p.ny - 1) ? d[TB_W] : ghost(bc, 3, xc);
-    const float xbb = (k > 0) ? xb : ghost(bc, 4, xc);
-    const float xff = (k < p.nz - 1) ? xf : ghost(bc, 5, xc);
+    const float xw = (i == 0) ? hghost(bc, 0, xc) : d[-1];
+    const float xe = (i == p.nx - 1) ? hghost(bc, 1, xc) : d[1];
+    const float xs = (j > 0) ? d[-TB_W] : hghost(bc, 2, xc);
+    const float xn = (j < p.ny - 1) ? d[TB_W] : hghost(bc, 3, xc);
+    const float xbb = (k > 0) ? xb : hghost(bc, 4, xc);
+    const float xff = (k < p.nz - 1) ? xf : hghost(bc, 5, xc);
     float f, x;
     mixed_cell(xc, xw, xe, xs, xn, xbb, xff, kxr[0], kxr[1], kyr[0], kyr[TB_W], kB, kF, r, xp, s.mom, s.dh2, s.cX,
                s._dx, s._dy, s._dz, _dx2, _dy2, _dz2, f, x);
