@@ -105,17 +105,35 @@ inline MixScal mix_scal(const DyrelScal& s, double dtau_prev) {
 
 // One cell of the FP32 inner iteration (the single place its arithmetic is
 // written, so every kernel that updates a cell rounds alike):
-//     F = (R + cX x + div q(x)) / diag,  x' = x + mom (x - xprev) - dh2 F
+//     F = (R + cX x + div q(x)) * (1 / diag),  x' = x + mom (x - xprev) - dh2 F
 // with q = -k dx on the six faces and diag = sum of k/dx^2 over them + cX;
 // div q is evaluated per axis as dx^2 (k_in (x - x_in) - k_out (x_out - x)).
-// Every operation is an explicit round-to-nearest intrinsic: the compiler may
-// neither contract nor reassociate them, so the value of a cell does not depend
-// on the kernel it is inlined into (k_mixed_inner shares fluxes between the
-// four cells of a quad, k_mixed_inner2 does not).
-__device__ __forceinline__ void mixed_cell(float xc, float xw, float xe, float xs, float xn, float xb, float xf,
-                                           float kW, float kE, float kS, float kN, float kB, float kF, float r,
-                                           float xprev, float mom, float dh2, float cX, float _dx, float _dy,
-                                           float _dz, float _dx2, float _dy2, float _dz2, float& f, float& xnew) {
+// Every operation is an explicit round-to-nearest intrinsic (and 1 / diag one
+// approximate reciprocal): the compiler may neither contract nor reassociate
+// them, so the value of a cell does not depend on the kernel it is inlined
+// into (k_mixed_inner shares fluxes between the four cells of a quad,
+// k_mixed_inner2 does not and hands 1 / diag from its first iteration of a
+// pass to the second).
+// approximate reciprocal (one MUFU operation, ~1 ulp); the diagonals it is
+// applied to are positive normal numbers
+__device__ __forceinline__ float rcp_approx(float v) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v));
+    return r;
+}
+// 1 / diag of a cell: diag = cX + sum over the faces of k/dx^2
+__device__ __forceinline__ float mixed_rdiag(float kW, float kE, float kS, float kN, float kB, float kF, float cX,
+                                             float _dx2, float _dy2, float _dz2) {
+    float diag = __fmaf_rn(__fadd_rn(kW, kE), _dx2, cX);
+    diag = __fmaf_rn(__fadd_rn(kS, kN), _dy2, diag);
+    diag = __fmaf_rn(__fadd_rn(kB, kF), _dz2, diag);
+    return rcp_approx(diag);
+}
+// the cell update given its 1 / diag
+__device__ __forceinline__ void mixed_cell_rd(float xc, float xw, float xe, float xs, float xn, float xb, float xf,
+                                              float kW, float kE, float kS, float kN, float kB, float kF, float r,
+                                              float xprev, float rd, float mom, float dh2, float cX, float _dx2,
+                                              float _dy2, float _dz2, float& f, float& xnew) {
     // dx (qE - qW) with q = -k dx (x_out - x_in) is dx^2 (kW (xc - xw) - kE (xe - xc))
     const float gx = __fmaf_rn(kW, __fsub_rn(xc, xw), -__fmul_rn(kE, __fsub_rn(xe, xc)));
     const float gy = __fmaf_rn(kS, __fsub_rn(xc, xs), -__fmul_rn(kN, __fsub_rn(xn, xc)));
@@ -124,11 +142,16 @@ __device__ __forceinline__ void mixed_cell(float xc, float xw, float xe, float x
     fu = __fmaf_rn(_dx2, gx, fu);
     fu = __fmaf_rn(_dy2, gy, fu);
     fu = __fmaf_rn(_dz2, gz, fu);
-    float diag = __fmaf_rn(__fadd_rn(kW, kE), _dx2, cX);
-    diag = __fmaf_rn(__fadd_rn(kS, kN), _dy2, diag);
-    diag = __fmaf_rn(__fadd_rn(kB, kF), _dz2, diag);
-    f = __fdividef(fu, diag);
+    f = __fmul_rn(fu, rd);
     xnew = __fmaf_rn(mom, __fsub_rn(xc, xprev), __fmaf_rn(-dh2, f, xc));
+}
+__device__ __forceinline__ void mixed_cell(float xc, float xw, float xe, float xs, float xn, float xb, float xf,
+                                           float kW, float kE, float kS, float kN, float kB, float kF, float r,
+                                           float xprev, float mom, float dh2, float cX, float _dx, float _dy,
+                                           float _dz, float _dx2, float _dy2, float _dz2, float& f, float& xnew) {
+    const float rd = mixed_rdiag(kW, kE, kS, kN, kB, kF, cX, _dx2, _dy2, _dz2);
+    mixed_cell_rd(xc, xw, xe, xs, xn, xb, xf, kW, kE, kS, kN, kB, kF, r, xprev, rd, mom, dh2, cX, _dx2, _dy2, _dz2, f,
+                  xnew);
 }
 
 // Ghost value of the FP32 correction fields: their BCs are homogeneous (the
@@ -341,6 +364,7 @@ constexpr int TB_LANES = 32, TB_X = 4 * TB_LANES, TB_Y = HT3D_TB_Y, TB_STAGES = 
 constexpr int TB_OX = TB_X, TB_OY = TB_Y - 2;  // cells of a tile that iteration B updates
 constexpr int TB_W = TB_X + 8;                 // every box: columns x0 - 4 .. x0 + TB_X + 3
 constexpr unsigned kTbWaitLimit = 1u << 22;
+constexpr int kTbRd = 3 * TB_Y * TB_X;  // floats of the three A-result planes (and of the three 1 / diag planes)
 
 struct __align__(128) TbStage {
     float D[TB_Y + 2][TB_W];    // rows y0-1 .. y0+TB_Y
@@ -406,13 +430,17 @@ struct QuadIn {
 };
 
 // One iteration on a quad: the four cells of mixed_quad with the same ghost
-// rules (i0, j, k: the quad's first cell; neighbours passed in).
+// rules (i0, j, k: the quad's first cell; neighbours passed in).  HAVE_RD:
+// the cells' 1 / diag are given in rd4; else they are computed and returned
+// in rd4 (iteration A hands them to iteration B, whose cells and face
+// conductivities are the same).
+template <bool HAVE_RD>
 __device__ __forceinline__ void pair_quad(const QuadIn& c, float4 xp, float dW, float dE, float4 xs4, float4 xn4,
                                           float4 xb4, float4 xf4, int i0, int j, int k, const Pad& p,
                                           const BC6<float>& bc, const MixScal& s, float _dx2, float _dy2, float _dz2,
-                                          float4& xout, float4& fout) {
+                                          float4& rd4, float4& xout, float4& fout) {
     const bool south = j > 0, north = j < p.ny - 1, back = k > 0, front = k < p.nz - 1;
-    float o[4], of[4];
+    float o[4], of[4], rd[4];
 #pragma unroll
     for (int m = 0; m < 4; ++m) {
         const int i = i0 + m;
@@ -424,10 +452,14 @@ __device__ __forceinline__ void pair_quad(const QuadIn& c, float4 xp, float dW, 
         const float xb = back ? c4(xb4, m) : hghost(bc, 4, xc);
         const float xf = front ? c4(xf4, m) : hghost(bc, 5, xc);
         const float kE = m == 3 ? c.kE3 : c4(c.kW, m + 1);
-        mixed_cell(xc, xw, xe, xs, xn, xb, xf, c4(c.kW, m), kE, c4(c.kS, m), c4(c.kN, m), c4(c.kB, m), c4(c.kF, m),
-                   c4(c.r, m), c4(xp, m), s.mom, s.dh2, s.cX, s._dx, s._dy, s._dz, _dx2, _dy2, _dz2, of[m], o[m]);
+        rd[m] = HAVE_RD ? c4(rd4, m)
+                        : mixed_rdiag(c4(c.kW, m), kE, c4(c.kS, m), c4(c.kN, m), c4(c.kB, m), c4(c.kF, m), s.cX,
+                                      _dx2, _dy2, _dz2);
+        mixed_cell_rd(xc, xw, xe, xs, xn, xb, xf, c4(c.kW, m), kE, c4(c.kS, m), c4(c.kN, m), c4(c.kB, m),
+                      c4(c.kF, m), c4(c.r, m), c4(xp, m), rd[m], s.mom, s.dh2, s.cX, _dx2, _dy2, _dz2, of[m], o[m]);
         if (i >= p.nx) o[m] = of[m] = 0.f;  // padding stays zero
     }
+    if (!HAVE_RD) rd4 = make_float4(rd[0], rd[1], rd[2], rd[3]);
     xout = make_float4(o[0], o[1], o[2], o[3]);
     fout = make_float4(of[0], of[1], of[2], of[3]);
 }
@@ -463,7 +495,8 @@ __global__ void __launch_bounds__(TB_LANES* TB_Y, TB_Y <= 8 ? 2 : 1) k_mixed_inn
     unsigned char* base = tb_raw + ((128 - (smem_u32(tb_raw) & 127)) & 127);
     TbStage* st = reinterpret_cast<TbStage*>(base);
     float* xbuf = reinterpret_cast<float*>(base + sizeof(TbStage) * TB_STAGES);  // A's result, three planes
-    uint64_t* bar = reinterpret_cast<uint64_t*>(base + sizeof(TbStage) * TB_STAGES + sizeof(float) * 3 * TB_Y * TB_X);
+    // A's 1 / diag, three planes, at kTbRd floats after the result of the same plane
+    uint64_t* bar = reinterpret_cast<uint64_t*>(base + sizeof(TbStage) * TB_STAGES + sizeof(float) * 2 * kTbRd);
     __shared__ int abort_flag;
     const int lane = threadIdx.x, ty = threadIdx.y, tid = lane + TB_LANES * ty;
     const int x0 = blockIdx.x * TB_OX, y0 = blockIdx.y * TB_OY - 1;  // tile origin (x0 % 4 == 0)
@@ -569,10 +602,12 @@ __global__ void __launch_bounds__(TB_LANES* TB_Y, TB_Y <= 8 ? 2 : 1) k_mixed_inn
             const float4 xp = lds4(&S0->Dp[0][0] + oK);
             const float4 xs4 = lds4(d0 - TB_W), xn4 = lds4(d0 + TB_W);
             const float4 xf4 = lds4(&S1->D[0][0] + oD);
-            float4 fa;
-            pair_quad(ca, xp, d0[-1], d0[4], xs4, xn4, dm1, xf4, i0, j, pl, p, bc, s, _dx2, _dy2, _dz2, da, fa);
+            float4 fa, rda;
+            pair_quad<false>(ca, xp, d0[-1], d0[4], xs4, xn4, dm1, xf4, i0, j, pl, p, bc, s, _dx2, _dy2, _dz2, rda, da,
+                             fa);
             dm1 = ca.xc;
             *reinterpret_cast<float4*>(xw_) = da;
+            *reinterpret_cast<float4*>(xw_ + kTbRd) = rda;
         }
         float ea = 0.f;  // the end cell's A result at plane pl
         if (ok && pl < p.nz && endc) {
@@ -605,9 +640,9 @@ __global__ void __launch_bounds__(TB_LANES* TB_Y, TB_Y <= 8 ? 2 : 1) k_mixed_inn
             QuadIn c = cb;
             const float4 xprev = c.xc;  // B's previous correction: A's input
             c.xc = dpc;
-            float4 xb2, fb;
-            pair_quad(c, xprev, bW, bE, lds4(xr_ - TB_X), lds4(xr_ + TB_X), dpm, da, i0, j, q, p, bc, s, _dx2, _dy2,
-                      _dz2, xb2, fb);
+            float4 xb2, fb, rdb = lds4(xr_ + kTbRd);
+            pair_quad<true>(c, xprev, bW, bE, lds4(xr_ - TB_X), lds4(xr_ + TB_X), dpm, da, i0, j, q, p, bc, s, _dx2,
+                            _dy2, _dz2, rdb, xb2, fb);
             *reinterpret_cast<float4*>(outD1) = dpc;
             *reinterpret_cast<float4*>(outD2) = xb2;
             if (STOREF) *reinterpret_cast<float4*>(outF) = fb;
@@ -629,7 +664,7 @@ __global__ void __launch_bounds__(TB_LANES* TB_Y, TB_Y <= 8 ? 2 : 1) k_mixed_inn
         xn_ = u;
     }
 }
-constexpr size_t kTbSmem = 128 + sizeof(TbStage) * TB_STAGES + sizeof(float) * 3 * TB_Y * TB_X + 8 * TB_STAGES;
+constexpr size_t kTbSmem = 128 + sizeof(TbStage) * TB_STAGES + sizeof(float) * 2 * kTbRd + 8 * TB_STAGES;
 
 // cuTensorMapEncodeTiled, fetched from the driver at run time (no libcuda link)
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
