@@ -356,7 +356,7 @@ __global__ void __launch_bounds__(128) k_weno_march_f32(const float* __restrict_
     }
 }
 
-// x: a warp marches 32 consecutive rows (one per lane) along a segment of x.
+// x: a warp marches 32 consecutive rows (one per lane) along x.
 // T0 and Vx reach shared memory through per-row rings of three 8-cell tiles,
 // filled by asynchronous 4-byte copies one tile ahead of the march; a step
 // reads its own row's ring (odd row pitch: the 32 lanes hit 32 banks) and
@@ -394,6 +394,11 @@ struct RingSrc {
     __device__ __forceinline__ void put(int c, float val) const { t[col(c)] = val; }
 };
 
+// The x sweep updates T in place, so a row is never split between warps:
+// a segment's halo (six cells on each side) would be the neighbouring
+// segment's cells, which another block may already have overwritten.  Within
+// a warp the ring's copies run ahead of its stores (tile v + 4 is fetched
+// after tile v + 1 is stored), so whole rows are safe.
 template <int QUIRK>
 __global__ void __launch_bounds__(32 * kXWarps) k_weno_xstream_f32(float* __restrict__ T, const float* __restrict__ Vx,
                                                                    float dt, float h, WenoBCf bc, int nx, int ny,
@@ -404,8 +409,7 @@ __global__ void __launch_bounds__(32 * kXWarps) k_weno_xstream_f32(float* __rest
     const long long row0 = ((long long)blockIdx.x * kXWarps + warp) * 32;
     if (row0 >= rows) return;  // whole warps only
     const int n = nx;
-    const int K = march_chunks(n);
-    const int c0 = (int)((long long)blockIdx.y * n / K), c1 = (int)((long long)(blockIdx.y + 1) * n / K);
+    const int c0 = 0, c1 = n;  // whole rows (see above)
     const int b0 = c0 - kXW;
     float* tr = ring[warp][0];
     float* vr = ring[warp][1];
@@ -600,7 +604,7 @@ float* axis_f32(ht3d_ctx* ctx, float* cur, float* other, float* tmp, const float
     if constexpr (AXIS == 0) {
         if (!periodic) {
             const long long rows = (long long)ny * nz, per_block = 32LL * kXWarps;
-            const dim3 g((unsigned)((rows + per_block - 1) / per_block), march_chunks(nx));
+            const dim3 g((unsigned)((rows + per_block - 1) / per_block));
             HT3D_LAUNCH(ctx, k_weno_xstream_f32<QUIRK>, g, 32 * kXWarps, 0, cur, V, dt, h, bcf(bc), nx, ny, nz);
             return cur;
         }

@@ -83,6 +83,31 @@ def test_sweep_f32_segments_against_oracle(ctx, orc, n, variant):
     assert rel_err(got[inner], To[inner]) <= 2e-5
 
 
+@pytest.mark.parametrize("n", [(511, 40, 36), (383, 24, 20), (36, 383, 24), (24, 20, 383)])
+def test_sweep_f32_long_lines_track_fp64(ctx, n):
+    """One FP32 sweep on boxes long along one axis (many segments per line,
+    flow along every axis) within 1e-6 of the FP64 sweep: the FP32 rounding of
+    a sweep is ~1e-7 there, so any cell computed from a stale neighbour (a
+    segment seam read while another block updates it) shows up."""
+    nx, ny, nz = n
+    V = sweep.curl_velocity(nx, ny, nz, seed=6)
+    T0 = sweep.blob(nx, ny, nz)
+    torch.cuda.synchronize()
+    dt = sweep.cfl_dt(nx, ny, nz, cfl=0.5)
+    h = (float(nx), float(ny), float(nz))
+    types, vals = BCS["hrl"]
+    T64 = T0.clone()
+    api.weno5_advect(ctx, T64, *V, dt, *h, types, vals, abi.WENO_V1, abi.FP64)
+    T32 = T0.float().permute(2, 1, 0).contiguous().permute(2, 1, 0)
+    V32 = [v.float().permute(2, 1, 0).contiguous().permute(2, 1, 0) for v in V]
+    api.weno5_advect_f32(ctx, T32, *V32, dt, *h, types, vals, abi.WENO_V1)
+    ctx.synchronize()
+    inner = (slice(1, -1),) * 3
+    ref = T64[inner]
+    assert bool(torch.isfinite(T32[inner]).all())
+    assert float((T32[inner].double() - ref).abs().max()) <= 1e-6 * float(ref.abs().max())
+
+
 def test_sweep_f32_keeps_a_uniform_field(ctx):
     """All differences vanish: a uniform field is advected exactly (Neumann walls)."""
     for n in (19, 67):
