@@ -796,27 +796,17 @@ __global__ void __launch_bounds__(TX* TY) k_mixed_check(
     const int k1 = min(nz, k0 + zchunk);
     double acc[3] = {0.0, 0.0, 0.0};
     float rq_num = 0.f, rq_den = 0.f;
-    // A warp is one row segment of 32 cells (TX = 32): the west neighbour's
-    // fold and the west face flux of a cell are the fold and east flux of the
-    // lane before it (same operands, same expression), taken by warp
-    // shuffles; lanes 0 evaluate theirs.  Every lane of a row that is inside
-    // the grid in y and z runs the loop (lanes past the x end on the last
-    // cell of the row, storing nothing), so the shuffles see all 32 lanes.
-    static_assert(TX == 32, "the check kernel's rows are whole warps");
-    const int lane = threadIdx.x;
-    if (j < ny && k0 < k1) {
-        const bool act = i < nx;
-        const int ic = act ? i : nx - 1;
+    if (i < nx && j < ny && k0 < k1) {
         const int n1 = nx + 2, n2 = ny + 2;
         const long long pl = (long long)n1 * n2, cpl = (long long)nx * ny, pp = p.plane;
-        const long long col = (ic + 1) + (long long)n1 * (j + 1);
-        const long long pcol = ic + (long long)p.PX * j;
+        const long long col = (i + 1) + (long long)n1 * (j + 1);
+        const long long pcol = i + (long long)p.PX * j;
         const double* xcol = Xin + col;
         const float* dcol = Din + pcol;
         double* ocol = Xout + col;
-        const long long ccol = ic + (long long)nx * j;
-        const double* kxcol = kx + ic + (long long)(nx + 1) * j;
-        const double* kycol = ky + ic + (long long)nx * j;
+        const long long ccol = i + (long long)nx * j;
+        const double* kxcol = kx + i + (long long)(nx + 1) * j;
+        const double* kycol = ky + i + (long long)nx * j;
         const double* kzcol = kz + ccol;
         auto fold = [&](long long e, long long pe) { return xcol[e] + (double)dcol[pe]; };
         double xc = fold(pl * (k0 + 1), pp * k0);
@@ -825,18 +815,15 @@ __global__ void __launch_bounds__(TX* TY) k_mixed_check(
         for (int k = k0; k < k1; ++k) {
             const long long e = pl * (k + 1), pe = pp * k;
             const double xf = (k == nz - 1) ? ghost(bc, 5, xc) : fold(e + pl, pe + pp);
-            const double xw_l = __shfl_up_sync(0xffffffffu, xc, 1);
-            const double xe_l = __shfl_down_sync(0xffffffffu, xc, 1);
-            const double xw = (ic == 0) ? ghost(bc, 0, xc) : (lane > 0 ? xw_l : fold(e - 1, pe - 1));
-            const double xe = (ic == nx - 1) ? ghost(bc, 1, xc) : (lane < TX - 1 ? xe_l : fold(e + 1, pe + 1));
+            const double xw = (i == 0) ? ghost(bc, 0, xc) : fold(e - 1, pe - 1);
+            const double xe = (i == nx - 1) ? ghost(bc, 1, xc) : fold(e + 1, pe + 1);
             const double xs = (j == 0) ? ghost(bc, 2, xc) : fold(e - n1, pe - p.PX);
             const double xn = (j == ny - 1) ? ghost(bc, 3, xc) : fold(e + n1, pe + p.PX);
             const long long c = ccol + cpl * k, pc = pcol + pe;
             const double qF = -kzcol[cpl * (k + 1)] * (s._dz * (xf - xc));
             const long long fxo = (long long)(nx + 1) * ny * k, fyo = (long long)nx * (ny + 1) * k;
+            const double qW = -kxcol[fxo] * (s._dx * (xc - xw));
             const double qE = -kxcol[fxo + 1] * (s._dx * (xe - xc));
-            const double qW_l = __shfl_up_sync(0xffffffffu, qE, 1);
-            const double qW = lane > 0 ? qW_l : -kxcol[fxo] * (s._dx * (xc - xw));
             const double qS = -kycol[fyo] * (s._dy * (xc - xs));
             const double qN = -kycol[fyo + nx] * (s._dy * (xn - xc));
             const double fu = R[c] + s.cX * xc + s._dx * (qE - qW) + s._dy * (qN - qS) + s._dz * (qF - qB);
@@ -846,24 +833,22 @@ __global__ void __launch_bounds__(TX* TY) k_mixed_check(
             const float f0old = __fdiv_rn(__fsub_rn(dprev, dcol[pe]), s32.dtau_prev);
             const float f0 = __fmaf_rn(s32.h1, f0old, __fmul_rn(s32.h2, f32));
             const float d = __fmul_rn(s32.dtau, f0);
-            if (act) {
-                if (CHECK) {
-                    acc[0] += fabs(fu);
-                    rq_num = __fmaf_rn(-d, __fsub_rn(f32, F32[pc]), rq_num);
-                    rq_den = __fmaf_rn(d, d, rq_den);
-                    F64[c] = f;
-                }
-                F32[pc] = f32;
-                Rin[pc] = (float)fu;
-                Dio[pc] = -d;
-                ocol[e] = xc;
-                if (ic == 0) ocol[e - 1] = xw;
-                if (ic == nx - 1) ocol[e + 1] = xe;
-                if (j == 0) ocol[e - n1] = xs;
-                if (j == ny - 1) ocol[e + n1] = xn;
-                if (k == 0) ocol[e - pl] = xb;
-                if (k == nz - 1) ocol[e + pl] = xf;
+            if (CHECK) {
+                acc[0] += fabs(fu);
+                rq_num = __fmaf_rn(-d, __fsub_rn(f32, F32[pc]), rq_num);
+                rq_den = __fmaf_rn(d, d, rq_den);
+                F64[c] = f;
             }
+            F32[pc] = f32;
+            Rin[pc] = (float)fu;
+            Dio[pc] = -d;
+            ocol[e] = xc;
+            if (i == 0) ocol[e - 1] = xw;
+            if (i == nx - 1) ocol[e + 1] = xe;
+            if (j == 0) ocol[e - n1] = xs;
+            if (j == ny - 1) ocol[e + n1] = xn;
+            if (k == 0) ocol[e - pl] = xb;
+            if (k == nz - 1) ocol[e + pl] = xf;
             xb = xc;
             xc = xf;
             qB = qF;

@@ -257,7 +257,11 @@ void ht3d_weno5_advect_impl(ht3d_ctx* ctx, double* Tc_ex, const double* Vx, cons
         if (quirk) weno_all<1, 0>(ctx, Tc_ex, T1, V, dt, h, bc, nx, ny, nz);
         else weno_all<0, 0>(ctx, Tc_ex, T1, V, dt, h, bc, nx, ny, nz);
     } else {
-        if (quirk) weno_all<1, 1>(ctx, Tc_ex, T1, V, dt, h, bc, nx, ny, nz);
+        bool periodic = false;
+        for (int a = 0; a < 3; ++a)
+            periodic = periodic || bc[a].typeL == HT3D_BC_PERIODIC || bc[a].typeR == HT3D_BC_PERIODIC;
+        if (!periodic) ht3d_weno5_mixed_march(ctx, Tc_ex, T1, V, dt, h, bc_type6, bc_val6, quirk, nx, ny, nz);
+        else if (quirk) weno_all<1, 1>(ctx, Tc_ex, T1, V, dt, h, bc, nx, ny, nz);
         else weno_all<0, 1>(ctx, Tc_ex, T1, V, dt, h, bc, nx, ny, nz);
     }
 }

@@ -116,3 +116,8 @@ __device__ __forceinline__ T line_at(const T* __restrict__ line, long long strid
 
 
 }  // namespace
+
+// the mixed form's fused sweep on the march kernels (weno_f32.cu): the BCs as
+// ht3d_weno5_advect takes them, none periodic
+void ht3d_weno5_mixed_march(ht3d_ctx* ctx, double* T, double* S, const double* const* V, double dt, const double* h,
+                            const int* bc_type6, const double* bc_val6, bool quirk, int nx, int ny, int nz);

@@ -34,6 +34,22 @@ __device__ __forceinline__ float weno_ghost(float v, bool left, const WenoBC& bc
     return t == HT3D_BC_DIRICHLET ? (float)(2 * (left ? bc.valL : bc.valR)) - v : v;
 }
 
+// Dirichlet/Neumann ends of an FP32 sweep: g = (float)(2 * value), so a ghost
+// g - v rounds like the reference's 2 value - v evaluated in FP32.
+struct WenoBCf {
+    int typeL, typeR;
+    float gL, gR;
+};
+__device__ __forceinline__ float weno_ghost(float v, bool left, const WenoBCf& bc) {
+    const int t = left ? bc.typeL : bc.typeR;
+    return t == HT3D_BC_DIRICHLET ? (left ? bc.gL : bc.gR) - v : v;
+}
+// FP64 ghost (the mixed form keeps T in FP64): 2 value - v in FP64
+__device__ __forceinline__ double weno_ghost(double v, bool left, const WenoBC& bc) {
+    const int t = left ? bc.typeL : bc.typeR;
+    return t == HT3D_BC_DIRICHLET ? 2 * (left ? bc.valL : bc.valR) - v : v;
+}
+
 // --------------------------------------------------------------- streams
 // A stream is the rolling state of one SSP-RK2 stage marching along a line:
 // init() takes x_{i-3} .. x_{i+2} for the first point i, step() takes
@@ -56,6 +72,9 @@ __device__ __forceinline__ float weno_ghost(float v, bool left, const WenoBC& bc
 // point evaluates only its weights: the indicators are computed once per
 // face instead of once per point and side.
 struct WenoStreamShared {
+    using value = float;      // storage and update type
+    using bc_type = WenoBCf;  // its end rules
+    using param = float;      // the grid factor h
     float x[6];   // x_{i-3} .. x_{i+2}
     float D[4];   // D_{i-2} .. D_{i+1}
     float bl[3];  // bL_{i-2} .. bL_i
@@ -161,6 +180,9 @@ struct WenoStreamShared {
 // quirk (whose fifth difference of dF- spans three cells).
 template <int QUIRK>
 struct WenoStreamWindow {
+    using value = float;
+    using bc_type = WenoBCf;
+    using param = float;
     float x[6];
     float h;
     __device__ __forceinline__ void init(const float (&x6)[6], float h_) {
@@ -181,6 +203,151 @@ struct WenoStreamWindow {
 template <int QUIRK> struct StreamOf { using type = WenoStreamWindow<QUIRK>; };
 template <> struct StreamOf<0> { using type = WenoStreamShared; };
 
+// Mixed-precision form of the face-shared stream (the WENO5 stage of the
+// mixed solver, weno5_mixed's split): T, the one-sided differences e (here
+// unscaled, FP64), their second differences a and third differences g, and
+// the central candidate p2 are FP64; the smoothness indicators, the floor and
+// the weights are FP32 from the differences scaled by h and rounded; the
+// weighted corrections (third differences, rounded to FP32) are added to p2
+// in FP64, and the derivative is scaled by h.  Per new face: one FP64
+// difference, one FP64 second and third difference, two conversions; per
+// evaluation: p2 and one addition in FP64 (against six differences, six
+// conversions and two corrections per point and side in the per-point form).
+struct WenoStreamMixed {
+    using value = double;
+    using bc_type = WenoBC;
+    using param = double;
+    double x[6];  // x_{i-3} .. x_{i+2}
+    double E[4];  // e_{i-2} .. e_{i+1} (e_j = x_{j+1} - x_j)
+    double ap;    // a_i
+    float D[4];   // h e, rounded to FP32, same faces
+    float bl[3], bc[2], br, g1[2], g3, e;
+    float hf;
+    double h;
+
+    __device__ __forceinline__ void init(const double (&x6)[6], double h_) {
+        h = h_;
+        hf = (float)h_;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) x[q] = x6[q];
+        double ee[5];
+        float d[5];
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+            ee[q] = x[q + 1] - x[q];  // e_{i-3} .. e_{i+1}
+            d[q] = hf * (float)ee[q];
+        }
+        float a2, a1, a0, u0, u1, u2;
+        WenoStreamShared::triple(d[0], d[1], d[2], a2, bl[0], u0, u1);
+        WenoStreamShared::triple(d[1], d[2], d[3], a1, bl[1], bc[0], u2);
+        WenoStreamShared::triple(d[2], d[3], d[4], a0, bl[2], bc[1], br);
+        const double A2 = __fma_rn(-2.0, ee[1], ee[0]) + ee[2];  // a_{i-2}
+        const double A1 = __fma_rn(-2.0, ee[2], ee[1]) + ee[3];  // a_{i-1}
+        const double A0 = __fma_rn(-2.0, ee[3], ee[2]) + ee[4];  // a_i
+        const float gm = (float)(A1 - A2), g0 = (float)(A0 - A1);
+        g1[0] = gm * (1.0f / 3.0f);
+        g1[1] = g0 * (1.0f / 3.0f);
+        g3 = 0.5f * g0;
+        ap = A0;
+        e = WenoStreamShared::floor5(d[0], d[1], d[2], d[3], d[4]);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            E[q] = ee[q + 1];
+            D[q] = d[q + 1];
+        }
+    }
+
+    __device__ __forceinline__ double back() const { return x[0]; }
+
+    __device__ __forceinline__ double step(double xn, double va, double vb, double dt) {
+        const double en = xn - x[5];  // e_{i+2}
+        const float Dn = hf * (float)en;
+        float af, bL1, bC1, bR1;
+        WenoStreamShared::triple(D[2], D[3], Dn, af, bL1, bC1, bR1);  // centre i+1 (indicators)
+        const double a1 = __fma_rn(-2.0, E[3], E[2]) + en;            // a_{i+1}
+        const float gf = (float)(a1 - ap);                            // g_{i+1}
+        const float G1n = gf * (1.0f / 3.0f), G3n = 0.5f * gf;
+        const float e1 = WenoStreamShared::floor5(D[0], D[1], D[2], D[3], Dn);
+        const double Vm = va < 0.0 ? va : 0.0;
+        const double Vp = vb >= 0.0 ? vb : 0.0;
+        double dFm = 0.0, dFp = 0.0;
+        if (upwind_active(Vp)) {
+            const double p2 = __fma_rn(2.0, E[2], __fma_rn(5.0, E[1], -E[0])) * (1.0 / 6.0);
+            dFm = p2 + (double)WenoStreamShared::mix(bl[0], bc[0], br, e, 0.0f, -g1[0], -g3);
+        }
+        if (upwind_active(Vm)) {
+            const double p2 = __fma_rn(2.0, E[1], __fma_rn(5.0, E[2], -E[3])) * (1.0 / 6.0);
+            dFp = p2 + (double)WenoStreamShared::mix(bR1, bc[1], bl[1], e1, 0.0f, G1n, g3);
+        }
+        const double out = x[3] - dt * (h * (Vp * dFm + Vm * dFp));
+#pragma unroll
+        for (int q = 0; q < 5; ++q) x[q] = x[q + 1];
+        x[5] = xn;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            E[q] = E[q + 1];
+            D[q] = D[q + 1];
+        }
+        E[3] = en;
+        D[3] = Dn;
+        bl[0] = bl[1];
+        bl[1] = bl[2];
+        bl[2] = bL1;
+        bc[0] = bc[1];
+        bc[1] = bC1;
+        br = bR1;
+        g1[0] = g1[1];
+        g1[1] = G1n;
+        g3 = G3n;
+        e = e1;
+        ap = a1;
+        return out;
+    }
+};
+
+// Mixed form from the 7-point window (weno5_mixed per point and side), for
+// the v2 stencil quirk.
+template <int QUIRK>
+struct WenoStreamMixedWindow {
+    using value = double;
+    using bc_type = WenoBC;
+    using param = double;
+    double x[6];
+    double h;
+    __device__ __forceinline__ void init(const double (&x6)[6], double h_) {
+        h = h_;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) x[q] = x6[q];
+    }
+    __device__ __forceinline__ double back() const { return x[0]; }
+    __device__ __forceinline__ double step(double xn, double va, double vb, double dt) {
+        const double Vm = va < 0.0 ? va : 0.0;
+        const double Vp = vb >= 0.0 ? vb : 0.0;
+        const float hf = (float)h;
+        double e[6];
+        float f[6];
+#pragma unroll
+        for (int o = 0; o < 5; ++o) e[o] = x[o + 1] - x[o];
+        e[5] = xn - x[5];
+#pragma unroll
+        for (int o = 0; o < 6; ++o) f[o] = hf * (float)e[o];
+        const double e5 = QUIRK ? x[5] - x[2] : e[4];
+        const float f5 = QUIRK ? hf * (float)e5 : f[4];
+        const double dFm = upwind_active(Vp) ? weno5_mixed(e[0], e[1], e[2], e[3], e5, f[0], f[1], f[2], f[3], f5)
+                                             : 0.0;
+        const double dFp = upwind_active(Vm)
+                               ? weno5_mixed(e[5], e[4], e[3], e[2], e[1], f[5], f[4], f[3], f[2], f[1])
+                               : 0.0;
+        const double out = x[3] - dt * (h * (Vp * dFm + Vm * dFp));
+#pragma unroll
+        for (int q = 0; q < 5; ++q) x[q] = x[q + 1];
+        x[5] = xn;
+        return out;
+    }
+};
+template <int QUIRK> struct MixedStreamOf { using type = WenoStreamMixedWindow<QUIRK>; };
+template <> struct MixedStreamOf<0> { using type = WenoStreamMixed; };
+
 // ------------------------------------------------------------------ march
 // Both stages along the segment [c0, c1) of a line of n cells (Neumann or
 // Dirichlet ends, n >= 3, c1 - c0 >= 3, c0 == 0 or c0 >= 8).  Stage 1 runs
@@ -190,36 +357,28 @@ template <> struct StreamOf<0> { using type = WenoStreamShared; };
 // T[c] = (T0[c] + stage2(T1)[c]) / 2.  Near the line's end T1 beyond it is the
 // mirror of the last three T1 values.
 
-// Dirichlet/Neumann ends of an FP32 sweep: g = (float)(2 * value), so a ghost
-// g - v rounds like the reference's 2 value - v evaluated in FP32.
-struct WenoBCf {
-    int typeL, typeR;
-    float gL, gR;
-};
-__device__ __forceinline__ float weno_ghost(float v, bool left, const WenoBCf& bc) {
-    const int t = left ? bc.typeL : bc.typeR;
-    return t == HT3D_BC_DIRICHLET ? (left ? bc.gL : bc.gR) - v : v;
-}
 
 template <class Stream>
 struct March {
+    using T = typename Stream::value;
+    using BC = typename Stream::bc_type;
     Stream s1, s2;
-    float v0, v1, v2, v3;  // faces c .. c + 3 of the next step
-    float gq0, gq1, gq2;   // tail: the T1 ghosts n, n + 1, n + 2
-    float tq0, tq1, tq2;   // tail: T0[n - 3 .. n - 1]
+    T v0, v1, v2, v3;  // faces c .. c + 3 of the next step
+    T gq0, gq1, gq2;   // tail: the T1 ghosts n, n + 1, n + 2
+    T tq0, tq1, tq2;   // tail: T0[n - 3 .. n - 1]
 
     //   src.t0(q): T0 at q in [c0 - 6, c0 + 6) (ghosts by the BC rule; positions
     //              before -3 only feed discarded points: any finite value)
     //   src.v(f):  face f in [c0 - 3, c0 + 3] (faces < 0: any finite value)
     template <class Src>
-    __device__ __forceinline__ void start(const Src& src, int c0, const WenoBCf& bc, float dt, float h) {
+    __device__ __forceinline__ void start(const Src& src, int c0, const BC& bc, T dt, typename Stream::param h) {
         {
-            float x[6];
+            T x[6];
 #pragma unroll
             for (int q = 0; q < 6; ++q) x[q] = src.t0(c0 - 6 + q);
             s1.init(x, h);
         }
-        float w[6];  // T1[c0 - 3 .. c0 + 2]
+        T w[6];  // T1[c0 - 3 .. c0 + 2]
 #pragma unroll
         for (int r = 0; r < 6; ++r) w[r] = s1.step(src.t0(c0 + r), src.v(c0 - 3 + r), src.v(c0 - 2 + r), dt);
         if (c0 == 0) {
@@ -235,18 +394,18 @@ struct March {
     }
     // step c with its stage-1 point c + 3 inside the line: xa = T0[c + 6]
     // (a ghost past the end), va = face c + 4; returns T[c]
-    __device__ __forceinline__ float step(float xa, float va, float dt) {
-        const float t0c = s1.back();  // T0[c]
-        const float t1 = s1.step(xa, v3, va, dt);
-        const float t = s2.step(t1, v0, v1, dt);
+    __device__ __forceinline__ T step(T xa, T va, T dt) {
+        const T t0c = s1.back();  // T0[c]
+        const T t1 = s1.step(xa, v3, va, dt);
+        const T t = s2.step(t1, v0, v1, dt);
         v0 = v1;
         v1 = v2;
         v2 = v3;
         v3 = va;
-        return 0.5f * t + 0.5f * t0c;
+        return (T)0.5 * t + (T)0.5 * t0c;
     }
     // at c = n - 3: s1 holds T0[n - 3 .. n + 2], s2 T1[n - 6 .. n - 1]
-    __device__ __forceinline__ void tail_enter(const WenoBCf& bc) {
+    __device__ __forceinline__ void tail_enter(const BC& bc) {
         tq0 = s1.x[0];
         tq1 = s1.x[1];
         tq2 = s1.x[2];
@@ -254,9 +413,9 @@ struct March {
         gq1 = weno_ghost(s2.x[4], false, bc);
         gq2 = weno_ghost(s2.x[3], false, bc);
     }
-    __device__ __forceinline__ float tail_step(float dt) {  // c = n - 3, n - 2, n - 1 in turn
-        const float t = s2.step(gq0, v0, v1, dt);
-        const float out = 0.5f * t + 0.5f * tq0;
+    __device__ __forceinline__ T tail_step(T dt) {  // c = n - 3, n - 2, n - 1 in turn
+        const T t = s2.step(gq0, v0, v1, dt);
+        const T out = (T)0.5 * t + (T)0.5 * tq0;
         gq0 = gq1;
         gq1 = gq2;
         tq0 = tq1;
@@ -270,21 +429,22 @@ struct March {
 
 // y or z line straight from HBM (out of place: src -> dst, the inner cells);
 // the read-only loads may move ahead of the stores of earlier steps.
+template <class T, class BC>
 struct LineSrc {
-    const float* line;  // inner cell 0 of the line
-    float* out;
-    const float* vline;  // face 0
+    const T* line;  // inner cell 0 of the line
+    T* out;
+    const T* vline;  // face 0
     long long stride, vs;
     int n;
-    WenoBCf bc;
-    __device__ __forceinline__ float ld(int q) const { return __ldg(line + (long long)q * stride); }
-    __device__ __forceinline__ float t0(int q) const {
+    BC bc;
+    __device__ __forceinline__ T ld(int q) const { return __ldg(line + (long long)q * stride); }
+    __device__ __forceinline__ T t0(int q) const {
         if (q >= 0 && q < n) return ld(q);
-        if (q < -3) return 0.0f;
+        if (q < -3) return (T)0;
         return q < 0 ? weno_ghost(ld(-1 - q), true, bc) : weno_ghost(ld(2 * n - 1 - q), false, bc);
     }
-    __device__ __forceinline__ float v(int f) const { return f >= 0 ? __ldg(vline + (long long)f * vs) : 0.0f; }
-    __device__ __forceinline__ void put(int c, float val) const { out[(long long)c * stride] = val; }
+    __device__ __forceinline__ T v(int f) const { return f >= 0 ? __ldg(vline + (long long)f * vs) : (T)0; }
+    __device__ __forceinline__ void put(int c, T val) const { out[(long long)c * stride] = val; }
 };
 
 // Balanced segments: kMarchL cells per thread on average, at least 48 each
@@ -293,10 +453,13 @@ constexpr int kMarchL = 64;
 constexpr int kMarchUnroll = 4;  // steps per software-pipelined body of the y/z march
 __host__ __device__ __forceinline__ int march_chunks(int n) { return n < 3 * kMarchL / 2 ? 1 : (n + kMarchL / 2) / kMarchL; }
 
-template <int AXIS, int QUIRK>
-__global__ void __launch_bounds__(128) k_weno_march_f32(const float* __restrict__ src, float* __restrict__ dst,
-                                                        const float* __restrict__ V, float dt, float h, WenoBCf bc,
-                                                        int nx, int ny, int nz) {
+template <int AXIS, class Stream>
+__global__ void __launch_bounds__(128) k_weno_march(const typename Stream::value* __restrict__ src,
+                                                    typename Stream::value* __restrict__ dst,
+                                                    const typename Stream::value* __restrict__ V,
+                                                    typename Stream::value dt, typename Stream::param h,
+                                                    typename Stream::bc_type bc, int nx, int ny, int nz) {
+    using T = typename Stream::value;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int o = blockIdx.y;  // k for the y-march, j for the z-march
     const int n = AXIS == 1 ? ny : nz;
@@ -304,7 +467,7 @@ __global__ void __launch_bounds__(128) k_weno_march_f32(const float* __restrict_
     const int c0 = (int)((long long)blockIdx.z * n / K), c1 = (int)((long long)(blockIdx.z + 1) * n / K);
     if (i >= nx) return;
     const int n1 = nx + 2, n2 = ny + 2;
-    LineSrc s;
+    LineSrc<T, typename Stream::bc_type> s;
     s.stride = AXIS == 1 ? (long long)n1 : (long long)n1 * n2;
     const long long first = AXIS == 1 ? (i + 1) + (long long)n1 * (1 + (long long)n2 * (o + 1))
                                       : (i + 1) + (long long)n1 * ((o + 1) + (long long)n2);
@@ -314,7 +477,7 @@ __global__ void __launch_bounds__(128) k_weno_march_f32(const float* __restrict_
     s.vline = AXIS == 1 ? V + i + (long long)nx * (ny + 1) * o : V + i + (long long)nx * o;
     s.n = n;
     s.bc = bc;
-    March<typename StreamOf<QUIRK>::type> M;
+    March<Stream> M;
     M.start(s, c0, bc, dt, h);
     const int cA = c1 < n ? c1 : n - 3;  // steps whose stage-1 point c + 3 is inside the line
     const int cB = min(cA, n - 6);       // ... and whose T0[c + 6] is too
@@ -322,14 +485,14 @@ __global__ void __launch_bounds__(128) k_weno_march_f32(const float* __restrict_
     if (cB - c0 >= 2 * kMarchUnroll) {
         // software pipeline: the T0 and face values of the next kMarchUnroll
         // steps are loaded while the current ones compute
-        float qt[kMarchUnroll], qv[kMarchUnroll];
+        T qt[kMarchUnroll], qv[kMarchUnroll];
 #pragma unroll
         for (int u = 0; u < kMarchUnroll; ++u) {
             qt[u] = s.ld(c + 6 + u);
             qv[u] = s.v(c + 4 + u);
         }
         for (; c + 2 * kMarchUnroll <= cB; c += kMarchUnroll) {
-            float nt[kMarchUnroll], nv[kMarchUnroll];
+            T nt[kMarchUnroll], nv[kMarchUnroll];
 #pragma unroll
             for (int u = 0; u < kMarchUnroll; ++u) {
                 nt[u] = s.ld(c + kMarchUnroll + 6 + u);  // < cB + 6 <= n
@@ -358,40 +521,46 @@ __global__ void __launch_bounds__(128) k_weno_march_f32(const float* __restrict_
 
 // x: a warp marches 32 consecutive rows (one per lane) along x.
 // T0 and Vx reach shared memory through per-row rings of three 8-cell tiles,
-// filled by asynchronous 4-byte copies one tile ahead of the march; a step
-// reads its own row's ring (odd row pitch: the 32 lanes hit 32 banks) and
+// filled by asynchronous element-size copies one tile ahead of the march; a
+// step reads its own row's ring (odd row pitch: the 32 lanes hit 32 banks,
+// 8-byte elements 16 bank pairs per half-warp) and
 // leaves T[c] in the slot of T0[c], which the warp then stores coalesced.
 // Tile u of a segment holds positions b0 + 8u .. b0 + 8u + 7 (b0 = c0 - 8)
 // in ring slot u % 3; the steps c0 + 8v .. c0 + 8v + 7 (block v) read tiles
 // v + 1 and v + 2 and write tile v + 1.
 constexpr int kXW = 8;
 constexpr int kXPitch = 3 * kXW + 1;
-constexpr int kXWarps = 4;
+// warps per block: the rings of one warp take 12.8 KB of 8-byte elements
+template <class T> struct XWarps { static constexpr int value = sizeof(T) == 4 ? 4 : 2; };
 
-__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+template <class T>
+__device__ __forceinline__ void cp_async_el(T* dst, const T* src) {
+    static_assert(sizeof(T) == 4 || sizeof(T) == 8, "4- or 8-byte elements");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src),
+                 "n"((int)sizeof(T))
                  : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
+template <class T, class BC>
 struct RingSrc {
-    float* t;         // this lane's row of the T0 ring
-    const float* vp;  // ... of the Vx ring
+    T* t;         // this lane's row of the T0 ring
+    const T* vp;  // ... of the Vx ring
     int b0, n;
-    WenoBCf bc;
+    BC bc;
     __device__ __forceinline__ int col(int q) const {
         const int d = q - b0;
         return ((d >> 3) % 3) * kXW + (d & 7);
     }
-    __device__ __forceinline__ float t0(int q) const {
+    __device__ __forceinline__ T t0(int q) const {
         if (q >= 0 && q < n) return t[col(q)];
-        if (q < -3) return 0.0f;
+        if (q < -3) return (T)0;
         return q < 0 ? weno_ghost(t[col(-1 - q)], true, bc) : weno_ghost(t[col(2 * n - 1 - q)], false, bc);
     }
-    __device__ __forceinline__ float v(int f) const { return f >= 0 ? vp[col(f)] : 0.0f; }
-    __device__ __forceinline__ void put(int c, float val) const { t[col(c)] = val; }
+    __device__ __forceinline__ T v(int f) const { return f >= 0 ? vp[col(f)] : (T)0; }
+    __device__ __forceinline__ void put(int c, T val) const { t[col(c)] = val; }
 };
 
 // The x sweep updates T in place, so a row is never split between warps:
@@ -399,11 +568,14 @@ struct RingSrc {
 // segment's cells, which another block may already have overwritten.  Within
 // a warp the ring's copies run ahead of its stores (tile v + 4 is fetched
 // after tile v + 1 is stored), so whole rows are safe.
-template <int QUIRK>
-__global__ void __launch_bounds__(32 * kXWarps) k_weno_xstream_f32(float* __restrict__ T, const float* __restrict__ Vx,
-                                                                   float dt, float h, WenoBCf bc, int nx, int ny,
-                                                                   int nz) {
-    __shared__ float ring[kXWarps][2][32 * kXPitch];
+template <class Stream>
+__global__ void __launch_bounds__(32 * XWarps<typename Stream::value>::value)
+    k_weno_xstream(typename Stream::value* __restrict__ T, const typename Stream::value* __restrict__ Vx,
+                   typename Stream::value dt, typename Stream::param h, typename Stream::bc_type bc, int nx, int ny,
+                   int nz) {
+    using E = typename Stream::value;
+    constexpr int kXWarps = XWarps<E>::value;
+    __shared__ E ring[kXWarps][2][32 * kXPitch];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long rows = (long long)ny * nz;
     const long long row0 = ((long long)blockIdx.x * kXWarps + warp) * 32;
@@ -411,8 +583,8 @@ __global__ void __launch_bounds__(32 * kXWarps) k_weno_xstream_f32(float* __rest
     const int n = nx;
     const int c0 = 0, c1 = n;  // whole rows (see above)
     const int b0 = c0 - kXW;
-    float* tr = ring[warp][0];
-    float* vr = ring[warp][1];
+    E* tr = ring[warp][0];
+    E* vr = ring[warp][1];
     // copy lanes: column lane & 7 of rows sub + 4 k (k = 0 .. 7), rows past the
     // last one read the last row and store nothing
     const int sub = lane >> 3, cc = lane & 7;
@@ -429,28 +601,28 @@ __global__ void __launch_bounds__(32 * kXWarps) k_weno_xstream_f32(float* __rest
             rel[k] = (unsigned)(tbase + (long long)(nx + 2) * (r + 2 * (r / ny)) - t0off);
         }
     }
-    const float* Tw = T + t0off;
-    const float* Vw = Vx + (long long)(nx + 1) * row0;
+    const E* Tw = T + t0off;
+    const E* Vw = Vx + (long long)(nx + 1) * row0;
     const int tq_lo = max(0, c0 - 6), tq_hi = min(n, c1 + 6);  // T0 positions a segment reads
     const int vq_lo = max(0, c0 - 3), vq_hi = min(n, c1 + 3);  // faces (inclusive)
     auto load_tile = [&](int u) {
         const int q = b0 + kXW * u + cc;
-        float* td = tr + (u % 3) * kXW + cc;
-        float* vd = vr + (u % 3) * kXW + cc;
+        E* td = tr + (u % 3) * kXW + cc;
+        E* vd = vr + (u % 3) * kXW + cc;
         const bool tq = q >= tq_lo && q < tq_hi, vq = q >= vq_lo && q <= vq_hi;
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
             const int r = sub + 4 * k;
             const long long rv = min(row0 + r, rlast) - row0;
-            if (tq) cp_async4(td + r * kXPitch, Tw + rel[k] + q);
-            if (vq) cp_async4(vd + r * kXPitch, Vw + (nx + 1) * rv + q);
+            if (tq) cp_async_el(td + r * kXPitch, Tw + rel[k] + q);
+            if (vq) cp_async_el(vd + r * kXPitch, Vw + (nx + 1) * rv + q);
         }
         cp_async_commit();
     };
     auto store_tile = [&](int u, int lo, int hi) {  // positions [lo, hi) of tile u
         const int q = b0 + kXW * u + cc;
         if (q < lo || q >= hi) return;
-        const float* ts = tr + (u % 3) * kXW + cc;
+        const E* ts = tr + (u % 3) * kXW + cc;
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
             const int r = sub + 4 * k;
@@ -462,33 +634,33 @@ __global__ void __launch_bounds__(32 * kXWarps) k_weno_xstream_f32(float* __rest
     load_tile(2);
     cp_async_wait<0>();
     __syncwarp();
-    RingSrc src;
+    RingSrc<E, typename Stream::bc_type> src;
     src.t = tr + lane * kXPitch;
     src.vp = vr + lane * kXPitch;
     src.b0 = b0;
     src.n = n;
     src.bc = bc;
-    March<typename StreamOf<QUIRK>::type> M;
+    March<Stream> M;
     M.start(src, c0, bc, dt, h);
     __syncwarp();
     load_tile(3);
     const int cA = c1 < n ? c1 : n - 3;
     for (int v = 0, cb = c0; cb < c1; ++v, cb += kXW) {
-        float* tcur = src.t + ((v + 1) % 3) * kXW;  // positions cb .. cb + 7
-        const float* tnxt = src.t + ((v + 2) % 3) * kXW;
-        const float* vcur = src.vp + ((v + 1) % 3) * kXW;
-        const float* vnxt = src.vp + ((v + 2) % 3) * kXW;
+        E* tcur = src.t + ((v + 1) % 3) * kXW;  // positions cb .. cb + 7
+        const E* tnxt = src.t + ((v + 2) % 3) * kXW;
+        const E* vcur = src.vp + ((v + 1) % 3) * kXW;
+        const E* vnxt = src.vp + ((v + 2) % 3) * kXW;
         if (cb + kXW <= cA && cb + kXW + 6 <= n) {  // eight steps without ghosts
 #pragma unroll
             for (int m = 0; m < kXW; ++m) {
-                const float xa = m + 6 < kXW ? tcur[m + 6] : tnxt[m + 6 - kXW];
-                const float va = m + 4 < kXW ? vcur[m + 4] : vnxt[m + 4 - kXW];
+                const E xa = m + 6 < kXW ? tcur[m + 6] : tnxt[m + 6 - kXW];
+                const E va = m + 4 < kXW ? vcur[m + 4] : vnxt[m + 4 - kXW];
                 tcur[m] = M.step(xa, va, dt);
             }
         } else {
             for (int m = 0; m < kXW && cb + m < c1; ++m) {
                 const int c = cb + m;
-                float out;
+                E out;
                 if (c < cA) {
                     out = M.step(src.t0(c + 6), src.v(c + 4), dt);
                 } else {
@@ -603,9 +775,11 @@ float* axis_f32(ht3d_ctx* ctx, float* cur, float* other, float* tmp, const float
     const bool periodic = bc.typeL == HT3D_BC_PERIODIC || bc.typeR == HT3D_BC_PERIODIC;
     if constexpr (AXIS == 0) {
         if (!periodic) {
-            const long long rows = (long long)ny * nz, per_block = 32LL * kXWarps;
+            using S = typename StreamOf<QUIRK>::type;
+            constexpr int warps = XWarps<float>::value;
+            const long long rows = (long long)ny * nz, per_block = 32LL * warps;
             const dim3 g((unsigned)((rows + per_block - 1) / per_block));
-            HT3D_LAUNCH(ctx, k_weno_xstream_f32<QUIRK>, g, 32 * kXWarps, 0, cur, V, dt, h, bcf(bc), nx, ny, nz);
+            HT3D_LAUNCH(ctx, k_weno_xstream<S>, g, 32 * warps, 0, cur, V, dt, h, bcf(bc), nx, ny, nz);
             return cur;
         }
         const size_t smem = sizeof(float) * 2 * (size_t)(nx + 6) * kRowWarps;
@@ -622,7 +796,8 @@ float* axis_f32(ht3d_ctx* ctx, float* cur, float* other, float* tmp, const float
         if (!periodic) {
             const int n = AXIS == 1 ? ny : nz;
             const dim3 g((nx + 127) / 128, AXIS == 1 ? nz : ny, march_chunks(n));
-            HT3D_LAUNCH(ctx, (k_weno_march_f32<AXIS, QUIRK>), g, 128, 0, cur, other, V, dt, h, bcf(bc), nx, ny, nz);
+            HT3D_LAUNCH(ctx, (k_weno_march<AXIS, typename StreamOf<QUIRK>::type>), g, 128, 0, cur, other, V, dt, h,
+                        bcf(bc), nx, ny, nz);
             return other;
         }
     }
@@ -646,7 +821,33 @@ void all_f32(ht3d_ctx* ctx, float* T, float* S, float* tmp, const float* const* 
     }
 }
 
+// The mixed form's fused sweep (FP64 T, mixed stencils): x in place, y T -> S,
+// z S -> T, every axis one launch (both stages).
+template <int QUIRK>
+void all_mixed(ht3d_ctx* ctx, double* T, double* S, const double* const* V, double dt, const double* h,
+               const WenoBC* bc, int nx, int ny, int nz) {
+    using St = typename MixedStreamOf<QUIRK>::type;
+    constexpr int warps = XWarps<double>::value;
+    const long long rows = (long long)ny * nz, per_block = 32LL * warps;
+    HT3D_LAUNCH(ctx, k_weno_xstream<St>, (unsigned)((rows + per_block - 1) / per_block), 32 * warps, 0, T, V[0], dt,
+                h[0], bc[0], nx, ny, nz);
+    HT3D_LAUNCH(ctx, (k_weno_march<1, St>), dim3((nx + 127) / 128, nz, march_chunks(ny)), 128, 0, T, S, V[1], dt,
+                h[1], bc[1], nx, ny, nz);
+    HT3D_LAUNCH(ctx, (k_weno_march<2, St>), dim3((nx + 127) / 128, ny, march_chunks(nz)), 128, 0, S, T, V[2], dt,
+                h[2], bc[2], nx, ny, nz);
+}
+
 }  // namespace
+
+// Mixed-form WENO5 sweep through the march kernels (weno.cu calls it when no
+// axis is periodic; S: an FP64 field of the ghosted size for the y axis).
+void ht3d_weno5_mixed_march(ht3d_ctx* ctx, double* T, double* S, const double* const* V, double dt, const double* h,
+                            const int* bc_type6, const double* bc_val6, bool quirk, int nx, int ny, int nz) {
+    WenoBC bc[3];
+    for (int a = 0; a < 3; ++a) bc[a] = WenoBC{bc_type6[2 * a], bc_type6[2 * a + 1], bc_val6[2 * a], bc_val6[2 * a + 1]};
+    if (quirk) all_mixed<1>(ctx, T, S, V, dt, h, bc, nx, ny, nz);
+    else all_mixed<0>(ctx, T, S, V, dt, h, bc, nx, ny, nz);
+}
 
 extern "C" int ht3d_weno5_advect_f32(ht3d_ctx* ctx, float* Tc_ex, const float* Vx, const float* Vy, const float* Vz,
                                      double dt, double _dx, double _dy, double _dz, const int* bc_type6,
