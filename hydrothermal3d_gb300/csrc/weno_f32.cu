@@ -203,6 +203,20 @@ struct WenoStreamWindow {
 template <int QUIRK> struct StreamOf { using type = WenoStreamWindow<QUIRK>; };
 template <> struct StreamOf<0> { using type = WenoStreamShared; };
 
+// The upwind factors of an FP64 face velocity, v < 0 ? v : 0 and
+// v >= 0 ? v : 0 (NaN gives 0), from the bit pattern: integer operations
+// instead of two compares on the FP64 pipe.
+__device__ __forceinline__ double neg_part(double v) {
+    const long long b = __double_as_longlong(v);
+    const unsigned long long m = (unsigned long long)b & 0x7fffffffffffffffULL;
+    return (b < 0 && m != 0 && m <= 0x7ff0000000000000ULL) ? v : 0.0;
+}
+__device__ __forceinline__ double pos_part(double v) {
+    const long long b = __double_as_longlong(v);
+    const unsigned long long m = (unsigned long long)b & 0x7fffffffffffffffULL;
+    return (m <= 0x7ff0000000000000ULL && (b >= 0 || m == 0)) ? v : 0.0;
+}
+
 // Mixed-precision form of the face-shared stream (the WENO5 stage of the
 // mixed solver, weno5_mixed's split): T, the one-sided differences e (here
 // unscaled, FP64), their second differences a and third differences g, and
@@ -268,18 +282,17 @@ struct WenoStreamMixed {
         const float gf = (float)(a1 - ap);                            // g_{i+1}
         const float G1n = gf * (1.0f / 3.0f), G3n = 0.5f * gf;
         const float e1 = WenoStreamShared::floor5(D[0], D[1], D[2], D[3], Dn);
-        const double Vm = va < 0.0 ? va : 0.0;
-        const double Vp = vb >= 0.0 ? vb : 0.0;
-        double dFm = 0.0, dFp = 0.0;
+        const double Vm = neg_part(va), Vp = pos_part(vb);
+        double rhs = 0.0;  // Vp dF- + Vm dF+ (unscaled derivatives)
         if (upwind_active(Vp)) {
             const double p2 = __fma_rn(2.0, E[2], __fma_rn(5.0, E[1], -E[0])) * (1.0 / 6.0);
-            dFm = p2 + (double)WenoStreamShared::mix(bl[0], bc[0], br, e, 0.0f, -g1[0], -g3);
+            rhs = Vp * (p2 + (double)WenoStreamShared::mix(bl[0], bc[0], br, e, 0.0f, -g1[0], -g3));
         }
         if (upwind_active(Vm)) {
             const double p2 = __fma_rn(2.0, E[1], __fma_rn(5.0, E[2], -E[3])) * (1.0 / 6.0);
-            dFp = p2 + (double)WenoStreamShared::mix(bR1, bc[1], bl[1], e1, 0.0f, G1n, g3);
+            rhs = __fma_rn(Vm, p2 + (double)WenoStreamShared::mix(bR1, bc[1], bl[1], e1, 0.0f, G1n, g3), rhs);
         }
-        const double out = x[3] - dt * (h * (Vp * dFm + Vm * dFp));
+        const double out = __fma_rn(-(dt * h), rhs, x[3]);  // dt h: loop invariant
 #pragma unroll
         for (int q = 0; q < 5; ++q) x[q] = x[q + 1];
         x[5] = xn;
