@@ -207,9 +207,13 @@ __device__ __forceinline__ void quad_cells(const float4& d, const float4& kx4, c
         float f, xn1;
         mixed_cell(xc, xw, xe, xs, xn, xb, xf, kW, kE, kS, kN, kB, kF, c4(r4, m), c4(dp4, m), mom, dh2, cX, _dx, _dy,
                    _dz, _dx2, _dy2, _dz2, f, xn1);
-        const bool valid = i < p.nx;
-        outD[m] = valid ? xn1 : 0.f;
-        outF[m] = valid ? f : 0.f;
+        outD[m] = xn1;
+        outF[m] = f;
+    }
+    if (i0 + 4 > p.nx) {  // the row's last quad: its padding cells stay zero
+#pragma unroll
+        for (int m = 0; m < 4; ++m)
+            if (i0 + m >= p.nx) outD[m] = outF[m] = 0.f;
     }
     if (!act) return;
     *reinterpret_cast<float4*>(Dio + base) = make_float4(outD[0], outD[1], outD[2], outD[3]);
@@ -457,7 +461,11 @@ __device__ __forceinline__ void pair_quad(const QuadIn& c, float4 xp, float dW, 
                                       _dx2, _dy2, _dz2);
         mixed_cell_rd(xc, xw, xe, xs, xn, xb, xf, c4(c.kW, m), kE, c4(c.kS, m), c4(c.kN, m), c4(c.kB, m),
                       c4(c.kF, m), c4(c.r, m), c4(xp, m), rd[m], s.mom, s.dh2, s.cX, _dx2, _dy2, _dz2, of[m], o[m]);
-        if (i >= p.nx) o[m] = of[m] = 0.f;  // padding stays zero
+    }
+    if (i0 + 4 > p.nx) {  // the row's last quad: its padding cells stay zero
+#pragma unroll
+        for (int m = 0; m < 4; ++m)
+            if (i0 + m >= p.nx) o[m] = of[m] = 0.f;
     }
     if (!HAVE_RD) rd4 = make_float4(rd[0], rd[1], rd[2], rd[3]);
     xout = make_float4(o[0], o[1], o[2], o[3]);
