@@ -798,68 +798,100 @@ __global__ void __launch_bounds__(TX* TY) k_mixed_check(
     double* __restrict__ F64, float* __restrict__ Rin, DyrelScal s, MixScal s32, int prev0, BC6<double> bc, Pad p,
     int zchunk, double* __restrict__ partials) {
     const int nx = p.nx, ny = p.ny, nz = p.nz;
-    const int i = blockIdx.x * TX + threadIdx.x;
-    const int j = blockIdx.y * TY + threadIdx.y;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+    const int i = x0 + tx;
+    const int j = y0 + ty;
     const int k0 = blockIdx.z * zchunk;
     const int k1 = min(nz, k0 + zchunk);
     double acc[3] = {0.0, 0.0, 0.0};
     float rq_num = 0.f, rq_den = 0.f;
-    if (i < nx && j < ny && k0 < k1) {
-        const int n1 = nx + 2, n2 = ny + 2;
-        const long long pl = (long long)n1 * n2, cpl = (long long)nx * ny, pp = p.plane;
-        const long long col = (i + 1) + (long long)n1 * (j + 1);
-        const long long pcol = i + (long long)p.PX * j;
+    // The folds X + D of a plane's tile and of its ring (the row before and
+    // after the tile, the column before and after it) go to shared memory,
+    // two planes deep: a cell's x- and y-neighbours are read there instead
+    // of being folded again (one fold per cell instead of five; the ring
+    // takes three warp instructions).  Every thread of the block runs the
+    // plane loop for the barriers; cells outside the grid do no work.
+    __shared__ double xt[2][TY + 2][TX + 2];
+    const bool act = i < nx && j < ny;
+    const int n1 = nx + 2, n2 = ny + 2;
+    const long long pl = (long long)n1 * n2, cpl = (long long)nx * ny, pp = p.plane;
+    // fold of inner cell (ii, jj) at plane kk
+    auto fold_at = [&](int ii, int jj, int kk) {
+        return Xin[(ii + 1) + (long long)n1 * (jj + 1) + pl * (kk + 1)] +
+               (double)Din[ii + (long long)p.PX * jj + pp * kk];
+    };
+    // ring cell of this thread, if any: warp 0 the row y0 - 1, warp TY - 1 the
+    // row y0 + TY, warp 1 the columns x0 - 1 (lanes 0 .. TY-1) and x0 + TX
+    // (lanes TY .. 2 TY - 1)
+    int ri = -1, rj = -1, rs = 0, rc = 0;  // cell, and its slot in the tile
+    if (ty == 0 && i < nx && y0 > 0) { ri = i; rj = y0 - 1; rs = 0; rc = tx + 1; }
+    else if (ty == TY - 1 && i < nx && y0 + TY < ny) { ri = i; rj = y0 + TY; rs = TY + 1; rc = tx + 1; }
+    else if (ty == 1 && tx < TY && x0 > 0 && y0 + tx < ny) { ri = x0 - 1; rj = y0 + tx; rs = tx + 1; rc = 0; }
+    else if (ty == 1 && tx >= TY && tx < 2 * TY && x0 + TX < nx && y0 + tx - TY < ny) {
+        ri = x0 + TX; rj = y0 + tx - TY; rs = tx - TY + 1; rc = TX + 1;
+    }
+    if (k0 < k1) {
+        const int ic = act ? i : 0, jc = act ? j : 0;  // cells outside the grid address cell (0, 0)
+        const long long col = (ic + 1) + (long long)n1 * (jc + 1);
+        const long long pcol = ic + (long long)p.PX * jc;
         const double* xcol = Xin + col;
         const float* dcol = Din + pcol;
         double* ocol = Xout + col;
-        const long long ccol = i + (long long)nx * j;
-        const double* kxcol = kx + i + (long long)(nx + 1) * j;
-        const double* kycol = ky + i + (long long)nx * j;
+        const long long ccol = ic + (long long)nx * jc;
+        const double* kxcol = kx + ic + (long long)(nx + 1) * jc;
+        const double* kycol = ky + ic + (long long)nx * jc;
         const double* kzcol = kz + ccol;
         auto fold = [&](long long e, long long pe) { return xcol[e] + (double)dcol[pe]; };
-        double xc = fold(pl * (k0 + 1), pp * k0);
-        double xb = (k0 == 0) ? ghost(bc, 4, xc) : fold(pl * k0, pp * (k0 - 1));
-        double qB = -kzcol[cpl * k0] * (s._dz * (xc - xb));
+        double xc = act ? fold(pl * (k0 + 1), pp * k0) : 0.0;
+        double xb = (!act || k0 == 0) ? ghost(bc, 4, xc) : fold(pl * k0, pp * (k0 - 1));
+        double qB = act ? -kzcol[cpl * k0] * (s._dz * (xc - xb)) : 0.0;
         for (int k = k0; k < k1; ++k) {
-            const long long e = pl * (k + 1), pe = pp * k;
-            const double xf = (k == nz - 1) ? ghost(bc, 5, xc) : fold(e + pl, pe + pp);
-            const double xw = (i == 0) ? ghost(bc, 0, xc) : fold(e - 1, pe - 1);
-            const double xe = (i == nx - 1) ? ghost(bc, 1, xc) : fold(e + 1, pe + 1);
-            const double xs = (j == 0) ? ghost(bc, 2, xc) : fold(e - n1, pe - p.PX);
-            const double xn = (j == ny - 1) ? ghost(bc, 3, xc) : fold(e + n1, pe + p.PX);
-            const long long c = ccol + cpl * k, pc = pcol + pe;
-            const double qF = -kzcol[cpl * (k + 1)] * (s._dz * (xf - xc));
-            const long long fxo = (long long)(nx + 1) * ny * k, fyo = (long long)nx * (ny + 1) * k;
-            const double qW = -kxcol[fxo] * (s._dx * (xc - xw));
-            const double qE = -kxcol[fxo + 1] * (s._dx * (xe - xc));
-            const double qS = -kycol[fyo] * (s._dy * (xc - xs));
-            const double qN = -kycol[fyo + nx] * (s._dy * (xn - xc));
-            const double fu = R[c] + s.cX * xc + s._dx * (qE - qW) + s._dy * (qN - qS) + s._dz * (qF - qB);
-            const double f = fu * invPC[c];
-            const float f32 = (float)f;
-            const float dprev = prev0 ? 0.f : Dio[pc];
-            const float f0old = __fdiv_rn(__fsub_rn(dprev, dcol[pe]), s32.dtau_prev);
-            const float f0 = __fmaf_rn(s32.h1, f0old, __fmul_rn(s32.h2, f32));
-            const float d = __fmul_rn(s32.dtau, f0);
-            if (CHECK) {
-                acc[0] += fabs(fu);
-                rq_num = __fmaf_rn(-d, __fsub_rn(f32, F32[pc]), rq_num);
-                rq_den = __fmaf_rn(d, d, rq_den);
-                F64[c] = f;
+            const int b = k & 1;
+            xt[b][ty + 1][tx + 1] = xc;
+            if (ri >= 0) xt[b][rs][rc] = fold_at(ri, rj, k);
+            __syncthreads();  // also orders the reads of plane k - 2 (same buffer) before these writes
+            if (act) {
+                const long long e = pl * (k + 1), pe = pp * k;
+                const double xf = (k == nz - 1) ? ghost(bc, 5, xc) : fold(e + pl, pe + pp);
+                const double xw = (i == 0) ? ghost(bc, 0, xc) : xt[b][ty + 1][tx];
+                const double xe = (i == nx - 1) ? ghost(bc, 1, xc) : xt[b][ty + 1][tx + 2];
+                const double xs = (j == 0) ? ghost(bc, 2, xc) : xt[b][ty][tx + 1];
+                const double xn = (j == ny - 1) ? ghost(bc, 3, xc) : xt[b][ty + 2][tx + 1];
+                const long long c = ccol + cpl * k, pc = pcol + pe;
+                const double qF = -kzcol[cpl * (k + 1)] * (s._dz * (xf - xc));
+                const long long fxo = (long long)(nx + 1) * ny * k, fyo = (long long)nx * (ny + 1) * k;
+                const double qW = -kxcol[fxo] * (s._dx * (xc - xw));
+                const double qE = -kxcol[fxo + 1] * (s._dx * (xe - xc));
+                const double qS = -kycol[fyo] * (s._dy * (xc - xs));
+                const double qN = -kycol[fyo + nx] * (s._dy * (xn - xc));
+                const double fu = R[c] + s.cX * xc + s._dx * (qE - qW) + s._dy * (qN - qS) + s._dz * (qF - qB);
+                const double f = fu * invPC[c];
+                const float f32 = (float)f;
+                const float dprev = prev0 ? 0.f : Dio[pc];
+                const float f0old = __fdiv_rn(__fsub_rn(dprev, dcol[pe]), s32.dtau_prev);
+                const float f0 = __fmaf_rn(s32.h1, f0old, __fmul_rn(s32.h2, f32));
+                const float d = __fmul_rn(s32.dtau, f0);
+                if (CHECK) {
+                    acc[0] += fabs(fu);
+                    rq_num = __fmaf_rn(-d, __fsub_rn(f32, F32[pc]), rq_num);
+                    rq_den = __fmaf_rn(d, d, rq_den);
+                    F64[c] = f;
+                }
+                F32[pc] = f32;
+                Rin[pc] = (float)fu;
+                Dio[pc] = -d;
+                ocol[e] = xc;
+                if (i == 0) ocol[e - 1] = xw;
+                if (i == nx - 1) ocol[e + 1] = xe;
+                if (j == 0) ocol[e - n1] = xs;
+                if (j == ny - 1) ocol[e + n1] = xn;
+                if (k == 0) ocol[e - pl] = xb;
+                if (k == nz - 1) ocol[e + pl] = xf;
+                xb = xc;
+                xc = xf;
+                qB = qF;
             }
-            F32[pc] = f32;
-            Rin[pc] = (float)fu;
-            Dio[pc] = -d;
-            ocol[e] = xc;
-            if (i == 0) ocol[e - 1] = xw;
-            if (i == nx - 1) ocol[e + 1] = xe;
-            if (j == 0) ocol[e - n1] = xs;
-            if (j == ny - 1) ocol[e + n1] = xn;
-            if (k == 0) ocol[e - pl] = xb;
-            if (k == nz - 1) ocol[e + pl] = xf;
-            xb = xc;
-            xc = xf;
-            qB = qF;
         }
     }
     if (!CHECK) return;
