@@ -506,15 +506,26 @@ __global__ void __launch_bounds__(TB_LANES* TB_Y, TB_Y <= 8 ? 2 : 1) k_mixed_inn
     // A's 1 / diag, three planes, at kTbRd floats after the result of the same plane
     uint64_t* bar = reinterpret_cast<uint64_t*>(base + sizeof(TbStage) * TB_STAGES + sizeof(float) * 2 * kTbRd);
     __shared__ int abort_flag;
+    // A's end-cell results of the last three planes ([plane % 3][west, east][row]):
+    // B of plane pl - 1 reads slot (pl - 1) % 3 after the CTA barrier of plane
+    // pl, and warp 0 writes it again at plane pl + 2, after the barrier of
+    // plane pl + 1, which every warp passes after its B of plane pl - 1
+    __shared__ float ebuf[3][2][TB_Y];
     const int lane = threadIdx.x, ty = threadIdx.y, tid = lane + TB_LANES * ty;
     const int x0 = blockIdx.x * TB_OX, y0 = blockIdx.y * TB_OY - 1;  // tile origin (x0 % 4 == 0)
     const int i0 = x0 + 4 * lane, j = y0 + ty;
     const bool rowin = j >= 0 && j < p.PY && i0 < p.PX;  // quad inside the padded array
     const bool inner = i0 < p.nx && j >= 0 && j < p.ny && ty >= 1 && ty <= TB_Y - 2;
-    // end cells: lane 0 computes x0 - 1, lane 31 x0 + TB_X (iteration A only)
-    const bool endc = lane == 0 || lane == TB_LANES - 1;
-    const int ie = lane == 0 ? x0 - 1 : x0 + TB_X;
-    const int ce = lane == 0 ? 3 : TB_X + 4;  // its column in the boxes
+    // end cells (iteration A only): the columns x0 - 1 and x0 + TB_X of the
+    // tile's rows, all computed by warp 0, which runs no iteration B: lane l
+    // takes row l % TB_Y, its west end for l < TB_Y and its east end above.
+    // Their results reach the warps' iteration B through ebuf.
+    static_assert(2 * TB_Y <= TB_LANES, "one end cell per lane of warp 0");
+    const bool endc = ty == 0 && lane < 2 * TB_Y;
+    const int er = lane % TB_Y, ej = y0 + er;  // its row
+    const int eside = lane < TB_Y ? 0 : 1;
+    const int ie = eside ? x0 + TB_X : x0 - 1;
+    const int ce = eside ? TB_X + 4 : 3;  // its column in the boxes
     const int k0 = blockIdx.z * zchunk, k1 = min(p.nz, k0 + zchunk);
     const int pa0 = max(k0 - 1, 0);
     const int plast = min(k1 + 1, p.nz);  // last staged plane (plane nz: its bottom z-faces)
@@ -562,9 +573,8 @@ __global__ void __launch_bounds__(TB_LANES* TB_Y, TB_Y <= 8 ? 2 : 1) k_mixed_inn
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
     float4 dm1 = (pa0 > 0 && rowin) ? *reinterpret_cast<const float4*>(Din + p.plane * (pa0 - 1) + colo) : z4;
     // the end cell's D at the plane before, and its A result at the plane before
-    const bool endin = endc && j >= 0 && j < p.PY && ie >= 0 && ie < p.PX;
-    float em1 = (pa0 > 0 && endin) ? Din[p.plane * (pa0 - 1) + ie + (long long)p.PX * j] : 0.f;
-    float ec = 0.f;
+    const bool endin = endc && ej >= 0 && ej < p.PY && ie >= 0 && ie < p.PX;
+    float em1 = (pa0 > 0 && endin) ? Din[p.plane * (pa0 - 1) + ie + (long long)p.PX * ej] : 0.f;
     float4 dpm = z4, dpc = z4;  // A's result at planes pl - 2 and pl - 1
     QuadIn cb{};                // A's inputs at plane pl - 1 (B's coefficients)
     for (int pl = pa0; pl <= k1; ++pl) {
@@ -617,13 +627,13 @@ __global__ void __launch_bounds__(TB_LANES* TB_Y, TB_Y <= 8 ? 2 : 1) k_mixed_inn
             *reinterpret_cast<float4*>(xw_) = da;
             *reinterpret_cast<float4*>(xw_ + kTbRd) = rda;
         }
-        float ea = 0.f;  // the end cell's A result at plane pl
         if (ok && pl < p.nz && endc) {
-            const int oe = ty * TB_W + ce;
-            const float* de = &S0->D[0][0] + (ty + 1) * TB_W + ce;
-            ea = pair_cell(de, &S0->kx[0][0] + oe, &S0->ky[0][0] + oe, (&S0->kz[0][0])[oe], (&S1->kz[0][0])[oe],
-                           (&S0->R[0][0])[oe], (&S0->Dp[0][0])[oe], em1, (&S1->D[0][0])[(ty + 1) * TB_W + ce], ie, j,
-                           pl, p, bc, s, _dx2, _dy2, _dz2);
+            const int oe = er * TB_W + ce;
+            const float* de = &S0->D[0][0] + (er + 1) * TB_W + ce;
+            ebuf[pl % 3][eside][er] =
+                pair_cell(de, &S0->kx[0][0] + oe, &S0->ky[0][0] + oe, (&S0->kz[0][0])[oe], (&S1->kz[0][0])[oe],
+                          (&S0->R[0][0])[oe], (&S0->Dp[0][0])[oe], em1, (&S1->D[0][0])[(er + 1) * TB_W + ce], ie, ej,
+                          pl, p, bc, s, _dx2, _dy2, _dz2);
             em1 = de[0];
         }
         __syncthreads();
@@ -641,8 +651,8 @@ __global__ void __launch_bounds__(TB_LANES* TB_Y, TB_Y <= 8 ? 2 : 1) k_mixed_inn
         // every lane takes part in the shuffles
         float bW = __shfl_up_sync(0xffffffffu, dpc.w, 1);
         float bE = __shfl_down_sync(0xffffffffu, dpc.x, 1);
-        if (lane == 0) bW = ec;
-        if (lane == TB_LANES - 1) bE = ec;
+        if (lane == 0) bW = ebuf[(pl + 2) % 3][0][ty];  // slot (pl - 1) % 3
+        if (lane == TB_LANES - 1) bE = ebuf[(pl + 2) % 3][1][ty];
         if (pl - 1 >= k0 && inner) {
             const int q = pl - 1;
             QuadIn c = cb;
@@ -660,7 +670,6 @@ __global__ void __launch_bounds__(TB_LANES* TB_Y, TB_Y <= 8 ? 2 : 1) k_mixed_inn
         outF += p.plane;
         dpm = dpc;
         dpc = da;
-        ec = ea;
         cb = ca;
         const TbStage* t = S0;
         S0 = S1;
