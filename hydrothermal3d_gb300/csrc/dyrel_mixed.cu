@@ -581,8 +581,9 @@ __global__ void __launch_bounds__(TB_LANES* TB_Y, TB_Y <= 8 ? 2 : 1) k_mixed_inn
         if (pl + 2 <= plast) {
             // slot (pl + 2) % 3 was last read by iteration A of planes pl - 1 and
             // pl - 2, which every warp finished before the CTA barrier of the
-            // previous plane
-            if (tid == 0) {
+            // previous plane.  Lane 0 of the last warp issues (that warp runs
+            // no iteration B; warp 0 computes the end cells).
+            if (tid == TB_LANES * (TB_Y - 1)) {
                 // order the earlier generic reads of this slot before the async-proxy writes
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 issue(pl + 2);
@@ -590,20 +591,16 @@ __global__ void __launch_bounds__(TB_LANES* TB_Y, TB_Y <= 8 ? 2 : 1) k_mixed_inn
             issued = pl + 2;
         }
         // planes pl and pl + 1 have landed (phase = number of earlier uses of the
-        // slot): lane 0 of every warp polls the barriers, __syncwarp then orders
-        // the copied data for the warp's other lanes.  A warp runs at most one
-        // plane ahead of another (one CTA barrier per plane), so the phase it
-        // waits for is always the slot's next one.
+        // slot): every lane waits on the barriers itself, which also makes the
+        // copied data visible to it.  Plane pl was waited for as plane pl + 1
+        // of the previous iteration (pl <= plast throughout).  A warp runs at
+        // most one plane ahead of another (one CTA barrier per plane), so the
+        // phase it waits for is always the slot's next one.
         bool ok = true;
-        if (lane == 0) {
-            ok = mbar_wait_bounded(&bar[pl % TB_STAGES], ((pl - pa0) / TB_STAGES) & 1, detect_limit);
-            if (pl + 1 <= plast)
-                ok = ok && mbar_wait_bounded(&bar[(pl + 1) % TB_STAGES], ((pl + 1 - pa0) / TB_STAGES) & 1,
-                                             detect_limit);
-            if (!ok) abort_flag = 1;
-        }
-        ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
-        __syncwarp();
+        if (pl == pa0) ok = mbar_wait_bounded(&bar[pl % TB_STAGES], 0, detect_limit);
+        if (pl + 1 <= plast)
+            ok = ok && mbar_wait_bounded(&bar[(pl + 1) % TB_STAGES], ((pl + 1 - pa0) / TB_STAGES) & 1, detect_limit);
+        if (!ok) abort_flag = 1;
         // ---- A: iteration n at plane pl, every quad of the halo tile
         QuadIn ca{};
         float4 da = z4;
