@@ -797,7 +797,7 @@ __global__ void __launch_bounds__(BS) k_ens_march(const __grid_constant__ EnsLau
 // (D has been folded into X).  CHECK = false (a refresh between the
 // reference's checks) skips the check sums and the FP64 F.
 template <bool CHECK>
-__global__ void __launch_bounds__(TX* TY) k_mixed_check(
+__global__ void __launch_bounds__(TX* TY, 3) k_mixed_check(
     const double* __restrict__ Xin, double* __restrict__ Xout, const float* __restrict__ Din, float* __restrict__ Dio,
     const double* __restrict__ R, const double* __restrict__ kx, const double* __restrict__ ky,
     const double* __restrict__ kz, const double* __restrict__ invPC, float* __restrict__ F32,
@@ -854,33 +854,50 @@ __global__ void __launch_bounds__(TX* TY) k_mixed_check(
         double qB = act ? -kzcol[cpl * k0] * (s._dz * (xc - xb)) : 0.0;
         for (int k = k0; k < k1; ++k) {
             const int b = k & 1;
+            // the plane's per-cell loads go out before the barrier, so their
+            // latency overlaps it (each address is read, and later written,
+            // by this thread alone)
+            const long long e = pl * (k + 1), pe = pp * k;
+            const long long c = ccol + cpl * k, pc = pcol + pe;
+            const long long fxo = (long long)(nx + 1) * ny * k, fyo = (long long)nx * (ny + 1) * k;
+            double gR = 0.0, gI = 0.0, gkF = 0.0, gkW = 0.0, gkE = 0.0, gkS = 0.0, gkN = 0.0, xnext = 0.0;
+            float gDp = 0.f, gD = 0.f, gF = 0.f;
+            if (act) {
+                gR = R[c];
+                gI = invPC[c];
+                gkF = kzcol[cpl * (k + 1)];
+                gkW = kxcol[fxo];
+                gkE = kxcol[fxo + 1];
+                gkS = kycol[fyo];
+                gkN = kycol[fyo + nx];
+                gDp = prev0 ? 0.f : Dio[pc];
+                gD = dcol[pe];
+                if (CHECK) gF = F32[pc];
+                if (k != nz - 1) xnext = fold(e + pl, pe + pp);
+            }
             xt[b][ty + 1][tx + 1] = xc;
             if (ri >= 0) xt[b][rs][rc] = fold_at(ri, rj, k);
             __syncthreads();  // also orders the reads of plane k - 2 (same buffer) before these writes
             if (act) {
-                const long long e = pl * (k + 1), pe = pp * k;
-                const double xf = (k == nz - 1) ? ghost(bc, 5, xc) : fold(e + pl, pe + pp);
+                const double xf = (k == nz - 1) ? ghost(bc, 5, xc) : xnext;
                 const double xw = (i == 0) ? ghost(bc, 0, xc) : xt[b][ty + 1][tx];
                 const double xe = (i == nx - 1) ? ghost(bc, 1, xc) : xt[b][ty + 1][tx + 2];
                 const double xs = (j == 0) ? ghost(bc, 2, xc) : xt[b][ty][tx + 1];
                 const double xn = (j == ny - 1) ? ghost(bc, 3, xc) : xt[b][ty + 2][tx + 1];
-                const long long c = ccol + cpl * k, pc = pcol + pe;
-                const double qF = -kzcol[cpl * (k + 1)] * (s._dz * (xf - xc));
-                const long long fxo = (long long)(nx + 1) * ny * k, fyo = (long long)nx * (ny + 1) * k;
-                const double qW = -kxcol[fxo] * (s._dx * (xc - xw));
-                const double qE = -kxcol[fxo + 1] * (s._dx * (xe - xc));
-                const double qS = -kycol[fyo] * (s._dy * (xc - xs));
-                const double qN = -kycol[fyo + nx] * (s._dy * (xn - xc));
-                const double fu = R[c] + s.cX * xc + s._dx * (qE - qW) + s._dy * (qN - qS) + s._dz * (qF - qB);
-                const double f = fu * invPC[c];
+                const double qF = -gkF * (s._dz * (xf - xc));
+                const double qW = -gkW * (s._dx * (xc - xw));
+                const double qE = -gkE * (s._dx * (xe - xc));
+                const double qS = -gkS * (s._dy * (xc - xs));
+                const double qN = -gkN * (s._dy * (xn - xc));
+                const double fu = gR + s.cX * xc + s._dx * (qE - qW) + s._dy * (qN - qS) + s._dz * (qF - qB);
+                const double f = fu * gI;
                 const float f32 = (float)f;
-                const float dprev = prev0 ? 0.f : Dio[pc];
-                const float f0old = __fdiv_rn(__fsub_rn(dprev, dcol[pe]), s32.dtau_prev);
+                const float f0old = __fdiv_rn(__fsub_rn(gDp, gD), s32.dtau_prev);
                 const float f0 = __fmaf_rn(s32.h1, f0old, __fmul_rn(s32.h2, f32));
                 const float d = __fmul_rn(s32.dtau, f0);
                 if (CHECK) {
                     acc[0] += fabs(fu);
-                    rq_num = __fmaf_rn(-d, __fsub_rn(f32, F32[pc]), rq_num);
+                    rq_num = __fmaf_rn(-d, __fsub_rn(f32, gF), rq_num);
                     rq_den = __fmaf_rn(d, d, rq_den);
                     F64[c] = f;
                 }
