@@ -335,8 +335,8 @@ __global__ void __launch_bounds__(HT3D_MIX_BS, HT3D_MIX_MINB) k_mixed_inner(cons
 // y0 + w, lane l the quad of cells x0 + 4l .. x0 + 4l + 3, as in
 // k_mixed_inner.  Marching through a chunk of zchunk planes it computes
 //   A: iteration n on every cell of the tile and on one cell past each end
-//      of its rows (lane 0 the cell x0 - 1, lane 31 the cell x0 + TB_X),
-//      plane p;
+//      of its rows (the cells x0 - 1 and x0 + TB_X of every row, all of
+//      them computed by warp 0, one per lane), plane p;
 //   B: iteration n+1 on the cells of the inner rows (warps 1..TB_Y-2) of
 //      plane p-1 from D' of planes p-2 (registers), p-1 (own quad in
 //      registers, x-neighbours by warp shuffles or the end cells,
@@ -534,7 +534,7 @@ __global__ void __launch_bounds__(TB_LANES* TB_Y, TB_Y <= 8 ? 2 : 1) k_mixed_inn
     const int oD = (ty + 1) * TB_W + 4 + 4 * lane;  // D, quad centre
     const int oK = ty * TB_W + 4 + 4 * lane;        // kx, ky (south), kz, R, Dp
     const int oC = ty * TB_X + 4 * lane;            // the A-result planes
-    auto issue = [&](int k) {  // thread 0: the six boxes of plane k into slot k % TB_STAGES
+    auto issue = [&](int k) {  // one thread: the six boxes of plane k into slot k % TB_STAGES
         if (k == skip_plane) return;  // HT3D_TUNE_WAIT_TEST only: never issued, its wait runs out
         TbStage& S = st[k % TB_STAGES];
         uint64_t* b = &bar[k % TB_STAGES];
