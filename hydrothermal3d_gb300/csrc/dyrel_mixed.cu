@@ -34,7 +34,10 @@ namespace {
 //
 // Element (i, j, k) of every FP32 field (corrections D and Dprev, FP32
 // residual Rin, F, face conductivities) sits at i + PX*(j + PY*k) with
-// PX = nx+1 rounded up to 32 (128-byte rows), PY = ny+1 and nz+1 planes.  One
+// PX = nx+1 rounded up to 8 (rows of whole 32-byte sectors, so every quad is
+// 16-byte aligned and every tensor-map stride a multiple of 16 bytes; rounding
+// to 32 cost the 31-95-cell ensemble members about a fifth of their bytes in
+// padding), PY = ny+1 and nz+1 planes.  One
 // index therefore addresses a cell, its west x-face, its south y-face and its
 // bottom z-face; the east/north/front faces are +1, +PX, +PX*PY.  There is no
 // ghost storage: ghosts are evaluated from the BCs.  Padding stays zero.
@@ -46,7 +49,7 @@ struct Pad {
 inline Pad make_pad(int nx, int ny, int nz) {
     Pad p;
     p.nx = nx; p.ny = ny; p.nz = nz;
-    p.PX = ((nx + 1 + 31) / 32) * 32;
+    p.PX = ((nx + 1 + 7) / 8) * 8;
     p.PY = ny + 1;
     p.nq = (nx + 3) / 4;
     p.plane = (long long)p.PX * p.PY;
