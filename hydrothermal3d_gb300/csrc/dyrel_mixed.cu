@@ -651,8 +651,10 @@ __global__ void __launch_bounds__(TB_LANES* TB_Y, TB_Y <= 8 ? 2 : 1) k_mixed_inn
         // every lane takes part in the shuffles
         float bW = __shfl_up_sync(0xffffffffu, dpc.w, 1);
         float bE = __shfl_down_sync(0xffffffffu, dpc.x, 1);
-        if (lane == 0) bW = ebuf[(pl + 2) % 3][0][ty];  // slot (pl - 1) % 3
-        if (lane == TB_LANES - 1) bE = ebuf[(pl + 2) % 3][1][ty];
+        // slot (pl - 1) % 3, written by warp 0 at plane pl - 1 (only read when
+        // B runs: the first plane of a chunk has no such slot yet)
+        if (lane == 0 && pl - 1 >= k0) bW = ebuf[(pl + 2) % 3][0][ty];
+        if (lane == TB_LANES - 1 && pl - 1 >= k0) bE = ebuf[(pl + 2) % 3][1][ty];
         if (pl - 1 >= k0 && inner) {
             const int q = pl - 1;
             QuadIn c = cb;
